@@ -1,0 +1,215 @@
+/*
+ * uww.h -- C ABI of the GB300 chunk-generation library (libuww_gb300.so).
+ *
+ * It replaces the terrain chunk builder of LelsersLasers/UnderwaterWorld:
+ *   - noise::Perlin::new(seed)                      (underwater_world/src/state.rs:359)
+ *   - perlin_util::perlin_3d_octaves / iso_at       (underwater_world/src/perlin_util.rs:6-29)
+ *   - Chunk::new / build_full / build_partial       (underwater_world/src/chunk.rs:89-103,266-313)
+ *     with build_iso, early_blank_check, build_mesh (chunk.rs:105-264)
+ *   - Chunk::not_blank / verts_buffer_slice / inds_buffer_slice / num_inds (chunk.rs:344-348)
+ *   - draw::VertColor                               (underwater_world/src/draw.rs:4-33)
+ *
+ * Every call returns an int status (UWW_OK == 0).  Device-pointer calls are
+ * asynchronous on the context's stream; the *_host calls copy in, build, copy
+ * out and synchronise.  A context is not re-entrant: one host thread at a time.
+ * No call falls back to the CPU: without a CUDA device they return
+ * UWW_ERR_CUDA.
+ */
+#ifndef UWW_H
+#define UWW_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define UWW_ABI_VERSION 1
+
+/* ---- status codes --------------------------------------------------------- */
+#define UWW_OK               0
+#define UWW_ERR_INVALID_ARG  1  /* bad pointer, size, LOD or parameter          */
+#define UWW_ERR_CUDA         2  /* CUDA runtime error (no device, launch fault) */
+#define UWW_ERR_CAPACITY     3  /* outputs did not fit; counts are valid, grow and rebuild */
+#define UWW_ERR_OOM          4  /* device or host allocation failed             */
+#define UWW_ERR_TIMEOUT      5  /* a bounded device-side wait gave up           */
+
+/* ---- limits ---------------------------------------------------------------- */
+#define UWW_MAX_OCTAVES 16
+#define UWW_MAX_CELLS   64      /* cells per chunk edge; 12, 24, 48 are the LODs used */
+
+/* ---- parameter enums ------------------------------------------------------ */
+#define UWW_BIAS_NONE      0    /* density = fBm                                       */
+#define UWW_BIAS_TERRACED  1    /* iso_at: adj = (nz*a)/b; d = (adj + fBm) - fmod(adj, c)  (perlin_util.rs:24-29) */
+#define UWW_BIAS_LINEAR    2    /* d = fBm + a*(world_z - b)                           */
+
+#define UWW_MATH_EXACT 0        /* reference f32 operation order, no FMA contraction (parity build) */
+#define UWW_MATH_FAST  1        /* FMA-contracted, table-driven noise (fast build)                  */
+
+#define UWW_DEDUP_ORIENTED 0    /* reference: one vertex per ordered corner pair (chunk.rs:233) */
+#define UWW_DEDUP_EDGE     1    /* one vertex per cube edge (both orientations share it)       */
+
+#define UWW_OUT_COLOR    1u     /* VertColor.color (sRGB depth ramp, chunk.rs:212-219)      */
+#define UWW_OUT_NORMALS  2u     /* per-vertex unit normal from the analytic density gradient */
+#define UWW_OUT_CASES    4u     /* per-cell 8-bit marching-cubes case index                  */
+#define UWW_OUT_SAMPLES  8u     /* the (cells+1)^3 f32 density samples (Build::isos, chunk.rs:43) */
+
+/* ---- chunk flags (uww_chunk_record.flags) --------------------------------- */
+#define UWW_CHUNK_EARLY_BLANK 1u  /* every sample above the iso-level: early_blank_check (chunk.rs:131-133) */
+#define UWW_CHUNK_HAS_MESH    2u  /* num_inds > 0: Chunk::not_blank (chunk.rs:344)                          */
+#define UWW_CHUNK_OVERFLOW    4u  /* this chunk's mesh did not fit the output capacity; not written          */
+
+/* World / density parameters.  uww_params_reference() fills the constants of
+ * chunk.rs:5-17, perlin_util.rs:6-29 and world.rs:11-12. */
+typedef struct uww_params {
+    uint32_t seed;          /* permutation seed, noise::Perlin::new(seed) (state.rs:359)        */
+    uint32_t octaves;       /* PERLIN_OCTAVES = 3 (chunk.rs:9); 1..UWW_MAX_OCTAVES             */
+    int32_t  chunk_size;    /* CHUNK_SIZE = 16 world units per chunk edge (chunk.rs:5)         */
+    float    base_freq;     /* noise units per world unit; 1/16 (chunk.rs:108: /CHUNK_SIZE)    */
+    float    lacunarity;    /* frequency *= 2.0 (perlin_util.rs:19)                            */
+    float    persistence;   /* amplitude *= 0.5 (perlin_util.rs:18)                            */
+    float    amplitude;     /* first-octave amplitude, 1.0 (perlin_util.rs:9)                  */
+    int32_t  normalize;     /* 1: total / sum(amplitudes) (perlin_util.rs:21)                  */
+    int32_t  bias_mode;     /* UWW_BIAS_*                                                      */
+    float    bias_a;        /* terraced: CHUNK_SIZE (16); linear: slope per world unit          */
+    float    bias_b;        /* terraced: MAX_HEIGHT (32); linear: z0 in world units             */
+    float    bias_c;        /* terraced: ADJ_Z_MOD (0.25); linear: unused                       */
+    float    iso_level;     /* ISO_LEVEL = -0.1 (chunk.rs:10); case bit i set when d_i < iso   */
+    float    offset[3];     /* world-space offset added to the noise input (0 in the reference) */
+    int32_t  explicit_amps; /* 1: per-octave amplitudes come from amps[]                       */
+    float    amps[UWW_MAX_OCTAVES];
+    int32_t  math_mode;     /* UWW_MATH_*                                                      */
+    int32_t  dedup_mode;    /* UWW_DEDUP_*                                                     */
+    uint32_t outputs;       /* UWW_OUT_* mask                                                  */
+    float    color_min_z;   /* world::MIN_Z = -2, in chunks (world.rs:12)                      */
+    float    color_max_z;   /* world::MAX_Z =  2, in chunks (world.rs:11)                      */
+} uww_params;
+
+/* One chunk to build.  pos is the chunk coordinate (Chunk::new(pos), chunk.rs:89);
+ * the chunk covers world [pos*chunk_size, (pos+1)*chunk_size) sampled at
+ * (cells+1)^3 points.  cell_offset is where this chunk's per-cell outputs
+ * (cases) start and sample_offset where its (cells+1)^3 samples start in a
+ * sample-grid array; uww_layout_cells() fills both. */
+typedef struct uww_chunk_desc {
+    int32_t  pos[3];
+    uint32_t cells;         /* 1..UWW_MAX_CELLS; the reference uses INTERNAL_SIZE = 12 */
+    uint32_t cell_offset;
+    uint32_t sample_offset;
+    uint32_t reserved[2];
+} uww_chunk_desc;           /* 32 bytes */
+
+/* Per-chunk result. Offsets index the batch's vertex and index arrays; index
+ * values are chunk-local vertex ids (as in the reference's per-chunk buffers). */
+typedef struct uww_chunk_record {
+    uint32_t num_verts;
+    uint32_t num_inds;      /* Chunk::num_inds (chunk.rs:348)       */
+    uint32_t vert_offset;
+    uint32_t ind_offset;
+    uint32_t flags;         /* UWW_CHUNK_*                          */
+    uint32_t num_active_cells;
+    uint32_t reserved[2];
+} uww_chunk_record;         /* 32 bytes */
+
+/* draw::VertColor (draw.rs:4-9): #[repr(C)] { pos: [f32;3], color: [f32;3] }, stride 24. */
+typedef struct uww_vert_color {
+    float pos[3];
+    float color[3];
+} uww_vert_color;
+
+/* Output buffers of a build.  Device pointers for uww_build_chunks*, host
+ * pointers for uww_build_chunks_host.  verts/inds/records are required; the
+ * others may be NULL (then that output is skipped even if requested). */
+typedef struct uww_mesh_out {
+    uww_vert_color*   verts;      /* vert_capacity entries                              */
+    float*            normals;    /* 3 * vert_capacity floats, or NULL                  */
+    uint32_t*         inds;       /* ind_capacity entries                               */
+    uint8_t*          cases;      /* sum(cells^3) bytes at desc.cell_offset, or NULL    */
+    float*            samples;    /* (cells+1)^3 f32 per chunk at desc.sample_offset, or NULL */
+    uww_chunk_record* records;    /* one per chunk                                      */
+    uint64_t*         totals;     /* device/host [4]: verts, inds, overflowed chunks, error flags; or NULL */
+    uint32_t          vert_capacity;
+    uint32_t          ind_capacity;
+} uww_mesh_out;
+
+typedef struct uww_ctx uww_ctx;
+
+/* ---- library --------------------------------------------------------------- */
+int         uww_abi_version(void);
+const char* uww_status_string(int status);
+
+/* Reference constants: chunk.rs:5-17, perlin_util.rs:6-29, world.rs:11-12; seed 0. */
+void uww_params_reference(uww_params* p);
+
+/* The seeded 256-entry permutation of noise::Perlin::new(seed) (state.rs:359). */
+int uww_perm_table(uint32_t seed, uint8_t out[256]);
+
+/* Fill desc[i].cell_offset / sample_offset with the running sums of cells^3 and
+ * (cells+1)^3; the totals go to *total_cells / *total_samples (either may be NULL). */
+int uww_layout_cells(uww_chunk_desc* desc, uint32_t n, uint64_t* total_cells, uint64_t* total_samples);
+
+/* ---- context (replaces the noise::Perlin handle passed to every build) ---- */
+/* stream: a cudaStream_t, or NULL for a stream the context creates and owns. */
+int   uww_ctx_create(const uww_params* p, void* stream, uww_ctx** out);
+int   uww_ctx_destroy(uww_ctx* ctx);
+int   uww_ctx_set_params(uww_ctx* ctx, const uww_params* p);
+int   uww_ctx_get_params(const uww_ctx* ctx, uww_params* p);
+void* uww_ctx_stream(uww_ctx* ctx);
+int   uww_ctx_sync(uww_ctx* ctx);
+
+/* ---- chunk builds ------------------------------------------------------------ */
+/* Batched build (replaces World's one-chunk-per-frame loop over Chunk::build_partial,
+ * world.rs:113-145): every chunk in one persistent launch fed by a device work
+ * queue.  d_chunks and out are device memory; max_cells bounds desc.cells.
+ * Asynchronous; read out->totals or records after uww_ctx_sync(). */
+int uww_build_chunks(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n,
+                     uint32_t max_cells, const uww_mesh_out* out);
+
+/* Marching cubes over caller-provided density samples instead of the noise:
+ * chunk i reads (cells+1)^3 f32 at d_samples + desc.sample_offset, laid out
+ * (x*S + y)*S + z like Build::isos (chunk.rs:43, 351-353).  Otherwise as
+ * uww_build_chunks. */
+int uww_build_chunks_from_samples(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint32_t max_cells,
+                                  const float* d_samples, const uww_mesh_out* out);
+
+/* One chunk per launch: the direct drop-in for Chunk::build_full (chunk.rs:266-268).
+ * d_chunk points to one device descriptor whose cells equal `cells`; out
+ * describes that chunk's own buffers (offsets in its record are 0) and
+ * out->totals is required.  Asynchronous. */
+int uww_build_chunk_plain(uww_ctx* ctx, const uww_chunk_desc* d_chunk, uint32_t cells, const uww_mesh_out* out);
+
+/* Host-buffer form of uww_build_chunks: copies the descriptors in, builds,
+ * copies records, vertices, normals, indices and cases out, synchronises.
+ * Returns UWW_ERR_CAPACITY (records still valid) when a capacity is too small. */
+int uww_build_chunks_host(uww_ctx* ctx, const uww_chunk_desc* h_chunks, uint32_t n,
+                          const uww_mesh_out* h_out);
+
+/* ---- tuning (written by the autotuner; 0 = automatic) ------------------------ */
+typedef struct uww_tuning {
+    int32_t threads;        /* threads per CTA (multiple of 32, <= 512)                     */
+    int32_t blocks_per_sm;  /* resident CTAs per SM of the persistent grid                   */
+    int32_t smem_cells;     /* chunks up to this many cells per edge work in shared memory;
+                               larger ones use a global scratch slot per CTA                */
+    int32_t reserved;
+} uww_tuning;
+int uww_ctx_set_tuning(uww_ctx* ctx, const uww_tuning* t);
+int uww_ctx_get_tuning(const uww_ctx* ctx, uww_tuning* t);
+
+/* ---- memory helpers for callers without their own CUDA binding --------------- */
+int uww_device_alloc(size_t bytes, void** out);
+int uww_device_free(void* p);
+int uww_host_alloc(size_t bytes, void** out);      /* page-locked host memory */
+int uww_host_free(void* p);
+/* asynchronous on the context stream; kind: 0 host->device, 1 device->host, 2 device->device */
+int uww_memcpy(uww_ctx* ctx, void* dst, const void* src, size_t bytes, int kind);
+int uww_memset(uww_ctx* ctx, void* dst, int value, size_t bytes);
+
+/* ---- point queries ------------------------------------------------------------ */
+/* density(world xyz) for n points: perlin_util::iso_at (perlin_util.rs:24-29) with
+ * (x,y,z) = world / CHUNK_SIZE as in boid.rs:132-137.  d_xyz: 3n floats; d_out: n. */
+int uww_density_at(uww_ctx* ctx, const float* d_xyz, uint32_t n, float* d_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* UWW_H */

@@ -1,0 +1,70 @@
+"""The C-ABI library loads and exports the declared interface (no GPU needed)."""
+import ctypes as C
+import subprocess
+
+import numpy as np
+
+from underwaterworld_gb300 import abi
+from underwaterworld_gb300.chunk import make_descs
+
+
+def test_library_exports_every_declared_symbol(built_lib):
+    declared = abi.declared_functions()
+    assert len(declared) >= 20
+    L = C.CDLL(str(built_lib))
+    for name in declared:
+        assert hasattr(L, name), name
+    out = subprocess.run(["nm", "-D", "--defined-only", str(built_lib)], capture_output=True, text=True).stdout
+    exported = {line.split()[-1] for line in out.splitlines() if " T " in line}
+    assert exported == set(declared), exported ^ set(declared)
+    assert set(abi._SIGS) == set(declared)
+
+
+def test_abi_version_and_status_strings(built_lib):
+    assert abi.lib().uww_abi_version() == 1
+    assert abi.status_string(abi.UWW_ERR_CAPACITY) == "output capacity exceeded"
+
+
+def test_struct_layouts():
+    assert C.sizeof(abi.ChunkDesc) == 32
+    assert C.sizeof(abi.ChunkRecord) == 32
+    assert abi.VERT_COLOR_DTYPE.itemsize == 24  # draw::VertColor stride (draw.rs:19)
+    assert C.sizeof(abi.Params) == 4 * (16 + 16 + 6)
+
+
+def test_reference_params(built_lib):
+    p = abi.reference_params()
+    assert (p.seed, p.octaves, p.chunk_size) == (0, 3, 16)
+    assert p.base_freq == np.float32(1 / 16)
+    assert (p.lacunarity, p.persistence, p.amplitude, p.normalize) == (2.0, 0.5, 1.0, 1)
+    assert p.bias_mode == abi.UWW_BIAS_TERRACED and (p.bias_a, p.bias_b, p.bias_c) == (16.0, 32.0, 0.25)
+    assert p.iso_level == np.float32(-0.1)
+    assert (p.color_min_z, p.color_max_z) == (-2.0, 2.0)
+
+
+def test_layout_cells(built_lib):
+    d = make_descs(np.zeros((3, 3)), [12, 24, 48])
+    raw = np.zeros(3, dtype=abi.CHUNK_DESC_DTYPE)
+    raw["cells"] = [12, 24, 48]
+    tc, ts = C.c_uint64(), C.c_uint64()
+    assert abi.lib().uww_layout_cells(raw.ctypes.data_as(C.c_void_p), 3, C.byref(tc), C.byref(ts)) == 0
+    np.testing.assert_array_equal(raw["cell_offset"], d["cell_offset"])
+    np.testing.assert_array_equal(raw["sample_offset"], d["sample_offset"])
+    assert tc.value == 12**3 + 24**3 + 48**3 and ts.value == 13**3 + 25**3 + 49**3
+    raw["cells"][1] = 0
+    assert abi.lib().uww_layout_cells(raw.ctypes.data_as(C.c_void_p), 3, None, None) == abi.UWW_ERR_INVALID_ARG
+
+
+def test_invalid_arguments_are_rejected_on_the_host(built_lib):
+    L = abi.lib()
+    p = abi.reference_params()
+    h = C.c_void_p()
+    bad = p.copy()
+    bad.octaves = 0
+    assert L.uww_ctx_create(C.byref(bad), None, C.byref(h)) == abi.UWW_ERR_INVALID_ARG
+    bad = p.copy()
+    bad.math_mode = 7
+    assert L.uww_ctx_create(C.byref(bad), None, C.byref(h)) == abi.UWW_ERR_INVALID_ARG
+    assert L.uww_ctx_create(C.byref(p), None, None) == abi.UWW_ERR_INVALID_ARG
+    assert L.uww_build_chunks(None, None, 0, 12, None) == abi.UWW_ERR_INVALID_ARG
+    assert L.uww_perm_table(0, None) == abi.UWW_ERR_INVALID_ARG

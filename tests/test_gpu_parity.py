@@ -1,0 +1,199 @@
+"""CUDA chunk builder vs the CPU oracle, through the C ABI.
+
+Parity build (UWW_MATH_EXACT): case indices, counts, flags, offsets, index
+buffers and vertex positions bit-exact; colours within COLOR_ATOL (powf);
+normals within NORMAL_ATOL.  Fast build: flipped cells and vertex error
+against the f64 oracle, reported and bounded.
+"""
+import numpy as np
+import pytest
+
+from underwaterworld_gb300 import abi, workloads
+from underwaterworld_gb300.chunk import Chunk, make_descs
+
+from helpers import assert_batches_equal, assert_records_equal, flipped_cells, load_golden, params_for_samples
+
+pytestmark = pytest.mark.gpu
+
+ALL = abi.UWW_OUT_COLOR | abi.UWW_OUT_NORMALS | abi.UWW_OUT_CASES
+
+
+def caps(ref):
+    return max(int(ref.totals[0]), 1), max(int(ref.totals[1]), 1)
+
+
+@pytest.mark.parametrize("name", ["single_cell", "single_cell_random", "grids"])
+def test_known_answers_from_samples(ctx_factory, oracle, name):
+    g = load_golden(name)
+    p = params_for_samples(g["iso_level"])
+    ctx = ctx_factory(p)
+    b = ctx.build_chunks_device(g["descs"], int(g["num_verts"].sum()) + 1, int(g["num_inds"].sum()) + 1,
+                                samples_in=g["samples"])
+    assert b.status == abi.UWW_OK
+    np.testing.assert_array_equal(b.records["num_verts"], g["num_verts"])
+    np.testing.assert_array_equal(b.records["num_inds"], g["num_inds"])
+    np.testing.assert_array_equal(b.inds, g["inds"])
+    np.testing.assert_array_equal(b.cases, g["cases"])
+    np.testing.assert_array_equal(b.verts["pos"], g["verts"])
+    np.testing.assert_allclose(b.verts["color"], g["colors"], rtol=0, atol=2e-6)
+
+
+@pytest.mark.parametrize("iso", [-0.1, 0.0])
+@pytest.mark.parametrize("dedup", [abi.UWW_DEDUP_ORIENTED, abi.UWW_DEDUP_EDGE])
+def test_reference_grid_bit_exact(ctx_factory, oracle, iso, dedup):
+    p, d = workloads.reference_grid(iso_level=iso, outputs=ALL)
+    p.dedup_mode = dedup
+    ref = oracle.build_chunks(p, d, precision=oracle.F32)
+    ctx = ctx_factory(p)
+    got = ctx.build_chunks_device(d, *caps(ref))
+    assert got.status == abi.UWW_OK
+    assert_batches_equal(got, ref)
+
+
+def test_host_path_equals_device_path(ctx_factory, oracle):
+    p, d = workloads.reference_grid(outputs=ALL)
+    ctx = ctx_factory(p)
+    ref = oracle.build_chunks(p, d)
+    a = ctx.build_chunks(d, *caps(ref))
+    b = ctx.build_chunks_device(d, *caps(ref))
+    assert a.status == abi.UWW_OK
+    assert_batches_equal(a, b)
+    assert_batches_equal(a, ref)
+
+
+def test_uniform_grid_subset_bit_exact(ctx_factory, oracle):
+    p, d = workloads.uniform_grid(seed=3, outputs=ALL)
+    # the z-layers that straddle the surface, plus blank ones above and below
+    sel = d[(d["pos"][:, 0] < 6) & (d["pos"][:, 1] < 6)]
+    ref = oracle.build_chunks(p, sel)
+    got = ctx_factory(p).build_chunks_device(sel, *caps(ref))
+    assert_batches_equal(got, ref)
+    assert (ref.records["flags"] & abi.UWW_CHUNK_HAS_MESH).sum() > 10
+
+
+@pytest.mark.parametrize("cells", [24, 48, 5, 1])
+def test_other_lods_bit_exact(ctx_factory, oracle, cells):
+    p, _ = workloads.uniform_grid(seed=1, outputs=ALL)
+    pos = [(1, 2, 7), (3, 3, 8), (0, 5, 7), (2, 2, 2)]
+    d = make_descs(pos, cells)
+    ref = oracle.build_chunks(p, d)
+    got = ctx_factory(p).build_chunks_device(d, *caps(ref))
+    assert_batches_equal(got, ref)
+
+
+def test_mixed_lod_batch_bit_exact(ctx_factory, oracle):
+    p, d = workloads.mixed_lod(seed=2, outputs=ALL)
+    sel = d[:96]
+    ref = oracle.build_chunks(p, sel)
+    got = ctx_factory(p).build_chunks_device(sel, *caps(ref))
+    assert_batches_equal(got, ref)
+
+
+def test_plain_per_chunk_launch_matches_batch(ctx_factory, oracle):
+    p, d = workloads.reference_grid(outputs=abi.UWW_OUT_COLOR | abi.UWW_OUT_NORMALS)
+    ctx = ctx_factory(p)
+    ref = oracle.build_chunks(p, d)
+    for i in [0, 31, 62, 64, 100, 124]:
+        ch = Chunk(tuple(d["pos"][i]))
+        ch.build_full(ctx)
+        v, n, ind = ref.chunk(i)
+        assert ch.num_inds() == len(ind)
+        assert ch.not_blank() == (len(ind) > 0)
+        np.testing.assert_array_equal(ch.inds(), ind)
+        np.testing.assert_array_equal(ch.verts()["pos"], v["pos"])
+        np.testing.assert_allclose(ch.normals(), n, atol=1e-6)
+
+
+def test_density_at_matches_oracle(ctx_factory, oracle):
+    for p, lo, hi in [(workloads.reference_grid()[0], -40, 40), (workloads.uniform_grid(seed=4)[0], 0, 256)]:
+        rng = np.random.default_rng(5)
+        x = rng.uniform(lo, hi, (10000, 3)).astype(np.float32)
+        np.testing.assert_array_equal(ctx_factory(p).density_at(x), oracle.density_at(p, x))
+
+
+def test_iso_at_chunk_units(ctx_factory, oracle):
+    p = abi.reference_params()
+    ctx = ctx_factory(p)
+    v = ctx.iso_at(0.5, -1.25, 0.75)
+    assert v == oracle.density_at(p, np.array([[8.0, -20.0, 12.0]], np.float32))[0]
+
+
+def test_capacity_overflow_then_regrow(ctx_factory, oracle):
+    p, d = workloads.reference_grid(outputs=ALL)
+    ctx = ctx_factory(p)
+    ref = oracle.build_chunks(p, d)
+    small = ctx.build_chunks_device(d, 1000, 3000)
+    assert small.status == abi.UWW_ERR_CAPACITY
+    np.testing.assert_array_equal(small.totals[:2], ref.totals[:2])
+    assert int(small.totals[2]) > 0
+    ok = (small.records["flags"] & abi.UWW_CHUNK_OVERFLOW) == 0
+    np.testing.assert_array_equal(small.records["num_inds"], ref.records["num_inds"])
+    # chunks that fitted were written correctly
+    for i in np.nonzero(ok & (ref.records["num_inds"] > 0))[0]:
+        v0, nv = ref.records["vert_offset"][i], ref.records["num_verts"][i]
+        i0, ni = ref.records["ind_offset"][i], ref.records["num_inds"][i]
+        np.testing.assert_array_equal(small.inds[i0:i0 + ni], ref.inds[i0:i0 + ni])
+        np.testing.assert_array_equal(small.verts["pos"][v0:v0 + nv], ref.verts["pos"][v0:v0 + nv])
+    big = ctx.build_chunks_device(d, int(small.totals[0]), int(small.totals[1]))
+    assert big.status == abi.UWW_OK
+    assert_batches_equal(big, ref)
+
+
+def test_empty_blank_and_solid_batches(ctx_factory, oracle):
+    p, d = workloads.reference_grid(outputs=ALL)
+    ctx = ctx_factory(p)
+    e = ctx.build_chunks_device(d[:0], 16, 16)
+    assert e.totals[0] == 0 and e.totals[1] == 0
+    for iso in (-50.0, 50.0):  # everything outside / everything inside
+        q = p.copy()
+        q.iso_level = iso
+        ctx.set_params(q)
+        b = ctx.build_chunks_device(d, 16, 16)
+        ref = oracle.build_chunks(q, d)
+        assert b.status == abi.UWW_OK and b.totals[0] == 0 and b.totals[1] == 0
+        assert_records_equal(b.records, ref.records)
+        np.testing.assert_array_equal(b.cases, ref.cases)
+        expect = abi.UWW_CHUNK_EARLY_BLANK if iso < 0 else 0
+        assert np.all(b.records["flags"] == expect)
+
+
+def test_bad_descriptor_is_flagged_not_built(ctx_factory):
+    p, d = workloads.reference_grid()
+    ctx = ctx_factory(p)
+    bad = d[:4].copy()
+    bad["cells"][2] = 40  # above the max_cells the launch was given
+    b = ctx.build_chunks_device(bad[[0, 1, 3]], 5000, 20000)  # sanity: good chunks alone
+    assert b.status == abi.UWW_OK
+    import ctypes as C
+    from underwaterworld_gb300.chunk import DeviceArray
+    d_desc = ctx.upload(bad)
+    d_rec, d_tot = DeviceArray(4 * 32), DeviceArray(32)
+    d_v, d_i = DeviceArray(5000 * 24), DeviceArray(20000 * 4)
+    out = abi.MeshOut(d_v.ptr, None, d_i.ptr, None, None, d_rec.ptr, d_tot.ptr, 5000, 20000)
+    assert abi.lib().uww_build_chunks(ctx.h, C.c_void_p(d_desc.ptr), 4, 12, C.byref(out)) == abi.UWW_OK
+    ctx.sync()
+    tot = ctx.download(d_tot, (4,), np.uint64)
+    assert int(tot[3]) & 2
+    rec = ctx.download(d_rec, (4,), abi.CHUNK_RECORD_DTYPE)
+    assert rec["num_inds"][2] == 0
+
+
+def test_fast_build_against_f64_oracle(ctx_factory, oracle):
+    """The FMA build: count flipped cells and the worst vertex error vs the f64 oracle."""
+    p, d = workloads.uniform_grid(seed=0, outputs=abi.UWW_OUT_CASES)
+    sel = d[(d["pos"][:, 0] < 8) & (d["pos"][:, 1] < 8)]
+    ref = oracle.build_chunks(p, sel, precision=oracle.F64)
+    q = p.copy()
+    q.math_mode = abi.UWW_MATH_FAST
+    got = ctx_factory(q).build_chunks_device(sel, int(ref.totals[0]) + 4096, int(ref.totals[1]) + 16384)
+    assert got.status == abi.UWW_OK
+    flips = flipped_cells(got.cases, ref.cases)
+    assert flips <= 1e-4 * len(ref.cases), flips
+    same = got.records["num_inds"] == ref.records["num_inds"]
+    err = 0.0
+    for i in np.nonzero(same & (ref.records["num_inds"] > 0))[0]:
+        gv, _, gi = got.chunk(i)
+        rv, _, ri = ref.chunk(i)
+        if np.array_equal(gi, ri):
+            err = max(err, float(np.abs(gv["pos"] - rv["pos"]).max()))
+    assert err < 1e-3, err

@@ -1,0 +1,74 @@
+"""Invariants of the marching-cubes tables generated from marching_table.rs."""
+import re
+from pathlib import Path
+
+import numpy as np
+
+HDR = Path(__file__).resolve().parent.parent / "underwaterworld_gb300" / "csrc" / "mc_tables.h"
+CORNERS = [(0, 0, 0), (1, 0, 0), (1, 0, 1), (0, 0, 1), (0, 1, 0), (1, 1, 0), (1, 1, 1), (0, 1, 1)]
+
+
+def _array(name):
+    src = HDR.read_text()
+    m = re.search(name + r"\[[^=]*=\s*\{(.*?)\};", src, re.S)
+    return [int(v, 0) for v in re.findall(r"-?(?:0x[0-9a-f]+|\d+)", m.group(1))]
+
+
+def tables():
+    edges = np.array(_array("UWW_EDGE_CORNERS"), dtype=int).reshape(12, 2)
+    tri = np.array(_array("UWW_TRI_TABLE"), dtype=int).reshape(256, 16)
+    ntri = np.array(_array("UWW_CASE_NTRI"), dtype=int)
+    emask = np.array(_array("UWW_CASE_EDGES"), dtype=int)
+    share = np.array(_array("UWW_EDGE_SHARE"), dtype=int).reshape(12, 4, 5)
+    return edges, tri, ntri, emask, share
+
+
+def test_rows_are_whole_triangles_and_terminated():
+    _, tri, ntri, _, _ = tables()
+    for c in range(256):
+        row = list(tri[c])
+        n = row.index(-1) if -1 in row else 16
+        assert n % 3 == 0 and n == 3 * ntri[c]
+        assert all(v == -1 for v in row[n:])
+        assert all(0 <= v < 12 for v in row[:n])
+
+
+def test_empty_and_full_cases():
+    _, tri, ntri, _, _ = tables()
+    assert ntri[0] == 0 and ntri[255] == 0
+    assert tri[0][0] == -1 and tri[255][0] == -1
+    assert ntri.max() == 5
+
+
+def test_each_row_uses_exactly_the_crossed_edges():
+    """A crossed edge is used by every cell holding it: the basis of owner-cell dedup."""
+    edges, _, _, emask, _ = tables()
+    for c in range(256):
+        crossed = 0
+        for e, (a, b) in enumerate(edges):
+            if ((c >> a) & 1) != ((c >> b) & 1):
+                crossed |= 1 << e
+        assert crossed == emask[c], c
+
+
+def test_complement_cases_use_same_edges():
+    _, _, ntri, emask, _ = tables()
+    for c in range(256):
+        assert emask[c] == emask[255 - c]
+
+
+def test_edge_share_table():
+    edges, _, _, _, share = tables()
+    for e, (a, b) in enumerate(edges):
+        A, B = np.array(CORNERS[a]), np.array(CORNERS[b])
+        seen_self = False
+        for dx, dy, dz, e2, same in share[e]:
+            off = np.array([dx, dy, dz])
+            a2, b2 = edges[e2]
+            A2, B2 = np.array(CORNERS[a2]) + off, np.array(CORNERS[b2]) + off
+            assert {tuple(A2), tuple(B2)} == {tuple(A), tuple(B)}
+            assert bool(same) == (tuple(A2) == tuple(A))
+            seen_self |= (dx, dy, dz, e2) == (0, 0, 0, e)
+        assert seen_self
+        keys = [tuple(s[:3]) for s in share[e]]
+        assert keys == sorted(keys), "candidates must be in cell order"

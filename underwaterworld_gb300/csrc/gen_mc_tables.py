@@ -1,0 +1,133 @@
+"""Generate ``mc_tables.h`` from the reference's marching-cubes tables.
+
+The two tables (``EDGE_VERTEX_INDICES[12][2]`` and ``TRIANGULATION[256][16]``)
+are parsed from ``underwater_world/src/marching_table.rs:1-273`` of
+LelsersLasers/UnderwaterWorld (MIT licence, Copyright (c) 2024 Millan Kumar)
+instead of being typed in, so the CUDA kernels and the CPU oracle use exactly
+the rows the reference walks.  Two derived tables are added:
+
+* ``UWW_CASE_NTRI[256]``  -- triangles per case (row length before -1, / 3);
+* ``UWW_CASE_EDGES[256]`` -- 12-bit mask of the edges a case's row references.
+
+Usage: ``python gen_mc_tables.py <path to marching_table.rs> [out.h]``.
+The generated header is committed; this script only runs when the tables
+must be regenerated.
+"""
+import re
+import sys
+from pathlib import Path
+
+
+def parse(src: str):
+    m = re.search(r"EDGE_VERTEX_INDICES[^=]*=\s*\[(.*?)\];", src, re.S)
+    edges = [tuple(int(v) for v in pair)
+             for pair in re.findall(r"\[\s*(\d+)\s*,\s*(\d+)\s*\]", m.group(1))]
+    m = re.search(r"TRIANGULATION[^=]*=\s*\[(.*)\];", src, re.S)
+    rows = [[int(v) for v in row.split(",") if v.strip()]
+            for row in re.findall(r"\[([-\d,\s]+)\]", m.group(1))]
+    assert len(edges) == 12 and all(len(e) == 2 for e in edges)
+    assert len(rows) == 256 and all(len(r) == 16 for r in rows)
+    return edges, rows
+
+
+def derive(rows):
+    ntri, emask = [], []
+    for r in rows:
+        n = r.index(-1) if -1 in r else 16
+        assert n % 3 == 0, "row length must be a multiple of 3"
+        assert all(v == -1 for v in r[n:])
+        ntri.append(n // 3)
+        m = 0
+        for e in r[:n]:
+            m |= 1 << e
+        emask.append(m)
+    return ntri, emask
+
+
+# Cube corner offsets in the reference's order (chunk.rs:144-153).
+CORNERS = [(0, 0, 0), (1, 0, 0), (1, 0, 1), (0, 0, 1),
+           (0, 1, 0), (1, 1, 0), (1, 1, 1), (0, 1, 1)]
+
+
+def edge_share(edges):
+    """For each cube edge e of a cell at the origin: the four cells that hold
+    the same physical edge, as (dx, dy, dz, e', same_orientation), sorted in
+    the builder's cell order (x outer, then y, then z)."""
+    table = []
+    for a, b in edges:
+        A, B = CORNERS[a], CORNERS[b]
+        axis = [i for i in range(3) if A[i] != B[i]][0]
+        lo = tuple(min(A[i], B[i]) for i in range(3))
+        others = [i for i in range(3) if i != axis]
+        cands = []
+        for du in (0, 1):
+            for dv in (0, 1):
+                C = list(lo)
+                C[others[0]] -= du
+                C[others[1]] -= dv
+                C = tuple(C)
+                found = None
+                for e2, (a2, b2) in enumerate(edges):
+                    A2 = tuple(CORNERS[a2][i] + C[i] for i in range(3))
+                    B2 = tuple(CORNERS[b2][i] + C[i] for i in range(3))
+                    if {A2, B2} == {A, B}:
+                        found = (C[0], C[1], C[2], e2, int(A2 == A))
+                assert found is not None
+                cands.append(found)
+        cands.sort(key=lambda t: (t[0], t[1], t[2]))
+        table.append(cands)
+    return table
+
+
+def emit(edges, rows, ntri, emask) -> str:
+    out = [
+        "// Generated by gen_mc_tables.py from underwater_world/src/marching_table.rs:1-273",
+        "// of LelsersLasers/UnderwaterWorld (MIT licence, Copyright (c) 2024 Millan Kumar).",
+        "// Do not edit by hand; regenerate with the script.",
+        "#pragma once",
+        "#include <stdint.h>",
+        "// UWW_TABLE_QUAL lets CUDA code place the tables in __constant__ memory.",
+        "#ifndef UWW_TABLE_QUAL",
+        "#define UWW_TABLE_QUAL",
+        "#endif",
+        "",
+        "// Bourke cube-edge -> (corner a, corner b); marching_table.rs:1-14.",
+        "UWW_TABLE_QUAL static const uint8_t UWW_EDGE_CORNERS[12][2] = {",
+    ]
+    out.append(",\n".join(f"    {{{a}, {b}}}" for a, b in edges))
+    out += ["};", "",
+            "// Bourke triangulation, -1 terminated; marching_table.rs:16-273.",
+            "UWW_TABLE_QUAL static const int8_t UWW_TRI_TABLE[256][16] = {"]
+    out.append(",\n".join("    {" + ", ".join(f"{v:2d}" for v in r) + "}" for r in rows))
+    out += ["};", "", "// Triangles per case (derived).",
+            "UWW_TABLE_QUAL static const uint8_t UWW_CASE_NTRI[256] = {"]
+    out.append(",\n".join("    " + ", ".join(str(v) for v in ntri[i:i + 16])
+                          for i in range(0, 256, 16)))
+    out += ["};", "", "// Edges referenced by each case's row, bit e = edge e (derived).",
+            "UWW_TABLE_QUAL static const uint16_t UWW_CASE_EDGES[256] = {"]
+    out.append(",\n".join("    " + ", ".join(f"0x{v:03x}" for v in emask[i:i + 8])
+                          for i in range(0, 256, 8)))
+    out += ["};", "",
+            "// For cube edge e: the 4 cells sharing that edge as {dx, dy, dz, e', same orientation},",
+            "// in cell order (x outer, y, z inner).  The first one inside the chunk (and, for",
+            "// oriented dedup, with the same orientation) is where the reference creates the vertex.",
+            "UWW_TABLE_QUAL static const int8_t UWW_EDGE_SHARE[12][4][5] = {"]
+    rows_out = []
+    for e, cands in enumerate(edge_share(edges)):
+        rows_out.append("    {" + ", ".join("{%d, %d, %d, %d, %d}" % c for c in cands) + "}")
+    out.append(",\n".join(rows_out))
+    out += ["};", ""]
+    return "\n".join(out)
+
+
+def main(argv):
+    src = Path(argv[1]).read_text()
+    dst = Path(argv[2]) if len(argv) > 2 else Path(__file__).with_name("mc_tables.h")
+    edges, rows = parse(src)
+    ntri, emask = derive(rows)
+    dst.write_text(emit(edges, rows, ntri, emask))
+    print(f"wrote {dst}")
+
+
+if __name__ == "__main__":
+    main(sys.argv)

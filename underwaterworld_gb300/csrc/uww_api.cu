@@ -1,0 +1,567 @@
+// uww_api.cu -- the C ABI (include/uww.h): contexts, parameter handling,
+// the seeded permutation, launch configuration and the host-buffer path.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "uww_internal.h"
+
+using namespace uww;
+
+struct uww_ctx {
+    uww_params params;
+    DevParams dev;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int device = 0;
+    int num_sms = 0;
+    size_t smem_optin = 0;
+
+    // tuning (0 = automatic)
+    int threads = 0;
+    int blocks_per_sm = 0;
+    int smem_cells = 0;
+
+    // device work state
+    unsigned long long* d_lookback = nullptr;
+    size_t lookback_cap = 0;
+    unsigned int* d_counter = nullptr;
+    unsigned long long* d_totals = nullptr;
+    uint8_t* d_scratch = nullptr;
+    size_t scratch_cap = 0;
+
+    // buffers of the host-buffer path
+    uww_chunk_desc* d_chunks = nullptr;
+    size_t chunks_cap = 0;
+    void* d_verts = nullptr;     size_t verts_cap = 0;
+    void* d_normals = nullptr;   size_t normals_cap = 0;
+    void* d_inds = nullptr;      size_t inds_cap = 0;
+    void* d_cases = nullptr;     size_t cases_cap = 0;
+    void* d_samples = nullptr;   size_t samples_cap = 0;
+    void* d_records = nullptr;   size_t records_cap = 0;
+    unsigned long long* h_totals = nullptr;
+};
+
+namespace {
+
+constexpr long long kSpinLimitCycles = 4000000000ll;  // ~2 s at 2 GHz
+
+int cuda_status(cudaError_t e) { return e == cudaSuccess ? UWW_OK : (e == cudaErrorMemoryAllocation ? UWW_ERR_OOM : UWW_ERR_CUDA); }
+
+// --- noise::Perlin::new(seed) permutation --------------------------------------
+// The crate seeds an XorShift128 generator with the bytes
+// [1,0,0,0, seed x3] (x = 1, y = z = w = seed) and shuffles 0..255 with
+// rand's Fisher-Yates (i from 255 down to 1, j uniform in [0, i]); the
+// bounded draw multiplies a 32-bit output by the range and rejects low
+// words above (range << clz(range)) - 1.
+struct XorShift128 {
+    uint32_t x, y, z, w;
+    uint32_t next()
+    {
+        const uint32_t t = x ^ (x << 11);
+        x = y; y = z; z = w;
+        w = w ^ (w >> 19) ^ (t ^ (t >> 8));
+        return w;
+    }
+    uint32_t below(uint32_t range)
+    {
+        const uint32_t zone = (range << __builtin_clz(range)) - 1u;
+        for (;;) {
+            const uint64_t m = (uint64_t)next() * range;
+            if ((uint32_t)m <= zone) return (uint32_t)(m >> 32);
+        }
+    }
+};
+
+void make_perm(uint32_t seed, uint8_t out[256])
+{
+    XorShift128 r{1u, seed, seed, seed};
+    for (int i = 0; i < 256; ++i) out[i] = (uint8_t)i;
+    for (uint32_t i = 255; i >= 1; --i) std::swap(out[i], out[r.below(i + 1)]);
+}
+
+bool finite(float v) { return std::isfinite(v); }
+
+int validate_params(const uww_params* p)
+{
+    if (!p) return UWW_ERR_INVALID_ARG;
+    if (p->octaves < 1 || p->octaves > UWW_MAX_OCTAVES) return UWW_ERR_INVALID_ARG;
+    if (p->chunk_size < 1 || p->chunk_size > (1 << 20)) return UWW_ERR_INVALID_ARG;
+    if (!finite(p->base_freq) || !finite(p->lacunarity) || !finite(p->persistence) || !finite(p->amplitude))
+        return UWW_ERR_INVALID_ARG;
+    if (!finite(p->iso_level) || !finite(p->offset[0]) || !finite(p->offset[1]) || !finite(p->offset[2]))
+        return UWW_ERR_INVALID_ARG;
+    if (p->bias_mode < UWW_BIAS_NONE || p->bias_mode > UWW_BIAS_LINEAR) return UWW_ERR_INVALID_ARG;
+    if (p->bias_mode == UWW_BIAS_TERRACED && (p->bias_b == 0.f || p->bias_c == 0.f)) return UWW_ERR_INVALID_ARG;
+    if (p->math_mode != UWW_MATH_EXACT && p->math_mode != UWW_MATH_FAST) return UWW_ERR_INVALID_ARG;
+    if (p->dedup_mode != UWW_DEDUP_ORIENTED && p->dedup_mode != UWW_DEDUP_EDGE) return UWW_ERR_INVALID_ARG;
+    if (p->color_max_z == p->color_min_z) return UWW_ERR_INVALID_ARG;
+    if (p->explicit_amps)
+        for (uint32_t k = 0; k < p->octaves; ++k)
+            if (!finite(p->amps[k])) return UWW_ERR_INVALID_ARG;
+    return UWW_OK;
+}
+
+void make_dev_params(const uww_params* p, DevParams* d)
+{
+    std::memset(d, 0, sizeof(*d));
+    make_perm(p->seed, d->perm);
+    // perlin_util.rs:8-20: frequency and amplitude advance by repeated f32 multiplies
+    float m = 1.f, a = p->amplitude;
+    for (uint32_t k = 0; k < p->octaves; ++k) {
+        d->mult[k] = m;
+        d->amp[k] = p->explicit_amps ? p->amps[k] : a;
+        m = m * p->lacunarity;
+        a = a * p->persistence;
+    }
+    d->octaves = (int32_t)p->octaves;
+    d->chunk_size = p->chunk_size;
+    d->base_freq = p->base_freq;
+    d->iso_level = p->iso_level;
+    for (int i = 0; i < 3; ++i) d->offset[i] = p->offset[i];
+    d->normalize = p->normalize;
+    d->bias_mode = p->bias_mode;
+    d->bias_a = p->bias_a;
+    d->bias_b = p->bias_b;
+    d->bias_c = p->bias_c;
+    d->color_min_z = p->color_min_z;
+    d->color_max_z = p->color_max_z;
+    d->outputs = p->outputs;
+    d->dedup_mode = p->dedup_mode;
+    d->math_mode = p->math_mode;
+}
+
+template <class T>
+int ensure_device(T** ptr, size_t* cap, size_t bytes)
+{
+    if (*cap >= bytes && *ptr) return UWW_OK;
+    if (*ptr) cudaFree(*ptr);
+    *ptr = nullptr;
+    *cap = 0;
+    size_t want = std::max<size_t>(bytes, 256);
+    cudaError_t e = cudaMalloc((void**)ptr, want);
+    if (e != cudaSuccess) { *ptr = nullptr; return cuda_status(e); }
+    *cap = want;
+    return UWW_OK;
+}
+
+struct LaunchCfg {
+    int threads;
+    uint32_t smem_cells;
+    size_t dyn_smem;
+    int grid;
+    size_t scratch_slot;
+};
+
+int plan_launch(uww_ctx* ctx, uint32_t n, uint32_t max_cells, bool queue, LaunchCfg* cfg)
+{
+    const size_t static_smem = build_static_smem_bytes();
+    const size_t cap = ctx->smem_optin > static_smem + 1024 ? ctx->smem_optin - static_smem - 1024 : 0;
+    uint32_t smem_cells = ctx->smem_cells > 0 ? (uint32_t)ctx->smem_cells : max_cells;
+    smem_cells = std::min(smem_cells, max_cells);
+    while (smem_cells > 0 && chunk_layout((int)smem_cells).total > cap) --smem_cells;
+    cfg->smem_cells = smem_cells;
+    cfg->dyn_smem = smem_cells > 0 ? chunk_layout((int)smem_cells).total : 0;
+    cfg->threads = ctx->threads > 0 ? ctx->threads : (max_cells > 16 ? 512 : 256);
+    cfg->scratch_slot = max_cells > smem_cells ? chunk_layout((int)max_cells).total : 0;
+    if (!queue) {
+        cfg->grid = 1;
+        return UWW_OK;
+    }
+    int bps = ctx->blocks_per_sm;
+    if (bps <= 0) {
+        cudaError_t e = build_occupancy(true, ctx->dev.math_mode == UWW_MATH_EXACT, cfg->threads, cfg->dyn_smem, &bps);
+        if (e != cudaSuccess) return cuda_status(e);
+        if (bps < 1) return UWW_ERR_INVALID_ARG;
+    }
+    const long long g = (long long)bps * ctx->num_sms;
+    cfg->grid = (int)std::min<long long>(g, n);
+    return UWW_OK;
+}
+
+int launch(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint32_t max_cells, const uww_mesh_out* out,
+           bool queue, const float* samples_in = nullptr)
+{
+    LaunchCfg cfg;
+    int st = plan_launch(ctx, n, max_cells, queue, &cfg);
+    if (st) return st;
+    if (cfg.scratch_slot) {
+        st = ensure_device(&ctx->d_scratch, &ctx->scratch_cap, cfg.scratch_slot * (size_t)cfg.grid);
+        if (st) return st;
+    }
+    BuildArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.chunks = d_chunks;
+    a.n = n;
+    a.max_cells = max_cells;
+    a.verts = out->verts;
+    a.normals = out->normals;
+    a.inds = out->inds;
+    a.cases = out->cases;
+    a.samples_out = (ctx->params.outputs & UWW_OUT_SAMPLES) ? out->samples : nullptr;
+    a.samples_in = samples_in;
+    a.records = out->records;
+    a.totals = out->totals ? reinterpret_cast<unsigned long long*>(out->totals) : ctx->d_totals;
+    a.vert_capacity = out->vert_capacity;
+    a.ind_capacity = out->ind_capacity;
+    a.scratch = ctx->d_scratch;
+    a.scratch_slot_bytes = cfg.scratch_slot;
+    a.smem_cells = cfg.smem_cells;
+    a.spin_limit_cycles = kSpinLimitCycles;
+    if (queue) {
+        st = ensure_device(&ctx->d_lookback, &ctx->lookback_cap, (size_t)n * sizeof(unsigned long long));
+        if (st) return st;
+        a.lookback = ctx->d_lookback;
+        a.work_counter = ctx->d_counter;
+        cudaError_t e;
+        if ((e = cudaMemsetAsync(ctx->d_lookback, 0, (size_t)n * sizeof(unsigned long long), ctx->stream)) != cudaSuccess)
+            return cuda_status(e);
+        if ((e = cudaMemsetAsync(ctx->d_counter, 0, sizeof(unsigned int), ctx->stream)) != cudaSuccess)
+            return cuda_status(e);
+        if ((e = cudaMemsetAsync(a.totals, 0, 4 * sizeof(unsigned long long), ctx->stream)) != cudaSuccess)
+            return cuda_status(e);
+    }
+    return cuda_status(launch_build(ctx->dev, a, queue, cfg.grid, cfg.threads, cfg.dyn_smem, ctx->stream));
+}
+
+int check_out(const uww_mesh_out* out)
+{
+    if (!out || !out->verts || !out->inds || !out->records) return UWW_ERR_INVALID_ARG;
+    if (out->vert_capacity > kLbVertMax) return UWW_ERR_INVALID_ARG;
+    return UWW_OK;
+}
+
+}  // namespace
+
+#pragma GCC visibility push(default)
+extern "C" {
+
+int uww_abi_version(void) { return UWW_ABI_VERSION; }
+
+const char* uww_status_string(int s)
+{
+    switch (s) {
+    case UWW_OK: return "ok";
+    case UWW_ERR_INVALID_ARG: return "invalid argument";
+    case UWW_ERR_CUDA: return "CUDA error";
+    case UWW_ERR_CAPACITY: return "output capacity exceeded";
+    case UWW_ERR_OOM: return "out of memory";
+    case UWW_ERR_TIMEOUT: return "device wait timed out";
+    default: return "unknown status";
+    }
+}
+
+void uww_params_reference(uww_params* p)
+{
+    if (!p) return;
+    std::memset(p, 0, sizeof(*p));
+    p->seed = 0;
+    p->octaves = 3;             // PERLIN_OCTAVES (chunk.rs:9)
+    p->chunk_size = 16;         // CHUNK_SIZE (chunk.rs:5)
+    p->base_freq = 1.0f / 16.0f;  // (local + offset) / CHUNK_SIZE (chunk.rs:108)
+    p->lacunarity = 2.0f;       // perlin_util.rs:19
+    p->persistence = 0.5f;      // perlin_util.rs:18
+    p->amplitude = 1.0f;        // perlin_util.rs:9
+    p->normalize = 1;           // perlin_util.rs:21
+    p->bias_mode = UWW_BIAS_TERRACED;
+    p->bias_a = 16.0f;          // CHUNK_SIZE
+    p->bias_b = 32.0f;          // MAX_HEIGHT (chunk.rs:11)
+    p->bias_c = 0.25f;          // ADJ_Z_MOD (chunk.rs:12)
+    p->iso_level = -0.1f;       // ISO_LEVEL (chunk.rs:10)
+    p->math_mode = UWW_MATH_EXACT;
+    p->dedup_mode = UWW_DEDUP_ORIENTED;
+    p->outputs = UWW_OUT_COLOR;
+    p->color_min_z = -2.0f;     // world::MIN_Z (world.rs:12)
+    p->color_max_z = 2.0f;      // world::MAX_Z (world.rs:11)
+}
+
+int uww_perm_table(uint32_t seed, uint8_t out[256])
+{
+    if (!out) return UWW_ERR_INVALID_ARG;
+    make_perm(seed, out);
+    return UWW_OK;
+}
+
+int uww_layout_cells(uww_chunk_desc* desc, uint32_t n, uint64_t* total_cells, uint64_t* total_samples)
+{
+    if (!desc && n) return UWW_ERR_INVALID_ARG;
+    uint64_t off = 0, soff = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        const uint64_t c = desc[i].cells;
+        if (c < 1 || c > UWW_MAX_CELLS) return UWW_ERR_INVALID_ARG;
+        if (off > 0xffffffffull || soff > 0xffffffffull) return UWW_ERR_INVALID_ARG;
+        desc[i].cell_offset = (uint32_t)off;
+        desc[i].sample_offset = (uint32_t)soff;
+        off += c * c * c;
+        soff += (c + 1) * (c + 1) * (c + 1);
+    }
+    if (total_cells) *total_cells = off;
+    if (total_samples) *total_samples = soff;
+    return UWW_OK;
+}
+
+int uww_ctx_create(const uww_params* p, void* stream, uww_ctx** out)
+{
+    if (!out) return UWW_ERR_INVALID_ARG;
+    *out = nullptr;
+    int st = validate_params(p);
+    if (st) return st;
+    uww_ctx* ctx = new (std::nothrow) uww_ctx();
+    if (!ctx) return UWW_ERR_OOM;
+    ctx->params = *p;
+    make_dev_params(p, &ctx->dev);
+    cudaError_t e = cudaGetDevice(&ctx->device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    int optin = 0;
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
+    ctx->smem_optin = (size_t)optin;
+    if (e == cudaSuccess) {
+        const size_t static_smem = build_static_smem_bytes();
+        e = prepare_build_kernels(ctx->smem_optin > static_smem ? ctx->smem_optin - static_smem : 0);
+    }
+    if (e == cudaSuccess) {
+        if (stream) ctx->stream = (cudaStream_t)stream;
+        else { e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking); ctx->own_stream = true; }
+    }
+    if (e == cudaSuccess) e = cudaMalloc((void**)&ctx->d_counter, sizeof(unsigned int));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&ctx->d_totals, 4 * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMallocHost((void**)&ctx->h_totals, 4 * sizeof(unsigned long long));
+    if (e != cudaSuccess) {
+        uww_ctx_destroy(ctx);
+        return cuda_status(e);
+    }
+    *out = ctx;
+    return UWW_OK;
+}
+
+int uww_ctx_destroy(uww_ctx* ctx)
+{
+    if (!ctx) return UWW_ERR_INVALID_ARG;
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    cudaFree(ctx->d_lookback);
+    cudaFree(ctx->d_counter);
+    cudaFree(ctx->d_totals);
+    cudaFree(ctx->d_scratch);
+    cudaFree(ctx->d_chunks);
+    cudaFree(ctx->d_verts);
+    cudaFree(ctx->d_normals);
+    cudaFree(ctx->d_inds);
+    cudaFree(ctx->d_cases);
+    cudaFree(ctx->d_samples);
+    cudaFree(ctx->d_records);
+    if (ctx->h_totals) cudaFreeHost(ctx->h_totals);
+    if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return UWW_OK;
+}
+
+int uww_ctx_set_params(uww_ctx* ctx, const uww_params* p)
+{
+    if (!ctx) return UWW_ERR_INVALID_ARG;
+    int st = validate_params(p);
+    if (st) return st;
+    ctx->params = *p;
+    make_dev_params(p, &ctx->dev);
+    return UWW_OK;
+}
+
+int uww_ctx_get_params(const uww_ctx* ctx, uww_params* p)
+{
+    if (!ctx || !p) return UWW_ERR_INVALID_ARG;
+    *p = ctx->params;
+    return UWW_OK;
+}
+
+void* uww_ctx_stream(uww_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+int uww_ctx_sync(uww_ctx* ctx)
+{
+    if (!ctx) return UWW_ERR_INVALID_ARG;
+    return cuda_status(cudaStreamSynchronize(ctx->stream));
+}
+
+int uww_build_chunks(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint32_t max_cells,
+                     const uww_mesh_out* out)
+{
+    if (!ctx) return UWW_ERR_INVALID_ARG;
+    int st = check_out(out);
+    if (st) return st;
+    if (max_cells < 1 || max_cells > UWW_MAX_CELLS) return UWW_ERR_INVALID_ARG;
+    if (n == 0) {
+        if (out->totals) return cuda_status(cudaMemsetAsync(out->totals, 0, 4 * sizeof(uint64_t), ctx->stream));
+        return UWW_OK;
+    }
+    if (!d_chunks) return UWW_ERR_INVALID_ARG;
+    return launch(ctx, d_chunks, n, max_cells, out, true);
+}
+
+int uww_build_chunks_from_samples(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint32_t max_cells,
+                                  const float* d_samples, const uww_mesh_out* out)
+{
+    if (!ctx) return UWW_ERR_INVALID_ARG;
+    int st = check_out(out);
+    if (st) return st;
+    if (max_cells < 1 || max_cells > UWW_MAX_CELLS) return UWW_ERR_INVALID_ARG;
+    if (n == 0) {
+        if (out->totals) return cuda_status(cudaMemsetAsync(out->totals, 0, 4 * sizeof(uint64_t), ctx->stream));
+        return UWW_OK;
+    }
+    if (!d_chunks || !d_samples) return UWW_ERR_INVALID_ARG;
+    return launch(ctx, d_chunks, n, max_cells, out, true, d_samples);
+}
+
+int uww_build_chunk_plain(uww_ctx* ctx, const uww_chunk_desc* d_chunk, uint32_t cells, const uww_mesh_out* out)
+{
+    if (!ctx || !d_chunk) return UWW_ERR_INVALID_ARG;
+    int st = check_out(out);
+    if (st) return st;
+    if (!out->totals) return UWW_ERR_INVALID_ARG;
+    if (cells < 1 || cells > UWW_MAX_CELLS) return UWW_ERR_INVALID_ARG;
+    return launch(ctx, d_chunk, 1, cells, out, false);
+}
+
+int uww_build_chunks_host(uww_ctx* ctx, const uww_chunk_desc* h_chunks, uint32_t n, const uww_mesh_out* h_out)
+{
+    if (!ctx) return UWW_ERR_INVALID_ARG;
+    int st = check_out(h_out);
+    if (st) return st;
+    if (n && !h_chunks) return UWW_ERR_INVALID_ARG;
+    const bool want_cases = (ctx->params.outputs & UWW_OUT_CASES) && h_out->cases;
+    const bool want_normals = (ctx->params.outputs & UWW_OUT_NORMALS) && h_out->normals;
+    const bool want_samples = (ctx->params.outputs & UWW_OUT_SAMPLES) && h_out->samples;
+    uint32_t max_cells = 1;
+    uint64_t case_bytes = 0, sample_count = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        const uint32_t c = h_chunks[i].cells;
+        if (c < 1 || c > UWW_MAX_CELLS) return UWW_ERR_INVALID_ARG;
+        max_cells = std::max(max_cells, c);
+        case_bytes = std::max<uint64_t>(case_bytes, (uint64_t)h_chunks[i].cell_offset + (uint64_t)c * c * c);
+        sample_count = std::max<uint64_t>(sample_count,
+                                          (uint64_t)h_chunks[i].sample_offset + (uint64_t)(c + 1) * (c + 1) * (c + 1));
+    }
+    if (n == 0) {
+        if (h_out->totals) std::memset(h_out->totals, 0, 4 * sizeof(uint64_t));
+        return UWW_OK;
+    }
+    cudaStream_t s = ctx->stream;
+    if ((st = ensure_device(&ctx->d_chunks, &ctx->chunks_cap, (size_t)n * sizeof(uww_chunk_desc)))) return st;
+    if ((st = ensure_device(&ctx->d_records, &ctx->records_cap, (size_t)n * sizeof(uww_chunk_record)))) return st;
+    if ((st = ensure_device(&ctx->d_verts, &ctx->verts_cap, (size_t)h_out->vert_capacity * sizeof(uww_vert_color)))) return st;
+    if ((st = ensure_device(&ctx->d_inds, &ctx->inds_cap, (size_t)h_out->ind_capacity * sizeof(uint32_t)))) return st;
+    if (want_normals && (st = ensure_device(&ctx->d_normals, &ctx->normals_cap, (size_t)h_out->vert_capacity * 12))) return st;
+    if (want_cases && (st = ensure_device(&ctx->d_cases, &ctx->cases_cap, (size_t)case_bytes))) return st;
+    if (want_samples && (st = ensure_device(&ctx->d_samples, &ctx->samples_cap, (size_t)sample_count * 4))) return st;
+
+    cudaError_t e = cudaMemcpyAsync(ctx->d_chunks, h_chunks, (size_t)n * sizeof(uww_chunk_desc), cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return cuda_status(e);
+    uww_mesh_out d_out;
+    d_out.verts = (uww_vert_color*)ctx->d_verts;
+    d_out.normals = want_normals ? (float*)ctx->d_normals : nullptr;
+    d_out.inds = (uint32_t*)ctx->d_inds;
+    d_out.cases = want_cases ? (uint8_t*)ctx->d_cases : nullptr;
+    d_out.samples = want_samples ? (float*)ctx->d_samples : nullptr;
+    d_out.records = (uww_chunk_record*)ctx->d_records;
+    d_out.totals = reinterpret_cast<uint64_t*>(ctx->d_totals);
+    d_out.vert_capacity = h_out->vert_capacity;
+    d_out.ind_capacity = h_out->ind_capacity;
+    if ((st = launch(ctx, ctx->d_chunks, n, max_cells, &d_out, true))) return st;
+    if ((e = cudaMemcpyAsync(h_out->records, ctx->d_records, (size_t)n * sizeof(uww_chunk_record), cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+        return cuda_status(e);
+    if ((e = cudaMemcpyAsync(ctx->h_totals, ctx->d_totals, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+        return cuda_status(e);
+    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_status(e);
+    const uint64_t tv = std::min<uint64_t>(ctx->h_totals[0], h_out->vert_capacity);
+    const uint64_t ti = std::min<uint64_t>(ctx->h_totals[1], h_out->ind_capacity);
+    if (tv && (e = cudaMemcpyAsync(h_out->verts, ctx->d_verts, tv * sizeof(uww_vert_color), cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+        return cuda_status(e);
+    if (tv && want_normals && (e = cudaMemcpyAsync(h_out->normals, ctx->d_normals, tv * 12, cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+        return cuda_status(e);
+    if (ti && (e = cudaMemcpyAsync(h_out->inds, ctx->d_inds, ti * sizeof(uint32_t), cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+        return cuda_status(e);
+    if (want_cases && case_bytes && (e = cudaMemcpyAsync(h_out->cases, ctx->d_cases, case_bytes, cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+        return cuda_status(e);
+    if (want_samples && sample_count &&
+        (e = cudaMemcpyAsync(h_out->samples, ctx->d_samples, sample_count * 4, cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+        return cuda_status(e);
+    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_status(e);
+    if (h_out->totals) std::memcpy(h_out->totals, ctx->h_totals, 4 * sizeof(uint64_t));
+    if (ctx->h_totals[3] & kErrTimeout) return UWW_ERR_TIMEOUT;
+    if (ctx->h_totals[3] & kErrBadChunk) return UWW_ERR_INVALID_ARG;
+    if (ctx->h_totals[2]) return UWW_ERR_CAPACITY;
+    return UWW_OK;
+}
+
+int uww_ctx_set_tuning(uww_ctx* ctx, const uww_tuning* t)
+{
+    if (!ctx || !t) return UWW_ERR_INVALID_ARG;
+    if (t->threads < 0 || t->threads > 512 || (t->threads % 32) != 0) return UWW_ERR_INVALID_ARG;
+    if (t->blocks_per_sm < 0 || t->blocks_per_sm > 32) return UWW_ERR_INVALID_ARG;
+    if (t->smem_cells < 0 || t->smem_cells > UWW_MAX_CELLS) return UWW_ERR_INVALID_ARG;
+    ctx->threads = t->threads;
+    ctx->blocks_per_sm = t->blocks_per_sm;
+    ctx->smem_cells = t->smem_cells;
+    return UWW_OK;
+}
+
+int uww_ctx_get_tuning(const uww_ctx* ctx, uww_tuning* t)
+{
+    if (!ctx || !t) return UWW_ERR_INVALID_ARG;
+    t->threads = ctx->threads;
+    t->blocks_per_sm = ctx->blocks_per_sm;
+    t->smem_cells = ctx->smem_cells;
+    t->reserved = 0;
+    return UWW_OK;
+}
+
+int uww_device_alloc(size_t bytes, void** out)
+{
+    if (!out) return UWW_ERR_INVALID_ARG;
+    *out = nullptr;
+    return cuda_status(cudaMalloc(out, bytes ? bytes : 1));
+}
+
+int uww_device_free(void* p) { return cuda_status(cudaFree(p)); }
+
+int uww_host_alloc(size_t bytes, void** out)
+{
+    if (!out) return UWW_ERR_INVALID_ARG;
+    *out = nullptr;
+    return cuda_status(cudaMallocHost(out, bytes ? bytes : 1));
+}
+
+int uww_host_free(void* p) { return cuda_status(cudaFreeHost(p)); }
+
+int uww_memcpy(uww_ctx* ctx, void* dst, const void* src, size_t bytes, int kind)
+{
+    if (!ctx || (bytes && (!dst || !src))) return UWW_ERR_INVALID_ARG;
+    cudaMemcpyKind k;
+    switch (kind) {
+    case 0: k = cudaMemcpyHostToDevice; break;
+    case 1: k = cudaMemcpyDeviceToHost; break;
+    case 2: k = cudaMemcpyDeviceToDevice; break;
+    default: return UWW_ERR_INVALID_ARG;
+    }
+    if (!bytes) return UWW_OK;
+    return cuda_status(cudaMemcpyAsync(dst, src, bytes, k, ctx->stream));
+}
+
+int uww_memset(uww_ctx* ctx, void* dst, int value, size_t bytes)
+{
+    if (!ctx || (bytes && !dst)) return UWW_ERR_INVALID_ARG;
+    if (!bytes) return UWW_OK;
+    return cuda_status(cudaMemsetAsync(dst, value, bytes, ctx->stream));
+}
+
+int uww_density_at(uww_ctx* ctx, const float* d_xyz, uint32_t n, float* d_out)
+{
+    if (!ctx || (n && (!d_xyz || !d_out))) return UWW_ERR_INVALID_ARG;
+    return cuda_status(launch_density(ctx->dev, d_xyz, n, d_out, ctx->stream));
+}
+
+}  // extern "C"
+#pragma GCC visibility pop

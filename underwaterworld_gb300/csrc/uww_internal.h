@@ -1,0 +1,81 @@
+// uww_internal.h -- host/device shared declarations of libuww_gb300.
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "uww.h"
+#include "uww_device.cuh"
+
+namespace uww {
+
+// Per-chunk working set, in shared memory when it fits, else in a global
+// scratch slot owned by the CTA.  Offsets are 16-byte aligned.
+struct ChunkLayout {
+    uint32_t rho;      // (N+1)^3 f32 samples, index (x*S + y)*S + z
+    uint32_t cases;    // N^3 u8 case indices, cell order x, y, z
+    uint32_t vbase;    // N^3 u32: first chunk-local vertex id created by each cell
+    uint32_t active;   // active-cell list (u16 when N^3 <= 65536, else u32)
+    uint32_t ibase;    // per active cell: first index position (u32)
+    uint32_t total;
+    bool active16;
+};
+
+__host__ __device__ inline uint32_t align16(uint32_t v) { return (v + 15u) & ~15u; }
+
+__host__ __device__ inline ChunkLayout chunk_layout(int N)
+{
+    ChunkLayout L;
+    const uint32_t S = (uint32_t)N + 1, NC = (uint32_t)N * N * N;
+    L.active16 = NC <= 65536u;
+    uint32_t o = 0;
+    L.rho = o;    o = align16(o + S * S * S * 4u);
+    L.cases = o;  o = align16(o + NC);
+    L.vbase = o;  o = align16(o + NC * 4u);
+    L.active = o; o = align16(o + NC * (L.active16 ? 2u : 4u));
+    L.ibase = o;  o = align16(o + NC * 4u);
+    L.total = o;
+    return L;
+}
+
+// Lookback word: [63:62] status, [61:30] indices, [29:0] vertices.
+constexpr unsigned long long kLbAggregate = 1ull << 62;
+constexpr unsigned long long kLbInclusive = 2ull << 62;
+constexpr unsigned long long kLbVertMax = (1ull << 30) - 1;
+constexpr unsigned long long kLbIndMax = (1ull << 32) - 1;
+
+// totals[3] error bits
+constexpr unsigned long long kErrTimeout = 1ull;
+constexpr unsigned long long kErrBadChunk = 2ull;
+
+struct BuildArgs {
+    const uww_chunk_desc* chunks;
+    uint32_t n;
+    uint32_t max_cells;
+    uww_vert_color* verts;
+    float* normals;
+    uint32_t* inds;
+    uint8_t* cases;
+    float* samples_out;              // optional copy of each chunk's density samples
+    const float* samples_in;         // when set, samples are read instead of computed
+    uww_chunk_record* records;
+    unsigned long long* totals;      // never NULL inside the kernel
+    uint32_t vert_capacity;
+    uint32_t ind_capacity;
+    unsigned long long* lookback;    // n words, zeroed before the launch (queue mode)
+    unsigned int* work_counter;      // zeroed before the launch (queue mode)
+    uint8_t* scratch;                // per-CTA slots for chunks above smem_cells
+    size_t scratch_slot_bytes;
+    uint32_t smem_cells;             // chunks with cells <= smem_cells work in shared memory
+    long long spin_limit_cycles;     // bound on every device-side wait
+};
+
+// Launch helpers (uww_build.cu).
+size_t build_static_smem_bytes();
+cudaError_t launch_build(const DevParams& p, const BuildArgs& a, bool queue, int grid, int threads,
+                         size_t dyn_smem, cudaStream_t s);
+cudaError_t build_occupancy(bool queue, bool exact, int threads, size_t dyn_smem, int* blocks_per_sm);
+cudaError_t prepare_build_kernels(size_t max_dyn_smem);
+cudaError_t launch_density(const DevParams& p, const float* xyz, uint32_t n, float* out, cudaStream_t s);
+
+}  // namespace uww
