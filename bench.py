@@ -1,0 +1,413 @@
+"""Chunk-generation benchmark: batched GB300 build vs one-chunk-per-launch vs CPU.
+
+Workload (one step): build every chunk of the uniform grid -- 16x16x16 = 4096
+chunks of 12^3 cells (13^3 = 2197 f32 samples each, 9.0M samples), 4-octave
+fBm (base frequency 0.04, lacunarity 2, persistence 0.5) minus 0.03*(z-128),
+iso-level 0 -- with permutation seed (step % 10), producing VertColor
+vertices, unit normals and u32 indices per chunk plus per-chunk records.
+
+  value    chunks/s of the batched persistent build (fast build, FMA on),
+           inputs resident in HBM, CUDA events on the context stream, L2
+           flushed (256 MiB write) before every timed step.
+  e2e      chunks/s through uww_build_chunks_host with pinned host buffers:
+           descriptor upload, build, record/vertex/normal/index download.
+  plain    chunks/s of the plain form: one launch per chunk (the drop-in of
+           Chunk::build_full), same kernel code.
+  exact    chunks/s of the parity build (reference f32 order, no FMA).
+
+``--impl reference`` times the reference algorithm on the host cores instead:
+the CPU oracle in reference semantics (f64 noise, O(V) linear dedup search,
+powf colours), with all host threads, on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+import numpy as np  # noqa: E402
+
+METRIC = "chunks/s (noise+MC, batched vs per-chunk) & fwd+adjoint Mvox/s on 1 GB300"
+UNIT = "chunks/s"
+N_SEEDS = 10
+
+# Algorithmic FP32 work of the noise stage, counted on the reference
+# formulation (one flop per add/sub/mul/div/floor):
+FLOPS_PER_OCTAVE = 83          # one Perlin evaluation + fBm accumulate
+FLOPS_PER_SAMPLE_EXTRA = 16    # world coordinates, normalisation, linear bias
+FLOPS_PER_OCTAVE_GRAD = 254    # Perlin value + analytic gradient + accumulate (normals)
+FLOPS_PER_VERTEX_EXTRA = 60    # interpolation, colour ramp, normalisation
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--plain-steps", type=int, default=2)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--quick", action="store_true", help="skip plain/exact/e2e legs (profiling runs)")
+    ap.add_argument("--threads", type=int, default=0, help="threads per CTA (0: tuned/automatic)")
+    ap.add_argument("--bps", type=int, default=0, help="resident CTAs per SM (0: tuned/automatic)")
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in Path(self.path).read_text().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_model():
+    try:
+        for line in Path("/proc/cpuinfo").read_text().splitlines():
+            if line.lower().startswith(("model name", "cpu model")):
+                return line.split(":", 1)[1].strip()
+        out = subprocess.run(["lscpu"], capture_output=True, text=True).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name"):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
+
+
+def workload(seed):
+    from underwaterworld_gb300 import abi, workloads
+    return workloads.uniform_grid(seed=seed, outputs=abi.UWW_OUT_COLOR | abi.UWW_OUT_NORMALS)
+
+
+def cpu_reference(descs, seeds, threads, budget_s=20.0):
+    """The reference algorithm on the host: oracle in f64 reference semantics with
+    the O(V) dedup search and colours (no normals, like the reference)."""
+    from oracle import oracle as O
+    from underwaterworld_gb300 import abi
+    O.build()
+    done, t0, i = 0, time.perf_counter(), 0
+    while True:
+        p, _ = workload(seeds[i % len(seeds)])
+        p.outputs = abi.UWW_OUT_COLOR
+        O.build_chunks(p, descs, precision=O.F64, search=O.SEARCH_LINEAR, threads=threads)
+        done += len(descs)
+        i += 1
+        el = time.perf_counter() - t0
+        if el > budget_s or i >= len(seeds):
+            return done / el, done, el
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from underwaterworld_gb300.chunk import make_descs  # noqa: F401
+    _, descs = workload(0)
+    threads = os.cpu_count() or 1
+    vals = []
+    # warm-up: build the oracle and touch the code once on a small sample
+    for _ in range(max(args.warmup, 0)):
+        cpu_reference(descs[:64], [0], threads, budget_s=1.0)
+    steps = max(1, min(args.steps, 3))
+    for s in range(steps):
+        v, n, el = cpu_reference(descs, [s % N_SEEDS], threads, budget_s=60.0)
+        vals.append(v)
+    value = statistics.median(vals)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0, "steps": steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * len(descs) / value, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "uniform grid 16x16x16 chunks of 12^3 cells, 4-oct fBm f=0.04, bias -0.03(z-128), iso 0",
+                   "chunks_per_step": int(len(descs)), "threads": threads},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"full 4096-chunk grid per step, {threads} threads, CPU: {cpu_model()}"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    rank, world, local = dist_env()
+    import torch
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+
+    from underwaterworld_gb300 import abi, build as B
+    from underwaterworld_gb300.chunk import Context, HostArray
+    B.build()
+    L = abi.lib()
+    # One explicit stream for everything: the library's launches, torch's own
+    # work (L2 flush, copies) and the timing events.  (The default stream's
+    # handle is 0, which would make the library create a stream of its own.)
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.set_stream(stream)
+    assert stream.cuda_stream != 0
+
+    params, descs = [], None
+    for s in range(N_SEEDS):
+        p, d = workload((s + rank * N_SEEDS) % 1000)
+        p.math_mode = abi.UWW_MATH_FAST
+        params.append(p)
+        descs = d
+    n = len(descs)
+    ctx = Context(params[0], stream=stream.cuda_stream)
+    if args.threads or args.bps:
+        ctx.set_tuning(threads=args.threads, blocks_per_sm=args.bps)
+
+    d_desc = torch.from_numpy(descs.view(np.uint8).copy()).to(dev)
+    # capacity: one sizing pass per seed
+    vcap, icap = 1 << 20, 1 << 22
+    out_t = {}
+
+    def alloc(vc, ic):
+        out_t["verts"] = torch.empty(vc * 24, dtype=torch.uint8, device=dev)
+        out_t["normals"] = torch.empty(vc * 12, dtype=torch.uint8, device=dev)
+        out_t["inds"] = torch.empty(ic * 4, dtype=torch.uint8, device=dev)
+        out_t["records"] = torch.empty(n * 32, dtype=torch.uint8, device=dev)
+        out_t["totals"] = torch.zeros(4, dtype=torch.int64, device=dev)
+        return abi.MeshOut(out_t["verts"].data_ptr(), out_t["normals"].data_ptr(), out_t["inds"].data_ptr(), None,
+                           None, out_t["records"].data_ptr(), out_t["totals"].data_ptr(), vc, ic)
+
+    out = alloc(vcap, icap)
+    maxv = maxi = 0
+    for p in params:
+        ctx.set_params(p)
+        abi.check(L.uww_build_chunks(ctx.h, C.c_void_p(d_desc.data_ptr()), n, 12, C.byref(out)), "build")
+        tot = out_t["totals"].cpu().numpy()
+        maxv, maxi = max(maxv, int(tot[0])), max(maxi, int(tot[1]))
+    vcap, icap = int(maxv * 1.1) + 1024, int(maxi * 1.1) + 4096
+    out = alloc(vcap, icap)
+
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def step(i, o=None):
+        ctx.set_params(params[i % N_SEEDS])
+        abi.check(L.uww_build_chunks(ctx.h, C.c_void_p(d_desc.data_ptr()), n, 12, C.byref(o or out)), "build")
+
+    for i in range(args.warmup):
+        step(i)
+    torch.cuda.synchronize()
+    tot = out_t["totals"].cpu().numpy()
+    assert int(tot[2]) == 0 and int(tot[3]) == 0, tot
+
+    # ---- timed batched steps ----
+    clocks = ClockSampler(local)
+    clocks.start()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    times, verts_sum, inds_sum = [], 0, 0
+    for i in range(args.steps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        step(i)
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1) * 1e-3)
+        tot = out_t["totals"].cpu().numpy()
+        verts_sum += int(tot[0])
+        inds_sum += int(tot[1])
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clk = clocks.stop()
+    t_total = sum(times)
+    if world > 1:
+        tt = torch.tensor([t_total], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_total = float(tt.item())
+    value = world * n * args.steps / t_total
+    ms_step = 1e3 * t_total / args.steps
+
+    extra = {}
+    if not args.quick:
+        # ---- exact (parity) build ----
+        ex_times = []
+        for i in range(max(3, args.steps // 2)):
+            q = params[i % N_SEEDS].copy()
+            q.math_mode = abi.UWW_MATH_EXACT
+            ctx.set_params(q)
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            abi.check(L.uww_build_chunks(ctx.h, C.c_void_p(d_desc.data_ptr()), n, 12, C.byref(out)), "build")
+            e1.record(stream)
+            e1.synchronize()
+            ex_times.append(e0.elapsed_time(e1) * 1e-3)
+        extra["exact_chunks_per_s"] = n / statistics.mean(ex_times)
+
+        # ---- plain: one launch per chunk, each into its own slot ----
+        ctx.set_params(params[0])
+        per = 15 * 12 ** 3
+        pv = torch.empty(n * per * 24, dtype=torch.uint8, device=dev)
+        pn = torch.empty(n * per * 12, dtype=torch.uint8, device=dev)
+        pi = torch.empty(n * per * 4, dtype=torch.uint8, device=dev)
+        pr = torch.empty(n * 32, dtype=torch.uint8, device=dev)
+        pt = torch.empty(n * 32, dtype=torch.uint8, device=dev)
+        outs = [abi.MeshOut(pv.data_ptr() + k * per * 24, pn.data_ptr() + k * per * 12, pi.data_ptr() + k * per * 4,
+                            None, None, pr.data_ptr() + 32 * k, pt.data_ptr() + 32 * k, per, per) for k in range(n)]
+        base = d_desc.data_ptr()
+        fn = L.uww_build_chunk_plain
+        for k in range(64):
+            fn(ctx.h, C.c_void_p(base + 32 * k), 12, C.byref(outs[k]))
+        torch.cuda.synchronize()
+        pl = []
+        for _ in range(args.plain_steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for k in range(n):
+                fn(ctx.h, C.c_void_p(base + 32 * k), 12, C.byref(outs[k]))
+            e1.record(stream)
+            e1.synchronize()
+            pl.append(e0.elapsed_time(e1) * 1e-3)
+        extra["plain_chunks_per_s"] = n / statistics.mean(pl)
+        del pv, pn, pi
+
+        # ---- e2e through the host-buffer API with pinned buffers ----
+        h_desc = HostArray((n,), abi.CHUNK_DESC_DTYPE)
+        h_desc.array[:] = descs
+        h_rec = HostArray((n,), abi.CHUNK_RECORD_DTYPE)
+        h_v = HostArray((vcap,), abi.VERT_COLOR_DTYPE)
+        h_n = HostArray((vcap, 3), np.float32)
+        h_i = HostArray((icap,), np.uint32)
+        h_t = np.zeros(4, np.uint64)
+        hout = abi.MeshOut(h_v.ptr, h_n.ptr, h_i.ptr, None, None, h_rec.ptr, h_t.ctypes.data, vcap, icap)
+        e2e_t, h2d, d2h = [], 0, 0
+        for i in range(args.warmup + args.steps):
+            ctx.set_params(params[i % N_SEEDS])
+            t0 = time.perf_counter()
+            abi.check(L.uww_build_chunks_host(ctx.h, C.c_void_p(h_desc.ptr), n, C.byref(hout)), "host build")
+            t1 = time.perf_counter()
+            if i >= args.warmup:
+                e2e_t.append(t1 - t0)
+                h2d += n * 32
+                d2h += n * 32 + 32 + int(h_t[0]) * (24 + 12) + int(h_t[1]) * 4
+        k = len(e2e_t)
+        extra["e2e"] = {"value": world * n / statistics.mean(e2e_t), "unit": UNIT,
+                        "h2d_bytes_per_step": h2d // k, "d2h_bytes_per_step": d2h // k}
+
+    # ---- FP32 peak probe (roofline denominator) ----
+    sink = torch.empty(152 * 8 * 256, dtype=torch.float32, device=dev)
+    fl = C.c_double()
+    for _ in range(2):
+        L.uww_probe_fma(ctx.h, 152 * 8, 4096, C.c_void_p(sink.data_ptr()), C.byref(fl))
+    torch.cuda.synchronize()
+    pk = []
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        L.uww_probe_fma(ctx.h, 152 * 8, 4096, C.c_void_p(sink.data_ptr()), C.byref(fl))
+        e1.record(stream)
+        e1.synchronize()
+        pk.append(fl.value / (e0.elapsed_time(e1) * 1e-3))
+    fp32_peak = max(pk) / 1e12
+
+    samples = n * 13 ** 3
+    mean_v, mean_i = verts_sum / args.steps, inds_sum / args.steps
+    oct_ = params[0].octaves
+    flops = samples * (oct_ * FLOPS_PER_OCTAVE + FLOPS_PER_SAMPLE_EXTRA) + \
+        mean_v * (oct_ * FLOPS_PER_OCTAVE_GRAD + FLOPS_PER_VERTEX_EXTRA)
+    achieved = flops / (t_total / args.steps) / 1e12
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded chunk grid; seeds 0-9 cycle per step)",
+        "config": {"workload": "uniform grid: 16x16x16 = 4096 chunks of 12^3 cells (13^3 f32 samples), "
+                               "4-oct fBm f=0.04 lac 2 pers 0.5, bias -0.03(z-128), iso 0; "
+                               "outputs VertColor + normals + u32 indices",
+                   "chunks_per_step": n, "cells_per_step": n * 12 ** 3, "samples_per_step": samples,
+                   "build": "fast (FMA), persistent grid + device work queue + decoupled look-back",
+                   "l2": "flushed (256 MiB write) before each timed step",
+                   "mean_verts_per_step": mean_v, "mean_inds_per_step": mean_i},
+        "mvoxels_per_s": value * 12 ** 3 / 1e6,
+        "msamples_per_s": value * 13 ** 3 / 1e6,
+        "gpu_launches": args.steps,
+        "clocks": clk,
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                     "frac": achieved / fp32_peak, "traffic": None,
+                     "peak_source": "measured live: FMA probe kernel (uww_probe_fma), 152x8 CTAs",
+                     "flops_per_step": flops},
+    }
+    line.update({k: v for k, v in extra.items() if k != "e2e"})
+    if "e2e" in extra:
+        line["e2e"] = extra["e2e"]
+    if "plain_chunks_per_s" in extra:
+        line["batched_over_plain"] = value / world / extra["plain_chunks_per_s"]
+
+    if rank == 0 and not args.no_cpu and not args.quick:
+        cv, cn, cel = cpu_reference(descs, [0], 1, budget_s=30.0)
+        line["cpu_baseline"] = {"value": cv, "unit": UNIT, "cores": 1, "kind": "port",
+                                "sample": f"{cn} chunks (full seed-0 grid) in {cel:.1f} s, oracle f64 reference "
+                                          f"semantics with linear dedup search, 1 thread, CPU: {cpu_model()}"}
+    if rank == 0:
+        print(json.dumps(line))
+    ctx.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

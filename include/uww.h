@@ -130,13 +130,24 @@ typedef struct uww_mesh_out {
     uint64_t*         totals;     /* device/host [4]: verts, inds, overflowed chunks, error flags; or NULL */
     uint32_t          vert_capacity;
     uint32_t          ind_capacity;
+    uint64_t          case_capacity;    /* bytes available at cases; a chunk whose cells would
+                                           fall outside is not written and raises UWW_ERRFLAG_RANGE */
+    uint64_t          sample_capacity;  /* floats available at samples; same rule             */
 } uww_mesh_out;
+
+/* totals[3] error flags of a device build */
+#define UWW_ERRFLAG_TIMEOUT 1u   /* a bounded device wait gave up (UWW_ERR_TIMEOUT)          */
+#define UWW_ERRFLAG_BAD     2u   /* a descriptor had cells outside 1..max_cells, or its
+                                    input samples lay outside the given sample array          */
+#define UWW_ERRFLAG_RANGE   4u   /* a per-cell or per-sample output lay outside its capacity */
 
 typedef struct uww_ctx uww_ctx;
 
 /* ---- library --------------------------------------------------------------- */
 int         uww_abi_version(void);
 const char* uww_status_string(int status);
+/* Text of the last CUDA error seen by a call on this host thread ("" if none). */
+const char* uww_last_error(void);
 
 /* Reference constants: chunk.rs:5-17, perlin_util.rs:6-29, world.rs:11-12; seed 0. */
 void uww_params_reference(uww_params* p);
@@ -170,7 +181,7 @@ int uww_build_chunks(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n,
  * (x*S + y)*S + z like Build::isos (chunk.rs:43, 351-353).  Otherwise as
  * uww_build_chunks. */
 int uww_build_chunks_from_samples(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint32_t max_cells,
-                                  const float* d_samples, const uww_mesh_out* out);
+                                  const float* d_samples, uint64_t sample_count, const uww_mesh_out* out);
 
 /* One chunk per launch: the direct drop-in for Chunk::build_full (chunk.rs:266-268).
  * d_chunk points to one device descriptor whose cells equal `cells`; out
@@ -186,7 +197,8 @@ int uww_build_chunks_host(uww_ctx* ctx, const uww_chunk_desc* h_chunks, uint32_t
 
 /* ---- tuning (written by the autotuner; 0 = automatic) ------------------------ */
 typedef struct uww_tuning {
-    int32_t threads;        /* threads per CTA (multiple of 32, <= 512)                     */
+    int32_t threads;        /* compute threads per CTA (multiple of 32, <= 192 or 224..512); the
+                               batched build adds one control warp                          */
     int32_t blocks_per_sm;  /* resident CTAs per SM of the persistent grid                   */
     int32_t smem_cells;     /* chunks up to this many cells per edge work in shared memory;
                                larger ones use a global scratch slot per CTA                */
@@ -208,6 +220,14 @@ int uww_memset(uww_ctx* ctx, void* dst, int value, size_t bytes);
 /* density(world xyz) for n points: perlin_util::iso_at (perlin_util.rs:24-29) with
  * (x,y,z) = world / CHUNK_SIZE as in boid.rs:132-137.  d_xyz: 3n floats; d_out: n. */
 int uww_density_at(uww_ctx* ctx, const float* d_xyz, uint32_t n, float* d_out);
+
+/* ---- diagnostics --------------------------------------------------------------- */
+/* FP32 roofline probe: launches `blocks` CTAs of 256 threads, each running
+ * iters*128 independent FMAs, on the context stream; *flops receives the flop
+ * count (2 per FMA) so that flops / elapsed time is the achievable FP32 rate.
+ * d_sink: blocks*256 floats.  No counterpart in the reference (used to state
+ * the FP32 peak the noise stage is measured against). */
+int uww_probe_fma(uww_ctx* ctx, uint32_t blocks, uint32_t iters, float* d_sink, double* flops);
 
 #ifdef __cplusplus
 }

@@ -41,7 +41,7 @@ def lib():
         L.oracle_perm.argtypes = [C.c_uint32, P]
         L.oracle_perm.restype = None
         L.oracle_build_chunks.argtypes = [C.POINTER(abi.Params), C.c_int, C.c_int, P, C.c_uint32,
-                                          C.POINTER(abi.MeshOut), C.c_int, P]
+                                          C.POINTER(abi.MeshOut), C.c_int, P, C.c_uint64]
         L.oracle_build_chunks.restype = C.c_int
         L.oracle_sample_grid.argtypes = [C.POINTER(abi.Params), C.c_int, P, P]
         L.oracle_sample_grid.restype = C.c_int
@@ -79,10 +79,10 @@ def build_chunks(params: abi.Params, descs: np.ndarray, precision: int = F32, se
         return a.ctypes.data if a is not None else None
 
     out = abi.MeshOut(ptr(verts), ptr(normals), ptr(inds), ptr(cases), ptr(samples), ptr(records), ptr(totals),
-                      vcap, icap)
+                      vcap, icap, cases.size if cases is not None else 0, samples.size if samples is not None else 0)
     sin = np.ascontiguousarray(samples_in, dtype=np.float32) if samples_in is not None else None
     st = lib().oracle_build_chunks(C.byref(params), precision, search, descs.ctypes.data_as(C.c_void_p), n,
-                                   C.byref(out), threads, ptr(sin))
+                                   C.byref(out), threads, ptr(sin), sin.size if sin is not None else 0)
     if st not in (abi.UWW_OK, abi.UWW_ERR_CAPACITY):
         raise RuntimeError(f"oracle_build_chunks failed: {st}")
     nv, ni = min(int(totals[0]), vcap), min(int(totals[1]), icap)

@@ -450,9 +450,9 @@ typedef struct {
     const uww_chunk_desc* chunks;
     uint32_t n;
     chunk_build* builds;
-    uint8_t* cases;
-    float* samples_out;
-    const float* samples_in;
+    uint8_t** cases_at;
+    float** samples_out_at;
+    const float** samples_in_at;
     volatile uint32_t* next;
     pthread_mutex_t* mu;
 } worker_args;
@@ -466,16 +466,14 @@ static void* worker(void* arg)
         *a->next = i + 1;
         pthread_mutex_unlock(a->mu);
         if (i >= a->n) break;
-        uint8_t* cases = a->cases ? a->cases + a->chunks[i].cell_offset : NULL;
-        float* so = a->samples_out ? a->samples_out + a->chunks[i].sample_offset : NULL;
-        const float* si = a->samples_in ? a->samples_in + a->chunks[i].sample_offset : NULL;
-        build_chunk(a->cfg, &a->chunks[i], &a->builds[i], cases, so, si);
+        build_chunk(a->cfg, &a->chunks[i], &a->builds[i], a->cases_at[i], a->samples_out_at[i], a->samples_in_at[i]);
     }
     return NULL;
 }
 
 int oracle_build_chunks(const uww_params* p, int precision, int search, const uww_chunk_desc* chunks,
-                        uint32_t n, const uww_mesh_out* out, int threads, const float* samples_in)
+                        uint32_t n, const uww_mesh_out* out, int threads, const float* samples_in,
+                        uint64_t samples_in_count)
 {
     if (!p || (!chunks && n) || !out || !out->records) return UWW_ERR_INVALID_ARG;
     for (uint32_t i = 0; i < n; ++i)
@@ -487,16 +485,33 @@ int oracle_build_chunks(const uww_params* p, int precision, int search, const uw
     if (!builds) return UWW_ERR_OOM;
     uint8_t* cases = (p->outputs & UWW_OUT_CASES) ? out->cases : NULL;
     float* samples_out = (p->outputs & UWW_OUT_SAMPLES) ? out->samples : NULL;
+    /* per-chunk pointers, each checked against the capacity it writes into */
+    uint8_t** cases_at = (uint8_t**)calloc(n ? n : 1, sizeof(uint8_t*));
+    float** so_at = (float**)calloc(n ? n : 1, sizeof(float*));
+    const float** si_at = (const float**)calloc(n ? n : 1, sizeof(float*));
+    uint64_t errflags = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        const uint64_t c = chunks[i].cells, nc = c * c * c, ns = (c + 1) * (c + 1) * (c + 1);
+        if (samples_in) {
+            if (chunks[i].sample_offset + ns > samples_in_count) { free(builds); free(cases_at); free(so_at); free(si_at); return UWW_ERR_INVALID_ARG; }
+            si_at[i] = samples_in + chunks[i].sample_offset;
+        }
+        if (cases) {
+            if (chunks[i].cell_offset + nc <= out->case_capacity) cases_at[i] = cases + chunks[i].cell_offset;
+            else errflags |= UWW_ERRFLAG_RANGE;
+        }
+        if (samples_out) {
+            if (chunks[i].sample_offset + ns <= out->sample_capacity) so_at[i] = samples_out + chunks[i].sample_offset;
+            else errflags |= UWW_ERRFLAG_RANGE;
+        }
+    }
 
     if (threads <= 1 || n <= 1) {
-        for (uint32_t i = 0; i < n; ++i)
-            build_chunk(&cfg, &chunks[i], &builds[i], cases ? cases + chunks[i].cell_offset : NULL,
-                        samples_out ? samples_out + chunks[i].sample_offset : NULL,
-                        samples_in ? samples_in + chunks[i].sample_offset : NULL);
+        for (uint32_t i = 0; i < n; ++i) build_chunk(&cfg, &chunks[i], &builds[i], cases_at[i], so_at[i], si_at[i]);
     } else {
         volatile uint32_t next = 0;
         pthread_mutex_t mu = PTHREAD_MUTEX_INITIALIZER;
-        worker_args a = {&cfg, chunks, n, builds, cases, samples_out, samples_in, &next, &mu};
+        worker_args a = {&cfg, chunks, n, builds, cases_at, so_at, si_at, &next, &mu};
         pthread_t* tid = (pthread_t*)malloc(sizeof(pthread_t) * (size_t)threads);
         for (int t = 0; t < threads; ++t) pthread_create(&tid[t], NULL, worker, &a);
         for (int t = 0; t < threads; ++t) pthread_join(tid[t], NULL);
@@ -533,9 +548,13 @@ int oracle_build_chunks(const uww_params* p, int precision, int search, const uw
         out->totals[0] = vo;
         out->totals[1] = io;
         out->totals[2] = overflow;
-        out->totals[3] = 0;
+        out->totals[3] = errflags;
     }
     free(builds);
+    free(cases_at);
+    free(so_at);
+    free(si_at);
+    if (errflags && status == UWW_OK) status = UWW_ERR_INVALID_ARG;
     return status;
 }
 

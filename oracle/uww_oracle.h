@@ -20,7 +20,8 @@ extern "C" {
 void   oracle_perm(uint32_t seed, uint8_t P[256]);
 /* samples_in (optional): build from these samples (at desc.sample_offset) instead of the noise */
 int    oracle_build_chunks(const uww_params* p, int precision, int search, const uww_chunk_desc* chunks,
-                           uint32_t n, const uww_mesh_out* out, int threads, const float* samples_in);
+                           uint32_t n, const uww_mesh_out* out, int threads, const float* samples_in,
+                           uint64_t samples_in_count);
 int    oracle_sample_grid(const uww_params* p, int precision, const uww_chunk_desc* d, float* isos);
 int    oracle_density_at(const uww_params* p, int precision, const float* xyz, uint32_t n, float* out,
                          float* grad);

@@ -55,5 +55,10 @@ def params_for_samples(iso_level: float, outputs: int = abi.UWW_OUT_COLOR | abi.
     return p
 
 
+def relayout(descs):
+    """Descriptors of a subset, with their per-cell and per-sample offsets re-packed."""
+    return make_descs(descs["pos"], descs["cells"])
+
+
 def flipped_cells(cases_a: np.ndarray, cases_b: np.ndarray) -> int:
     return int(np.count_nonzero(cases_a != cases_b))

@@ -11,7 +11,8 @@ import pytest
 from underwaterworld_gb300 import abi, workloads
 from underwaterworld_gb300.chunk import Chunk, make_descs
 
-from helpers import assert_batches_equal, assert_records_equal, flipped_cells, load_golden, params_for_samples
+from helpers import (assert_batches_equal, assert_records_equal, flipped_cells, load_golden, params_for_samples,
+                     relayout)
 
 pytestmark = pytest.mark.gpu
 
@@ -64,7 +65,7 @@ def test_host_path_equals_device_path(ctx_factory, oracle):
 def test_uniform_grid_subset_bit_exact(ctx_factory, oracle):
     p, d = workloads.uniform_grid(seed=3, outputs=ALL)
     # the z-layers that straddle the surface, plus blank ones above and below
-    sel = d[(d["pos"][:, 0] < 6) & (d["pos"][:, 1] < 6)]
+    sel = relayout(d[(d["pos"][:, 0] < 6) & (d["pos"][:, 1] < 6)])
     ref = oracle.build_chunks(p, sel)
     got = ctx_factory(p).build_chunks_device(sel, *caps(ref))
     assert_batches_equal(got, ref)
@@ -83,7 +84,7 @@ def test_other_lods_bit_exact(ctx_factory, oracle, cells):
 
 def test_mixed_lod_batch_bit_exact(ctx_factory, oracle):
     p, d = workloads.mixed_lod(seed=2, outputs=ALL)
-    sel = d[:96]
+    sel = relayout(d[:96])
     ref = oracle.build_chunks(p, sel)
     got = ctx_factory(p).build_chunks_device(sel, *caps(ref))
     assert_batches_equal(got, ref)
@@ -162,7 +163,7 @@ def test_bad_descriptor_is_flagged_not_built(ctx_factory):
     ctx = ctx_factory(p)
     bad = d[:4].copy()
     bad["cells"][2] = 40  # above the max_cells the launch was given
-    b = ctx.build_chunks_device(bad[[0, 1, 3]], 5000, 20000)  # sanity: good chunks alone
+    b = ctx.build_chunks_device(relayout(bad[[0, 1, 3]]), 5000, 20000)  # sanity: good chunks alone
     assert b.status == abi.UWW_OK
     import ctypes as C
     from underwaterworld_gb300.chunk import DeviceArray
@@ -173,27 +174,90 @@ def test_bad_descriptor_is_flagged_not_built(ctx_factory):
     assert abi.lib().uww_build_chunks(ctx.h, C.c_void_p(d_desc.ptr), 4, 12, C.byref(out)) == abi.UWW_OK
     ctx.sync()
     tot = ctx.download(d_tot, (4,), np.uint64)
-    assert int(tot[3]) & 2
+    assert int(tot[3]) & abi.UWW_ERRFLAG_BAD
     rec = ctx.download(d_rec, (4,), abi.CHUNK_RECORD_DTYPE)
     assert rec["num_inds"][2] == 0
+
+
+def test_per_cell_outputs_are_range_checked(ctx_factory):
+    """A cases buffer smaller than the descriptors' cell offsets need: no write past it."""
+    import ctypes as C
+    from underwaterworld_gb300.chunk import DeviceArray
+    p, d = workloads.reference_grid(outputs=abi.UWW_OUT_CASES)
+    ctx = ctx_factory(p)
+    d = d[:8]
+    d_desc = ctx.upload(d)
+    d_rec, d_tot = DeviceArray(8 * 32), DeviceArray(32)
+    d_v, d_i = DeviceArray(50000 * 24), DeviceArray(200000 * 4)
+    cap = 3 * 12 ** 3 + 100  # room for three chunks' cases only
+    d_cases = DeviceArray(cap + 4096)
+    guard = np.full(cap + 4096, 0xAB, np.uint8)
+    abi.check(abi.lib().uww_memcpy(ctx.h, C.c_void_p(d_cases.ptr), guard.ctypes.data_as(C.c_void_p), guard.size, 0))
+    out = abi.MeshOut(d_v.ptr, None, d_i.ptr, d_cases.ptr, None, d_rec.ptr, d_tot.ptr, 50000, 200000, cap, 0)
+    assert abi.lib().uww_build_chunks(ctx.h, C.c_void_p(d_desc.ptr), 8, 12, C.byref(out)) == abi.UWW_OK
+    ctx.sync()
+    tot = ctx.download(d_tot, (4,), np.uint64)
+    assert int(tot[3]) & abi.UWW_ERRFLAG_RANGE
+    back = ctx.download(d_cases, (cap + 4096,), np.uint8)
+    assert np.all(back[cap:] == 0xAB), "nothing written past the capacity"
 
 
 def test_fast_build_against_f64_oracle(ctx_factory, oracle):
     """The FMA build: count flipped cells and the worst vertex error vs the f64 oracle."""
     p, d = workloads.uniform_grid(seed=0, outputs=abi.UWW_OUT_CASES)
-    sel = d[(d["pos"][:, 0] < 8) & (d["pos"][:, 1] < 8)]
+    sel = relayout(d[(d["pos"][:, 0] < 8) & (d["pos"][:, 1] < 8)])
     ref = oracle.build_chunks(p, sel, precision=oracle.F64)
     q = p.copy()
     q.math_mode = abi.UWW_MATH_FAST
     got = ctx_factory(q).build_chunks_device(sel, int(ref.totals[0]) + 4096, int(ref.totals[1]) + 16384)
+    exact = ctx_factory(p).build_chunks_device(sel, int(ref.totals[0]) + 4096, int(ref.totals[1]) + 16384)
+    assert got.status == abi.UWW_OK and exact.status == abi.UWW_OK
+
+    def vertex_error(b):
+        same = b.records["num_inds"] == ref.records["num_inds"]
+        errs = []
+        for i in np.nonzero(same & (ref.records["num_inds"] > 0))[0]:
+            gv, _, gi = b.chunk(i)
+            rv, _, ri = ref.chunk(i)
+            if np.array_equal(gi, ri):
+                errs.append(np.abs(gv["pos"] - rv["pos"]).max(axis=1))
+        e = np.concatenate(errs)
+        return float(e.max()), float(np.median(e))
+
+    flips_fast = flipped_cells(got.cases, ref.cases)
+    flips_exact = flipped_cells(exact.cases, ref.cases)
+    fast_max, fast_med = vertex_error(got)
+    exact_max, exact_med = vertex_error(exact)
+    print(f"vs f64 oracle over {len(ref.cases)} cells: fast build {flips_fast} flipped cells, max vertex error "
+          f"{fast_max:.3g} (median {fast_med:.3g}); exact f32 build {flips_exact} flipped, max {exact_max:.3g} "
+          f"(median {exact_med:.3g}) world units")
+    assert flips_fast <= 1e-4 * len(ref.cases), flips_fast
+    # f32 noise against f64 noise: errors concentrate on near-degenerate edges
+    # (both endpoint samples close to the iso-level); bound them at 1% of a cell
+    cell = 16.0 / 12
+    assert fast_max < 0.01 * cell and exact_max < 0.01 * cell, (fast_max, exact_max)
+    assert fast_med < 1e-4 and exact_med < 1e-4
+
+
+@pytest.mark.parametrize("which", ["reference", "mixed", "lod24"])
+def test_fast_build_other_workloads(ctx_factory, oracle, which):
+    """The fast (column) noise on the terraced reference world, mixed LODs and 24^3 chunks."""
+    if which == "reference":
+        p, d = workloads.reference_grid(outputs=abi.UWW_OUT_CASES)
+    elif which == "mixed":
+        p, d = workloads.mixed_lod(seed=1, outputs=abi.UWW_OUT_CASES)
+        d = relayout(d[:128])
+    else:
+        p, d = workloads.uniform_grid(seed=2, outputs=abi.UWW_OUT_CASES)
+        d = make_descs(d["pos"][(d["pos"][:, 2] >= 6) & (d["pos"][:, 2] <= 9)][:64], 24)
+    ref = oracle.build_chunks(p, d, precision=oracle.F64)
+    q = p.copy()
+    q.math_mode = abi.UWW_MATH_FAST
+    got = ctx_factory(q).build_chunks_device(d, int(ref.totals[0]) + 8192, int(ref.totals[1]) + 32768)
     assert got.status == abi.UWW_OK
     flips = flipped_cells(got.cases, ref.cases)
-    assert flips <= 1e-4 * len(ref.cases), flips
-    same = got.records["num_inds"] == ref.records["num_inds"]
-    err = 0.0
-    for i in np.nonzero(same & (ref.records["num_inds"] > 0))[0]:
-        gv, _, gi = got.chunk(i)
-        rv, _, ri = ref.chunk(i)
-        if np.array_equal(gi, ri):
-            err = max(err, float(np.abs(gv["pos"] - rv["pos"]).max()))
-    assert err < 1e-3, err
+    print(f"{which}: {flips} flipped of {len(ref.cases)} cells")
+    assert flips <= max(2, 1e-4 * len(ref.cases)), flips
+    blank_ref = (ref.records["flags"] & abi.UWW_CHUNK_HAS_MESH) > 0
+    blank_got = (got.records["flags"] & abi.UWW_CHUNK_HAS_MESH) > 0
+    assert np.count_nonzero(blank_ref != blank_got) <= 1

@@ -128,3 +128,10 @@ def test_empty_batch(oracle):
     p = abi.reference_params()
     b = oracle.build_chunks(p, make_descs(np.zeros((0, 3)), 12))
     assert b.totals[0] == 0 and b.totals[1] == 0 and len(b.records) == 0
+
+
+def test_oracle_range_checks_per_cell_outputs(oracle):
+    p, d = workloads.reference_grid(outputs=abi.UWW_OUT_CASES)
+    sub = d[[0, 5, 9]]  # offsets still those of the full grid: beyond a 3-chunk buffer
+    with pytest.raises(RuntimeError):
+        oracle.build_chunks(p, sub)

@@ -24,6 +24,7 @@ UWW_MATH_EXACT, UWW_MATH_FAST = 0, 1
 UWW_DEDUP_ORIENTED, UWW_DEDUP_EDGE = 0, 1
 UWW_OUT_COLOR, UWW_OUT_NORMALS, UWW_OUT_CASES, UWW_OUT_SAMPLES = 1, 2, 4, 8
 UWW_CHUNK_EARLY_BLANK, UWW_CHUNK_HAS_MESH, UWW_CHUNK_OVERFLOW = 1, 2, 4
+UWW_ERRFLAG_TIMEOUT, UWW_ERRFLAG_BAD, UWW_ERRFLAG_RANGE = 1, 2, 4
 H2D, D2H, D2D = 0, 1, 2
 
 
@@ -58,7 +59,8 @@ class ChunkRecord(C.Structure):
 class MeshOut(C.Structure):
     _fields_ = [("verts", C.c_void_p), ("normals", C.c_void_p), ("inds", C.c_void_p), ("cases", C.c_void_p),
                 ("samples", C.c_void_p), ("records", C.c_void_p), ("totals", C.c_void_p),
-                ("vert_capacity", C.c_uint32), ("ind_capacity", C.c_uint32)]
+                ("vert_capacity", C.c_uint32), ("ind_capacity", C.c_uint32),
+                ("case_capacity", C.c_uint64), ("sample_capacity", C.c_uint64)]
 
 
 class Tuning(C.Structure):
@@ -85,10 +87,11 @@ P = C.c_void_p
 _SIGS = {
     "uww_abi_version": (C.c_int, []),
     "uww_status_string": (C.c_char_p, [C.c_int]),
+    "uww_last_error": (C.c_char_p, []),
     "uww_params_reference": (None, [C.POINTER(Params)]),
     "uww_perm_table": (C.c_int, [C.c_uint32, P]),
     "uww_layout_cells": (C.c_int, [P, C.c_uint32, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
-    "uww_build_chunks_from_samples": (C.c_int, [P, P, C.c_uint32, C.c_uint32, P, C.POINTER(MeshOut)]),
+    "uww_build_chunks_from_samples": (C.c_int, [P, P, C.c_uint32, C.c_uint32, P, C.c_uint64, C.POINTER(MeshOut)]),
     "uww_ctx_create": (C.c_int, [C.POINTER(Params), P, C.POINTER(P)]),
     "uww_ctx_destroy": (C.c_int, [P]),
     "uww_ctx_set_params": (C.c_int, [P, C.POINTER(Params)]),
@@ -107,6 +110,7 @@ _SIGS = {
     "uww_memcpy": (C.c_int, [P, P, P, C.c_size_t, C.c_int]),
     "uww_memset": (C.c_int, [P, P, C.c_int, C.c_size_t]),
     "uww_density_at": (C.c_int, [P, P, C.c_uint32, P]),
+    "uww_probe_fma": (C.c_int, [P, C.c_uint32, C.c_uint32, P, C.POINTER(C.c_double)]),
 }
 
 _lib = None
@@ -116,6 +120,8 @@ class UWWError(RuntimeError):
     def __init__(self, status: int, what: str = ""):
         self.status = status
         msg = status_string(status) if _lib is not None else str(status)
+        if _lib is not None and status in (UWW_ERR_CUDA, UWW_ERR_OOM):
+            msg += " [" + _lib.uww_last_error().decode() + "]"
         super().__init__(f"{what}: {msg} ({status})" if what else f"{msg} ({status})")
 
 

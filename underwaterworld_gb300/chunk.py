@@ -204,7 +204,8 @@ class Context:
             return a.ctypes.data if a is not None else None
 
         out = abi.MeshOut(ptr(verts), ptr(normals), ptr(inds), ptr(cases), ptr(samples), ptr(records),
-                          ptr(totals), vert_capacity, ind_capacity)
+                          ptr(totals), vert_capacity, ind_capacity, cases.size if cases is not None else 0,
+                          samples.size if samples is not None else 0)
         st = lib().uww_build_chunks_host(self.h, descs.ctypes.data_as(C.c_void_p), n, C.byref(out))
         if st not in (abi.UWW_OK, abi.UWW_ERR_CAPACITY):
             raise abi.UWWError(st, "uww_build_chunks_host")
@@ -232,12 +233,14 @@ class Context:
         d_samp = DeviceArray(nsamp * 4) if want_samples else None
         d_tot = DeviceArray(32)
         out = abi.MeshOut(d_verts.ptr, d_norm.ptr if d_norm else None, d_inds.ptr, d_cases.ptr if d_cases else None,
-                          d_samp.ptr if d_samp else None, d_rec.ptr, d_tot.ptr, vert_capacity, ind_capacity)
+                          d_samp.ptr if d_samp else None, d_rec.ptr, d_tot.ptr, vert_capacity, ind_capacity,
+                          ncells if d_cases else 0, nsamp if d_samp else 0)
         max_cells = int(descs["cells"].max()) if n else 1
         if samples_in is not None:
-            d_in = self.upload(np.ascontiguousarray(samples_in, dtype=np.float32))
+            sin = np.ascontiguousarray(samples_in, dtype=np.float32)
+            d_in = self.upload(sin)
             check(lib().uww_build_chunks_from_samples(self.h, C.c_void_p(d_desc.ptr), n, max_cells,
-                                                      C.c_void_p(d_in.ptr), C.byref(out)),
+                                                      C.c_void_p(d_in.ptr), sin.size, C.byref(out)),
                   "uww_build_chunks_from_samples")
         else:
             check(lib().uww_build_chunks(self.h, C.c_void_p(d_desc.ptr), n, max_cells, C.byref(out)),

@@ -79,6 +79,35 @@ def edge_share(edges):
     return table
 
 
+def owned_masks(edges):
+    """[oriented dedup?][boundary flags] -> mask of the edges a cell creates vertices for.
+
+    Flag bits: 1 x==0, 2 y==0, 4 z==0, 8 x==N-1, 16 y==N-1, 32 z==N-1.  A cell
+    owns edge e when no earlier cell (in stream order) inside the chunk holds
+    the same edge (with the same orientation, for oriented dedup)."""
+    share = edge_share(edges)
+    out = []
+    for oriented in (0, 1):
+        row = []
+        for f in range(64):
+            lo = [bool(f & 1), bool(f & 2), bool(f & 4)]
+            hi = [bool(f & 8), bool(f & 16), bool(f & 32)]
+            m = 0
+            for e in range(12):
+                for dx, dy, dz, e2, same in share[e]:
+                    if oriented and not same:
+                        continue
+                    d = (dx, dy, dz)
+                    if any((d[i] < 0 and lo[i]) or (d[i] > 0 and hi[i]) for i in range(3)):
+                        continue
+                    if d == (0, 0, 0) and e2 == e:
+                        m |= 1 << e
+                    break
+            row.append(m)
+        out.append(row)
+    return out  # index 0: one vertex per edge, 1: oriented (reference) dedup
+
+
 def emit(edges, rows, ntri, emask) -> str:
     out = [
         "// Generated by gen_mc_tables.py from underwater_world/src/marching_table.rs:1-273",
@@ -97,7 +126,7 @@ def emit(edges, rows, ntri, emask) -> str:
     out.append(",\n".join(f"    {{{a}, {b}}}" for a, b in edges))
     out += ["};", "",
             "// Bourke triangulation, -1 terminated; marching_table.rs:16-273.",
-            "UWW_TABLE_QUAL static const int8_t UWW_TRI_TABLE[256][16] = {"]
+            "UWW_TABLE_QUAL static const int8_t UWW_TRI_TABLE[256][16] __attribute__((aligned(16))) = {"]
     out.append(",\n".join("    {" + ", ".join(f"{v:2d}" for v in r) + "}" for r in rows))
     out += ["};", "", "// Triangles per case (derived).",
             "UWW_TABLE_QUAL static const uint8_t UWW_CASE_NTRI[256] = {"]
@@ -116,6 +145,12 @@ def emit(edges, rows, ntri, emask) -> str:
     for e, cands in enumerate(edge_share(edges)):
         rows_out.append("    {" + ", ".join("{%d, %d, %d, %d, %d}" % c for c in cands) + "}")
     out.append(",\n".join(rows_out))
+    out += ["};", "",
+            "// Owned-edge mask of a cell by its boundary flags (bit 1 x==0, 2 y==0, 4 z==0, 8 x==N-1,",
+            "// 16 y==N-1, 32 z==N-1): [0] one vertex per edge, [1] oriented (reference) dedup; derived from UWW_EDGE_SHARE.",
+            "UWW_TABLE_QUAL static const uint16_t UWW_OWNED_MASK[2][64] = {"]
+    om = owned_masks(edges)
+    out.append(",\n".join("    {" + ", ".join(f"0x{v:03x}" for v in r) + "}" for r in om))
     out += ["};", ""]
     return "\n".join(out)
 

@@ -4,6 +4,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <new>
@@ -21,6 +22,7 @@ struct uww_ctx {
     int device = 0;
     int num_sms = 0;
     size_t smem_optin = 0;
+    size_t smem_dyn_max = 0;
 
     // tuning (0 = automatic)
     int threads = 0;
@@ -30,7 +32,9 @@ struct uww_ctx {
     // device work state
     unsigned long long* d_lookback = nullptr;
     size_t lookback_cap = 0;
+    unsigned long long* d_state = nullptr;
     unsigned int* d_counter = nullptr;
+    unsigned long long* d_acc = nullptr;
     unsigned long long* d_totals = nullptr;
     uint8_t* d_scratch = nullptr;
     size_t scratch_cap = 0;
@@ -51,7 +55,19 @@ namespace {
 
 constexpr long long kSpinLimitCycles = 4000000000ll;  // ~2 s at 2 GHz
 
-int cuda_status(cudaError_t e) { return e == cudaSuccess ? UWW_OK : (e == cudaErrorMemoryAllocation ? UWW_ERR_OOM : UWW_ERR_CUDA); }
+thread_local char g_last_error[256] = "";
+
+void note_error(const char* where, cudaError_t e)
+{
+    std::snprintf(g_last_error, sizeof(g_last_error), "%s: %s (%d)", where, cudaGetErrorString(e), (int)e);
+}
+
+int cuda_status(cudaError_t e, const char* where = "CUDA call")
+{
+    if (e == cudaSuccess) return UWW_OK;
+    note_error(where, e);
+    return e == cudaErrorMemoryAllocation ? UWW_ERR_OOM : UWW_ERR_CUDA;
+}
 
 // --- noise::Perlin::new(seed) permutation --------------------------------------
 // The crate seeds an XorShift128 generator with the bytes
@@ -153,6 +169,9 @@ int ensure_device(T** ptr, size_t* cap, size_t bytes)
 struct LaunchCfg {
     int threads;
     uint32_t smem_cells;
+    uint32_t slots;        // workspaces per CTA
+    size_t smem_buf;       // bytes of one shared-memory workspace
+    size_t ztable_offset;  // fast build z tables, after the workspaces
     size_t dyn_smem;
     int grid;
     size_t scratch_slot;
@@ -160,14 +179,25 @@ struct LaunchCfg {
 
 int plan_launch(uww_ctx* ctx, uint32_t n, uint32_t max_cells, bool queue, LaunchCfg* cfg)
 {
-    const size_t static_smem = build_static_smem_bytes();
-    const size_t cap = ctx->smem_optin > static_smem + 1024 ? ctx->smem_optin - static_smem - 1024 : 0;
+    // The batched form pipelines two chunks per CTA, so it holds two workspaces.
+    const uint32_t slots = queue ? 2u : 1u;
+    const size_t cap = ctx->smem_dyn_max;
     uint32_t smem_cells = ctx->smem_cells > 0 ? (uint32_t)ctx->smem_cells : max_cells;
     smem_cells = std::min(smem_cells, max_cells);
-    while (smem_cells > 0 && chunk_layout((int)smem_cells).total > cap) --smem_cells;
+    // the fast build also keeps per-chunk z tables (sized for the largest chunk)
+    const size_t zt = ctx->dev.math_mode == UWW_MATH_FAST ? ztable_bytes((int)max_cells + 1, ctx->dev.octaves) : 0;
+    while (smem_cells > 0 && (size_t)slots * chunk_layout((int)smem_cells).total + zt > cap) --smem_cells;
     cfg->smem_cells = smem_cells;
-    cfg->dyn_smem = smem_cells > 0 ? chunk_layout((int)smem_cells).total : 0;
-    cfg->threads = ctx->threads > 0 ? ctx->threads : (max_cells > 16 ? 512 : 256);
+    cfg->slots = slots;
+    cfg->smem_buf = smem_cells > 0 ? chunk_layout((int)smem_cells).total : 0;
+    cfg->ztable_offset = (size_t)slots * cfg->smem_buf;
+    cfg->dyn_smem = cfg->ztable_offset + zt;
+    // compute threads: by default about one per (x, y) sample column of the
+    // largest chunk, rounded so the last round of columns fills its warps;
+    // the batched form adds one control warp
+    const int compute = ctx->threads > 0 ? ctx->threads
+                      : max_cells <= 12 ? 192 : max_cells <= 24 ? 320 : 512;
+    cfg->threads = compute + (queue ? 32 : 0);
     cfg->scratch_slot = max_cells > smem_cells ? chunk_layout((int)max_cells).total : 0;
     if (!queue) {
         cfg->grid = 1;
@@ -185,13 +215,13 @@ int plan_launch(uww_ctx* ctx, uint32_t n, uint32_t max_cells, bool queue, Launch
 }
 
 int launch(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint32_t max_cells, const uww_mesh_out* out,
-           bool queue, const float* samples_in = nullptr)
+           bool queue, const float* samples_in = nullptr, unsigned long long samples_in_count = 0)
 {
     LaunchCfg cfg;
     int st = plan_launch(ctx, n, max_cells, queue, &cfg);
     if (st) return st;
     if (cfg.scratch_slot) {
-        st = ensure_device(&ctx->d_scratch, &ctx->scratch_cap, cfg.scratch_slot * (size_t)cfg.grid);
+        st = ensure_device(&ctx->d_scratch, &ctx->scratch_cap, cfg.scratch_slot * cfg.slots * (size_t)cfg.grid);
         if (st) return st;
     }
     BuildArgs a;
@@ -205,28 +235,36 @@ int launch(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint32_t ma
     a.cases = out->cases;
     a.samples_out = (ctx->params.outputs & UWW_OUT_SAMPLES) ? out->samples : nullptr;
     a.samples_in = samples_in;
+    a.samples_in_count = samples_in_count;
+    a.case_capacity = out->case_capacity;
+    a.sample_capacity = out->sample_capacity;
     a.records = out->records;
     a.totals = out->totals ? reinterpret_cast<unsigned long long*>(out->totals) : ctx->d_totals;
     a.vert_capacity = out->vert_capacity;
     a.ind_capacity = out->ind_capacity;
     a.scratch = ctx->d_scratch;
     a.scratch_slot_bytes = cfg.scratch_slot;
+    a.slots_per_cta = cfg.slots;
+    a.smem_buf_bytes = cfg.smem_buf;
+    a.ztable_offset = cfg.ztable_offset;
     a.smem_cells = cfg.smem_cells;
     a.spin_limit_cycles = kSpinLimitCycles;
     if (queue) {
-        st = ensure_device(&ctx->d_lookback, &ctx->lookback_cap, (size_t)n * sizeof(unsigned long long));
-        if (st) return st;
+        // The look-back words, ticket counter and accumulators are zero when a
+        // launch starts: zeroed once here on (re)allocation, and reset by the
+        // last CTA of every launch.  So a batched build is one kernel launch.
+        if (!ctx->d_lookback || ctx->lookback_cap < (size_t)n * sizeof(unsigned long long)) {
+            st = ensure_device(&ctx->d_lookback, &ctx->lookback_cap,
+                               std::max<size_t>((size_t)n, 4096) * sizeof(unsigned long long));
+            if (st) return st;
+            cudaError_t e = cudaMemsetAsync(ctx->d_lookback, 0, ctx->lookback_cap, ctx->stream);
+            if (e != cudaSuccess) return cuda_status(e, "cudaMemsetAsync");
+        }
         a.lookback = ctx->d_lookback;
         a.work_counter = ctx->d_counter;
-        cudaError_t e;
-        if ((e = cudaMemsetAsync(ctx->d_lookback, 0, (size_t)n * sizeof(unsigned long long), ctx->stream)) != cudaSuccess)
-            return cuda_status(e);
-        if ((e = cudaMemsetAsync(ctx->d_counter, 0, sizeof(unsigned int), ctx->stream)) != cudaSuccess)
-            return cuda_status(e);
-        if ((e = cudaMemsetAsync(a.totals, 0, 4 * sizeof(unsigned long long), ctx->stream)) != cudaSuccess)
-            return cuda_status(e);
+        a.acc = ctx->d_acc;
     }
-    return cuda_status(launch_build(ctx->dev, a, queue, cfg.grid, cfg.threads, cfg.dyn_smem, ctx->stream));
+    return cuda_status(launch_build(ctx->dev, a, queue, cfg.grid, cfg.threads, cfg.dyn_smem, ctx->stream), "build kernel launch");
 }
 
 int check_out(const uww_mesh_out* out)
@@ -242,6 +280,8 @@ int check_out(const uww_mesh_out* out)
 extern "C" {
 
 int uww_abi_version(void) { return UWW_ABI_VERSION; }
+
+const char* uww_last_error(void) { return g_last_error; }
 
 const char* uww_status_string(int s)
 {
@@ -315,25 +355,36 @@ int uww_ctx_create(const uww_params* p, void* stream, uww_ctx** out)
     if (!ctx) return UWW_ERR_OOM;
     ctx->params = *p;
     make_dev_params(p, &ctx->dev);
+    const char* where = "cudaGetDevice";
     cudaError_t e = cudaGetDevice(&ctx->device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, ctx->device);
     int optin = 0;
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
     ctx->smem_optin = (size_t)optin;
     if (e == cudaSuccess) {
+        where = "cudaFuncSetAttribute(MaxDynamicSharedMemorySize)";
         const size_t static_smem = build_static_smem_bytes();
-        e = prepare_build_kernels(ctx->smem_optin > static_smem ? ctx->smem_optin - static_smem : 0);
+        e = prepare_build_kernels(ctx->smem_optin, &ctx->smem_dyn_max);
     }
     if (e == cudaSuccess) {
+        where = "cudaStreamCreate";
         if (stream) ctx->stream = (cudaStream_t)stream;
         else { e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking); ctx->own_stream = true; }
     }
-    if (e == cudaSuccess) e = cudaMalloc((void**)&ctx->d_counter, sizeof(unsigned int));
+    if (e == cudaSuccess) {
+        where = "cudaMalloc";
+        // [0] ticket counter (u32), [1..3] overflow count, error flags, exit count
+        e = cudaMalloc((void**)&ctx->d_state, 4 * sizeof(unsigned long long));
+        if (e == cudaSuccess) e = cudaMemset(ctx->d_state, 0, 4 * sizeof(unsigned long long));
+        ctx->d_counter = reinterpret_cast<unsigned int*>(ctx->d_state);
+        ctx->d_acc = ctx->d_state + 1;
+    }
     if (e == cudaSuccess) e = cudaMalloc((void**)&ctx->d_totals, 4 * sizeof(unsigned long long));
-    if (e == cudaSuccess) e = cudaMallocHost((void**)&ctx->h_totals, 4 * sizeof(unsigned long long));
+    if (e == cudaSuccess) { where = "cudaMallocHost"; e = cudaMallocHost((void**)&ctx->h_totals, 4 * sizeof(unsigned long long)); }
     if (e != cudaSuccess) {
+        const int st2 = cuda_status(e, where);
         uww_ctx_destroy(ctx);
-        return cuda_status(e);
+        return st2;
     }
     *out = ctx;
     return UWW_OK;
@@ -344,7 +395,7 @@ int uww_ctx_destroy(uww_ctx* ctx)
     if (!ctx) return UWW_ERR_INVALID_ARG;
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     cudaFree(ctx->d_lookback);
-    cudaFree(ctx->d_counter);
+    cudaFree(ctx->d_state);
     cudaFree(ctx->d_totals);
     cudaFree(ctx->d_scratch);
     cudaFree(ctx->d_chunks);
@@ -401,7 +452,7 @@ int uww_build_chunks(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, u
 }
 
 int uww_build_chunks_from_samples(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint32_t max_cells,
-                                  const float* d_samples, const uww_mesh_out* out)
+                                  const float* d_samples, uint64_t sample_count, const uww_mesh_out* out)
 {
     if (!ctx) return UWW_ERR_INVALID_ARG;
     int st = check_out(out);
@@ -412,7 +463,7 @@ int uww_build_chunks_from_samples(uww_ctx* ctx, const uww_chunk_desc* d_chunks, 
         return UWW_OK;
     }
     if (!d_chunks || !d_samples) return UWW_ERR_INVALID_ARG;
-    return launch(ctx, d_chunks, n, max_cells, out, true, d_samples);
+    return launch(ctx, d_chunks, n, max_cells, out, true, d_samples, sample_count);
 }
 
 int uww_build_chunk_plain(uww_ctx* ctx, const uww_chunk_desc* d_chunk, uint32_t cells, const uww_mesh_out* out)
@@ -465,6 +516,8 @@ int uww_build_chunks_host(uww_ctx* ctx, const uww_chunk_desc* h_chunks, uint32_t
     d_out.inds = (uint32_t*)ctx->d_inds;
     d_out.cases = want_cases ? (uint8_t*)ctx->d_cases : nullptr;
     d_out.samples = want_samples ? (float*)ctx->d_samples : nullptr;
+    d_out.case_capacity = want_cases ? case_bytes : 0;
+    d_out.sample_capacity = want_samples ? sample_count : 0;
     d_out.records = (uww_chunk_record*)ctx->d_records;
     d_out.totals = reinterpret_cast<uint64_t*>(ctx->d_totals);
     d_out.vert_capacity = h_out->vert_capacity;
@@ -491,7 +544,7 @@ int uww_build_chunks_host(uww_ctx* ctx, const uww_chunk_desc* h_chunks, uint32_t
     if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_status(e);
     if (h_out->totals) std::memcpy(h_out->totals, ctx->h_totals, 4 * sizeof(uint64_t));
     if (ctx->h_totals[3] & kErrTimeout) return UWW_ERR_TIMEOUT;
-    if (ctx->h_totals[3] & kErrBadChunk) return UWW_ERR_INVALID_ARG;
+    if (ctx->h_totals[3] & (kErrBadChunk | kErrRange)) return UWW_ERR_INVALID_ARG;
     if (ctx->h_totals[2]) return UWW_ERR_CAPACITY;
     return UWW_OK;
 }
@@ -500,6 +553,7 @@ int uww_ctx_set_tuning(uww_ctx* ctx, const uww_tuning* t)
 {
     if (!ctx || !t) return UWW_ERR_INVALID_ARG;
     if (t->threads < 0 || t->threads > 512 || (t->threads % 32) != 0) return UWW_ERR_INVALID_ARG;
+    if (t->threads > 192 && t->threads < 224) return UWW_ERR_INVALID_ARG;  // between the two kernel shapes
     if (t->blocks_per_sm < 0 || t->blocks_per_sm > 32) return UWW_ERR_INVALID_ARG;
     if (t->smem_cells < 0 || t->smem_cells > UWW_MAX_CELLS) return UWW_ERR_INVALID_ARG;
     ctx->threads = t->threads;
@@ -555,6 +609,13 @@ int uww_memset(uww_ctx* ctx, void* dst, int value, size_t bytes)
     if (!ctx || (bytes && !dst)) return UWW_ERR_INVALID_ARG;
     if (!bytes) return UWW_OK;
     return cuda_status(cudaMemsetAsync(dst, value, bytes, ctx->stream));
+}
+
+int uww_probe_fma(uww_ctx* ctx, uint32_t blocks, uint32_t iters, float* d_sink, double* flops)
+{
+    if (!ctx || !d_sink || blocks == 0 || iters == 0) return UWW_ERR_INVALID_ARG;
+    if (flops) *flops = 2.0 * 8.0 * 16.0 * (double)iters * 256.0 * (double)blocks;
+    return cuda_status(launch_fma_probe((int)blocks, iters, d_sink, ctx->stream));
 }
 
 int uww_density_at(uww_ctx* ctx, const float* d_xyz, uint32_t n, float* d_out)

@@ -1,16 +1,21 @@
 // uww_build.cu -- the chunk-build kernel (noise + marching cubes + emission).
 //
-// One CTA builds one chunk at a time:
-//   1. samples the (N+1)^3 density grid (Chunk::build_iso, chunk.rs:105-129)
-//      into shared memory, and votes the early blank check (chunk.rs:131-133);
-//   2. classifies every cell to its 8-bit case (chunk.rs:144-162), counts its
-//      triangles and the vertices it creates, and block-scans those counts in
-//      the reference's cell order (x outer, y, z inner; chunk.rs:138-142);
-//   3. (batched form) takes the chunk's output offsets from a decoupled
-//      look-back over the work-queue order, so the batch is laid out compact
-//      and in chunk order in one pass;
-//   4. walks the active cells' triangle rows (chunk.rs:164-251) and writes
-//      chunk-local u32 indices and, once per vertex, VertColor + normal.
+// One CTA builds one chunk at a time.  Per chunk:
+//   front half (compute warps):
+//     1. the (N+1)^3 density grid (Chunk::build_iso, chunk.rs:105-129) into
+//        shared memory, and the early blank vote (chunk.rs:131-133);
+//     2. each cell's 8-bit case (chunk.rs:144-162), its triangle count and the
+//        number of vertices it creates, block-scanned in the reference's cell
+//        order (x outer, y, z inner; chunk.rs:138-142);
+//     3. publication of the chunk's counts for the device-wide prefix sum (a
+//        decoupled look-back over the work-queue order);
+//   back half:
+//     4. the chunk's output offsets (control warp, from the look-back) and its
+//        record;
+//     5. emission (compute warps): pass 1, one thread per active cell, walks
+//        the triangle rows (chunk.rs:164-251) and writes chunk-local u32
+//        indices and vertex positions; pass 2, one thread per vertex, writes
+//        the colour (chunk.rs:208-219) and the normal.
 //
 // Vertex dedup (chunk.rs:233) is resolved without a search: a crossed edge is
 // referenced by every cell that holds it, so the vertex the reference creates
@@ -18,10 +23,18 @@
 // owner's first reference to that edge.  Vertex ids are the running count of
 // owned first references, scanned over cells.
 //
-// The batched form runs as a persistent grid fed by an atomic ticket
-// counter; the plain form (one chunk per launch) is the same code without the
-// queue and look-back.
+// Batched form: a persistent grid fed by a device work queue (an atomic ticket
+// counter).  Each CTA is warp-specialised -- compute warps plus one control
+// warp -- and pipelines two chunks: once the compute warps finish the noise of
+// ticket i, the control warp resolves the look-back of ticket i-1 (while
+// ticket i is classified) and writes its record; once ticket i-1 is emitted
+// it takes ticket i+1 from the queue.  Look-back and record latency thus
+// overlap compute.  The plain form (one chunk per launch) runs
+// front then back with compute warps only.
 #include <cuda_runtime.h>
+
+#include <algorithm>
+#include <type_traits>
 
 #define UWW_TABLE_QUAL __constant__
 #include "mc_tables.h"
@@ -31,7 +44,69 @@ namespace uww {
 
 namespace {
 
+// Packed per-cell counts for the block scan: verts [21:0], inds [43:22], active [62:44].
+constexpr int kIndShift = 22;
+constexpr int kActShift = 44;
+constexpr unsigned long long kField22 = (1ull << 22) - 1;
+
+// Named barriers: 0 = whole CTA, 1 = compute warps, 2 = ticket hand-off,
+// 3 = offsets hand-off, 4 = noise done, 5 = emission done (2-5: compute
+// warps + control warp).
+constexpr int kBarCompute = 1;
+constexpr int kBarTicket = 2;
+constexpr int kBarOffsets = 3;
+constexpr int kBarNoiseDone = 4;  // compute warps arrive (no wait) once a chunk's noise is done
+constexpr int kBarEmitDone = 5;   // compute warps arrive (no wait) once the previous chunk is emitted
+
+__device__ __forceinline__ void bar_arrive(int id, int count)
+{
+    asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void bar_sync(int id, int count)
+{
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ int bar_or(int id, int count, int pred)
+{
+    int r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.s32 p, %1, 0;\n\t"
+        "bar.red.or.pred q, %2, %3, p;\n\t"
+        "selp.s32 %0, 1, 0, q;\n\t}"
+        : "=r"(r)
+        : "r"(pred), "r"(id), "r"(count)
+        : "memory");
+    return r;
+}
+
+// Per in-flight chunk, kept in shared memory between the front and back halves.
+struct ChunkInfo {
+    uint32_t ticket;
+    int32_t ox, oy, oz;
+    int32_t N;
+    uint32_t flags;               // UWW_CHUNK_EARLY_BLANK decided by the front half
+    uint32_t classified;          // the mesh stage ran (not bad, not early blank)
+    uint32_t pad;
+    unsigned long long total;     // packed counts
+};
+
+struct Ticket {
+    uww_chunk_desc desc;
+    uint32_t ticket;
+    uint32_t pad[3];
+};
+
+struct Offsets {
+    unsigned long long excl;      // verts | inds << 32
+    uint32_t fits;
+    uint32_t pad;
+};
+
 struct SmemTables {
+    float4 gp[256];               // gradient vector of P[i] (fast build: the last hash lookup)
     int8_t tri[256][16];
     uint16_t edges[256];
     uint8_t ntri[256];
@@ -41,10 +116,12 @@ struct SmemTables {
     uint16_t owned[2][64];        // [oriented?][boundary flags] -> owned edge mask
     unsigned long long warp_sums[32];
     unsigned long long chunk_total;
-    unsigned long long excl;       // packed exclusive prefix (verts | inds << 32)
-    uint32_t ticket;
-    uint32_t fits;
-    uint32_t any_inside;
+    ChunkInfo ci[2];              // the chunks in flight (front / back)
+    Ticket tk[2];                 // tickets handed from the control warp
+    Offsets off[2];               // offsets handed from the control warp
+    uint32_t overflow;            // chunks of this CTA that did not fit (control warp)
+    uint32_t errflags;            // UWW_ERRFLAG_* raised by this CTA
+    uint32_t last;                // this CTA is the last of the launch to finish
 };
 
 __device__ __forceinline__ int boundary_flags(int x, int y, int z, int N)
@@ -85,27 +162,168 @@ __device__ __forceinline__ int rank_in_row(const int8_t* row, unsigned owned, in
     return r;
 }
 
-__device__ __forceinline__ unsigned long long ld_acquire(const unsigned long long* p)
+// ---------------------------------------------------------------------------
+// Fast-build density grid, one compute thread per (x, y) column of samples.
+//
+// Along a column only z varies, and the z lattice cell, fraction and fade of
+// every octave depend on z alone: they are tabulated once per chunk in shared
+// memory, together with each octave's runs of consecutive samples that share
+// a z lattice cell.  Per column and octave the x/y lattice coordinates,
+// fades, partial hashes and bilinear weights are computed once; per run the 8
+// corner gradients are fetched (from gp, the gradient of P[i]) and reduced to
+// the run's polynomial in dz:
+//   A = g.xy . (d - o).xy and G = g.z per corner,
+//   n(dz) = al + be dz + fade(dz) (ga + de dz),
+//   al = sum_xy w A_xy0,  be = sum_xy w G_xy0,
+//   ga = sum_xy w (A_xy1 - G_xy1 - A_xy0),  de = sum_xy w (G_xy1 - G_xy0),
+// so a sample costs three FMAs plus its accumulate.  Same Perlin/fBm maths as
+// the parity build (trilinear interpolation == the k-polynomial) in a
+// different operation order with FMA contraction.  The depth bias seeds the
+// first octave; the early blank vote reads the last.  Returns whether any of
+// this thread's samples is at or below the iso-level.  Every compute thread
+// must call it.
+struct ZTable {
+    float2* dzc;   // [octave][z]: (dz, fade(dz))
+    int2* runs;    // [octave][run]: (first z, z lattice cell)
+    int* nruns;    // [octave]
+    float* bias;   // [z]
+};
+
+__device__ __forceinline__ ZTable ztable_at(uint8_t* base, int S, int octaves)
+{
+    ZTable t;
+    t.dzc = reinterpret_cast<float2*>(base);
+    t.runs = reinterpret_cast<int2*>(base + (size_t)octaves * S * sizeof(float2));
+    t.nruns = reinterpret_cast<int*>(base + (size_t)octaves * S * (sizeof(float2) + sizeof(int2)));
+    t.bias = reinterpret_cast<float*>(base + (size_t)octaves * S * (sizeof(float2) + sizeof(int2)) +
+                                      (size_t)octaves * sizeof(int));
+    return t;
+}
+
+__device__ __forceinline__ int sample_columns_fast(const DevParams& p, const uint8_t* __restrict__ P,
+                                                   const float4* __restrict__ gp, const ZTable Z,
+                                                   float* __restrict__ rho, int N, int ox, int oy, int oz,
+                                                   int ncomp)
+{
+    const int S = N + 1, SS = S * S, K = p.octaves;
+    const float s = __fdiv_rn((float)p.chunk_size, (float)N);
+    const float bf = p.base_freq;
+    float norm = kPerlinScale;
+    if (p.normalize) {
+        float mx = 0.f;
+        for (int k = 0; k < K; ++k) mx += p.amp[k];
+        norm = __fdiv_rn(kPerlinScale, mx);
+    }
+    const float zoff = (float)oz + p.offset[2];
+    const float iso = p.iso_level;
+
+    // ---- per-chunk z tables, shared by every column ----
+    for (int i = threadIdx.x; i < K * S; i += ncomp) {
+        const int k = i / S, z = i - k * S;
+        const float qz = fmaf((float)z, s, zoff) * (bf * p.mult[k]);
+        const float fz = floorf(qz);
+        const float dz = qz - fz;
+        Z.dzc[i] = make_float2(dz, fade<FastOps>(dz));
+        reinterpret_cast<int*>(Z.runs)[2 * i + 1] = (int)fz;  // staged: cell of sample z
+        if (k == 0) {
+            const float wz = fmaf((float)z, s, (float)oz);
+            float b = 0.f;
+            if (p.bias_mode == UWW_BIAS_TERRACED) {
+                const float adj = __fdiv_rn((wz + p.offset[2]) * bf * p.bias_a, p.bias_b);
+                b = adj - fmodf(adj, p.bias_c);
+            } else if (p.bias_mode == UWW_BIAS_LINEAR) {
+                b = p.bias_a * (wz - p.bias_b);
+            }
+            Z.bias[z] = b;
+        }
+    }
+    bar_sync(kBarCompute, ncomp);
+    // compact each octave's cells into runs (one thread per octave)
+    for (int k = threadIdx.x; k < K; k += ncomp) {
+        int2* r = Z.runs + k * S;
+        int n = 0, prev = 0;
+        for (int z = 0; z < S; ++z) {
+            const int iz = r[z].y;  // staged value; r[n] with n <= z is already consumed
+            if (z == 0 || iz != prev) r[n++] = make_int2(z, iz);
+            prev = iz;
+        }
+        Z.nruns[k] = n;
+    }
+    bar_sync(kBarCompute, ncomp);
+
+    int inside = 0;
+    for (int col = threadIdx.x; col < SS; col += ncomp) {
+        const int x = col / S, y = col - x * S;
+        float* out = rho + col * S;
+        const float nx = (fmaf((float)x, s, (float)ox) + p.offset[0]) * bf;
+        const float ny = (fmaf((float)y, s, (float)oy) + p.offset[1]) * bf;
+        for (int k = 0; k < K; ++k) {
+            const float m = p.mult[k], amp = p.amp[k] * norm;
+            const float qx = nx * m, qy = ny * m;
+            const float fx = floorf(qx), fy = floorf(qy);
+            const int ix = (int)fx, iy = (int)fy;
+            const float dx = qx - fx, dy = qy - fy, dx1 = dx - 1.f, dy1 = dy - 1.f;
+            const float a = fade<FastOps>(dx), b = fade<FastOps>(dy);
+            const float w00 = amp * (1.f - a) * (1.f - b), w10 = amp * a * (1.f - b);
+            const float w01 = amp * (1.f - a) * b, w11 = amp * a * b;
+            const int hx0 = P[ix & 255], hx1 = P[(ix + 1) & 255];
+            const int h00 = P[hx0 ^ (iy & 255)], h01 = P[hx0 ^ ((iy + 1) & 255)];
+            const int h10 = P[hx1 ^ (iy & 255)], h11 = P[hx1 ^ ((iy + 1) & 255)];
+            const float2* dzc = Z.dzc + k * S;
+            const int2* runs = Z.runs + k * S;
+            const int nr = Z.nruns[k];
+            const bool first = k == 0, last = k == K - 1;
+            for (int r = 0; r < nr; ++r) {
+                const int2 run = runs[r];
+                const int zb = run.x, ze = r + 1 < nr ? runs[r + 1].x : S;
+                const int z0 = run.y & 255, z1 = (run.y + 1) & 255;
+                float4 g;
+                g = gp[h00 ^ z0]; const float A0 = fmaf(g.x, dx, g.y * dy), G0 = g.z;
+                g = gp[h00 ^ z1]; const float A1 = fmaf(g.x, dx, g.y * dy), G1 = g.z;
+                g = gp[h01 ^ z0]; const float A2 = fmaf(g.x, dx, g.y * dy1), G2 = g.z;
+                g = gp[h01 ^ z1]; const float A3 = fmaf(g.x, dx, g.y * dy1), G3 = g.z;
+                g = gp[h10 ^ z0]; const float A4 = fmaf(g.x, dx1, g.y * dy), G4 = g.z;
+                g = gp[h10 ^ z1]; const float A5 = fmaf(g.x, dx1, g.y * dy), G5 = g.z;
+                g = gp[h11 ^ z0]; const float A6 = fmaf(g.x, dx1, g.y * dy1), G6 = g.z;
+                g = gp[h11 ^ z1]; const float A7 = fmaf(g.x, dx1, g.y * dy1), G7 = g.z;
+                const float al = fmaf(w00, A0, fmaf(w01, A2, fmaf(w10, A4, w11 * A6)));
+                const float be = fmaf(w00, G0, fmaf(w01, G2, fmaf(w10, G4, w11 * G6)));
+                const float ga = fmaf(w00, A1 - G1 - A0, fmaf(w01, A3 - G3 - A2, fmaf(w10, A5 - G5 - A4, w11 * (A7 - G7 - A6))));
+                const float de = fmaf(w00, G1 - G0, fmaf(w01, G3 - G2, fmaf(w10, G5 - G4, w11 * (G7 - G6))));
+#pragma unroll 2
+                for (int z = zb; z < ze; ++z) {
+                    const float2 t = dzc[z];
+                    const float v = fmaf(t.y, fmaf(de, t.x, ga), fmaf(be, t.x, al));
+                    const float r0 = v + (first ? Z.bias[z] : out[z]);
+                    out[z] = r0;
+                    if (last) inside |= !(r0 > iso);
+                }
+            }
+        }
+    }
+    return inside;
+}
+
+// ---------------------------------------------------------------------------
+// The look-back words carry their own payload (no other data is published
+// through them), so relaxed gpu-scope loads and stores suffice.
+__device__ __forceinline__ unsigned long long ld_relaxed(const unsigned long long* p)
 {
     unsigned long long v;
-    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
     return v;
 }
 
-__device__ __forceinline__ void st_release(unsigned long long* p, unsigned long long v)
+__device__ __forceinline__ void st_relaxed(unsigned long long* p, unsigned long long v)
 {
-    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
-// Packed per-cell counts for the block scan: verts [21:0], inds [43:22], active [62:44].
-constexpr int kIndShift = 22;
-constexpr int kActShift = 44;
-constexpr unsigned long long kField22 = (1ull << 22) - 1;
-
+// Exclusive scan over the compute threads (ncomp, a multiple of 32).
 __device__ __forceinline__ unsigned long long block_exclusive_scan(unsigned long long v, SmemTables& T,
-                                                                   unsigned long long& total)
+                                                                   unsigned long long& total, int ncomp)
 {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = ncomp >> 5;
     unsigned long long incl = v;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -113,7 +331,7 @@ __device__ __forceinline__ unsigned long long block_exclusive_scan(unsigned long
         if (lane >= o) incl += t;
     }
     if (lane == 31) T.warp_sums[warp] = incl;
-    __syncthreads();
+    bar_sync(kBarCompute, ncomp);
     if (warp == 0) {
         unsigned long long w = lane < nwarps ? T.warp_sums[lane] : 0ull;
         unsigned long long wi = w;
@@ -125,7 +343,7 @@ __device__ __forceinline__ unsigned long long block_exclusive_scan(unsigned long
         if (lane < nwarps) T.warp_sums[lane] = wi - w;  // exclusive warp offsets
         if (lane == nwarps - 1) T.chunk_total = wi;
     }
-    __syncthreads();
+    bar_sync(kBarCompute, ncomp);
     total = T.chunk_total;
     return T.warp_sums[warp] + incl - v;
 }
@@ -139,316 +357,522 @@ __device__ __forceinline__ unsigned long long sat_add_packed(unsigned long long 
     return v | (i << 30);
 }
 
-// Decoupled look-back by warp 0: publishes this ticket's aggregate, sums the
-// predecessors' values back to the nearest inclusive prefix, publishes the
-// inclusive prefix.  Returns the packed exclusive prefix.  Every wait is
-// bounded by spin_limit_cycles; on timeout the prefix saturates (so nothing is
-// written out of place) and the error flag is raised.
-__device__ unsigned long long lookback(const BuildArgs& a, uint32_t ticket, unsigned long long own)
+__device__ __forceinline__ unsigned long long pack_counts(unsigned long long total)
+{
+    return (total & kField22) | (((total >> kIndShift) & kField22) << 30);
+}
+
+// Publish a chunk's aggregate as soon as its counts are known (ticket 0
+// publishes its inclusive prefix right away).
+__device__ __forceinline__ void lookback_publish(const BuildArgs& a, uint32_t ticket, unsigned long long own)
+{
+    st_relaxed(&a.lookback[ticket], (ticket == 0 ? kLbInclusive : kLbAggregate) | own);
+}
+
+// Resolve a ticket's exclusive prefix, by one warp: sum the predecessors'
+// words back to the nearest inclusive prefix (4 words per lane per round
+// trip), then publish this ticket's inclusive prefix.  A predecessor that has
+// not published yet, closer than the nearest inclusive prefix, means wait and
+// re-read.  The wait is bounded by spin_limit_cycles; on timeout the prefix
+// saturates (so nothing is written out of place) and the error flag is raised.
+__device__ unsigned long long lookback_warp(const BuildArgs& a, uint32_t ticket, unsigned long long own,
+                                           uint32_t* errflags)
 {
     const int lane = threadIdx.x & 31;
-    if (ticket == 0) {
-        if (lane == 0) st_release(&a.lookback[0], kLbInclusive | own);
-        return 0ull;
-    }
-    if (lane == 0) st_release(&a.lookback[ticket], kLbAggregate | own);
     unsigned long long sum = 0ull;
-    long long j = (long long)ticket - 1;
-    const long long t0 = clock64();
-    bool timed_out = false;
-    for (;;) {
-        const long long idx = j - lane;
-        const unsigned long long s = idx >= 0 ? ld_acquire(&a.lookback[idx]) : kLbInclusive;
-        const unsigned status = (unsigned)(s >> 62);
-        if (__any_sync(0xffffffffu, status == 0)) {
-            if (clock64() - t0 > a.spin_limit_cycles) { timed_out = true; break; }
-            __nanosleep(64);
-            continue;
-        }
-        const unsigned incl = __ballot_sync(0xffffffffu, status == 2);
-        const int first = incl ? __ffs(incl) - 1 : 31;
-        unsigned long long mine = lane <= first ? (s & ~(3ull << 62)) : 0ull;
-        unsigned long long v = mine & kLbVertMax, i = (mine >> 30) & kLbIndMax;
+    if (ticket > 0) {
+        long long j = (long long)ticket - 1;
+        const long long t0 = clock64();
+        for (;;) {
+            unsigned long long w[4];
+            int mi = 0x7fffffff, mz = 0x7fffffff;
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            v += __shfl_xor_sync(0xffffffffu, v, o);
-            i += __shfl_xor_sync(0xffffffffu, i, o);
+            for (int q = 0; q < 4; ++q) {
+                const int dist = q * 32 + lane;
+                const long long idx = j - dist;
+                w[q] = idx >= 0 ? ld_relaxed(&a.lookback[idx]) : kLbInclusive;
+                const unsigned st = (unsigned)(w[q] >> 62);
+                if (st == 2u) mi = min(mi, dist);
+                if (st == 0u) mz = min(mz, dist);
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                mi = min(mi, __shfl_xor_sync(0xffffffffu, mi, o));
+                mz = min(mz, __shfl_xor_sync(0xffffffffu, mz, o));
+            }
+            if (mz < mi) {  // an unpublished predecessor lies before the nearest inclusive prefix
+                if (clock64() - t0 > a.spin_limit_cycles) {
+                    if (lane == 0) atomicOr(errflags, (uint32_t)kErrTimeout);
+                    sum = kLbVertMax | (kLbIndMax << 30);
+                    break;
+                }
+                __nanosleep(64);
+                continue;
+            }
+            unsigned long long v = 0ull, i = 0ull;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                if (q * 32 + lane <= mi) {
+                    v += w[q] & kLbVertMax;
+                    i += (w[q] >> 30) & kLbIndMax;
+                }
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                v += __shfl_xor_sync(0xffffffffu, v, o);
+                i += __shfl_xor_sync(0xffffffffu, i, o);
+            }
+            sum = sat_add_packed(sum, (v > kLbVertMax ? kLbVertMax : v) | ((i > kLbIndMax ? kLbIndMax : i) << 30));
+            if (mi != 0x7fffffff) break;
+            j -= 128;
         }
-        sum = sat_add_packed(sum, (v > kLbVertMax ? kLbVertMax : v) | ((i > kLbIndMax ? kLbIndMax : i) << 30));
-        if (incl) break;
-        j -= 32;
     }
-    if (timed_out) {
-        sum = kLbVertMax | (kLbIndMax << 30);
-        if (lane == 0) atomicOr(&a.totals[3], kErrTimeout);
-    }
-    if (lane == 0) st_release(&a.lookback[ticket], kLbInclusive | sat_add_packed(sum, own));
+    if (lane == 0) st_relaxed(&a.lookback[ticket], kLbInclusive | sat_add_packed(sum, own));
     return sum;
 }
 
+// The chunk record and its output offsets, from its exclusive prefix; run by
+// one thread.
+__device__ __forceinline__ void chunk_record(const BuildArgs& a, SmemTables& T, const ChunkInfo& ci,
+                                             unsigned long long ex, Offsets& off, bool queue)
+{
+    const uint32_t nV = (uint32_t)(ci.total & kField22);
+    const uint32_t nI = (uint32_t)((ci.total >> kIndShift) & kField22);
+    const uint32_t nA = (uint32_t)(ci.total >> kActShift);
+    const unsigned long long ev = ex & kLbVertMax, ei = (ex >> 30) & kLbIndMax;
+    const bool fits = ev + nV <= a.vert_capacity && ei + nI <= a.ind_capacity;
+    uint32_t flags = ci.flags;
+    if (nI > 0) flags |= UWW_CHUNK_HAS_MESH;
+    if (!fits) {
+        flags |= UWW_CHUNK_OVERFLOW;
+        T.overflow += 1;
+    }
+    off.excl = ev | (ei << 32);
+    off.fits = fits;
+    uww_chunk_record rec;
+    rec.num_verts = nV;
+    rec.num_inds = nI;
+    rec.vert_offset = (uint32_t)(ev > 0xffffffffull ? 0xffffffffull : ev);
+    rec.ind_offset = (uint32_t)(ei > 0xffffffffull ? 0xffffffffull : ei);
+    rec.flags = flags;
+    rec.num_active_cells = nA;
+    rec.reserved[0] = rec.reserved[1] = 0;
+    a.records[ci.ticket] = rec;
+    if (!queue || ci.ticket == a.n - 1) {
+        a.totals[0] = ev + nV;
+        a.totals[1] = ei + nI;
+    }
+}
+
+// ---------------------------------------------------------------------------
+struct Workspace {
+    float* rho;
+    uint8_t* cases;
+    void* vbase;
+    void* active;
+    void* ibase;
+    bool idx16, active16;
+    __device__ uint32_t get_vbase(int c) const
+    {
+        return idx16 ? (uint32_t)reinterpret_cast<const uint16_t*>(vbase)[c] : reinterpret_cast<const uint32_t*>(vbase)[c];
+    }
+    __device__ void set_vbase(int c, uint32_t v) const
+    {
+        if (idx16) reinterpret_cast<uint16_t*>(vbase)[c] = (uint16_t)v; else reinterpret_cast<uint32_t*>(vbase)[c] = v;
+    }
+    __device__ uint32_t get_ibase(int i) const
+    {
+        return idx16 ? (uint32_t)reinterpret_cast<const uint16_t*>(ibase)[i] : reinterpret_cast<const uint32_t*>(ibase)[i];
+    }
+    __device__ void set_ibase(int i, uint32_t v) const
+    {
+        if (idx16) reinterpret_cast<uint16_t*>(ibase)[i] = (uint16_t)v; else reinterpret_cast<uint32_t*>(ibase)[i] = v;
+    }
+    __device__ int get_active(int i) const
+    {
+        return active16 ? (int)reinterpret_cast<const uint16_t*>(active)[i] : (int)reinterpret_cast<const uint32_t*>(active)[i];
+    }
+    __device__ void set_active(int i, int c) const
+    {
+        if (active16) reinterpret_cast<uint16_t*>(active)[i] = (uint16_t)c; else reinterpret_cast<uint32_t*>(active)[i] = (uint32_t)c;
+    }
+};
+
+__device__ __forceinline__ Workspace workspace(const BuildArgs& a, uint8_t* dyn_smem, int buf, int N)
+{
+    const ChunkLayout L = chunk_layout(N);
+    uint8_t* base = (uint32_t)N <= a.smem_cells
+                        ? dyn_smem + (size_t)buf * a.smem_buf_bytes
+                        : a.scratch + ((size_t)blockIdx.x * a.slots_per_cta + buf) * a.scratch_slot_bytes;
+    Workspace w;
+    w.rho = reinterpret_cast<float*>(base + L.rho);
+    w.cases = base + L.cases;
+    w.vbase = base + L.vbase;
+    w.active = base + L.active;
+    w.ibase = base + L.ibase;
+    w.idx16 = L.idx16;
+    w.active16 = L.active16;
+    return w;
+}
+
+// Front half of a chunk into workspace `buf`.  Every compute thread must call it.
 template <class O, bool QUEUE>
-__global__ void __launch_bounds__(512) build_kernel(const DevParams p, const BuildArgs a)
+__device__ void chunk_front(const DevParams& p, const BuildArgs& a, SmemTables& T, uint8_t* dyn_smem,
+                            const uww_chunk_desc d, uint32_t ticket, int buf, int ncomp, int nall)
+{
+    const int tid = threadIdx.x;
+    const int oriented = p.dedup_mode == UWW_DEDUP_ORIENTED;
+    const bool want_cases = (p.outputs & UWW_OUT_CASES) != 0 && a.cases != nullptr;
+
+    const bool cells_ok = d.cells >= 1 && d.cells <= a.max_cells && d.cells <= UWW_MAX_CELLS;
+    const int N = cells_ok ? (int)d.cells : 1;
+    const int S = N + 1;
+    const int NC = N * N * N;
+    // every global read or write of this chunk's per-cell / per-sample data
+    // is checked against the capacity the caller gave
+    const bool bad = !cells_ok ||
+                     (a.samples_in && (unsigned long long)d.sample_offset + S * S * S > a.samples_in_count);
+    const bool cases_ok = want_cases && !bad && (unsigned long long)d.cell_offset + NC <= a.case_capacity;
+    const bool samples_ok = a.samples_out && !bad && (unsigned long long)d.sample_offset + S * S * S <= a.sample_capacity;
+    if (tid == 0) {
+        if (bad) atomicOr(&T.errflags, (uint32_t)kErrBadChunk);
+        else if ((want_cases && !cases_ok) || (a.samples_out && !samples_ok)) atomicOr(&T.errflags, (uint32_t)kErrRange);
+    }
+    const Workspace W = workspace(a, dyn_smem, buf, N);
+    float* rho = W.rho;
+    uint8_t* cases = W.cases;
+    const int ox = d.pos[0] * p.chunk_size, oy = d.pos[1] * p.chunk_size, oz = d.pos[2] * p.chunk_size;
+
+    // ---- density grid (build_iso) + early blank vote ----
+    int inside = 0;
+    if (!bad) {
+        const float s = __fdiv_rn((float)p.chunk_size, (float)N);  // SIZE_SCALE
+        const int S2 = S * S, S3 = S2 * S;
+        if (a.samples_in) {
+            const float* src = a.samples_in + d.sample_offset;
+            for (int idx = tid; idx < S3; idx += ncomp) {
+                const float v = src[idx];
+                rho[idx] = v;
+                inside |= !(v > p.iso_level);
+            }
+        } else if constexpr (std::is_same<O, FastOps>::value) {
+            inside = sample_columns_fast(p, T.perm, T.gp, ztable_at(dyn_smem + a.ztable_offset, S, p.octaves), rho, N,
+                                         ox, oy, oz, ncomp);
+        } else {
+            for (int idx = tid; idx < S3; idx += ncomp) {
+                const int x = idx / S2, r = idx - x * S2, y = r / S, z = r - y * S;
+                const float wx = O::add(O::mul((float)x, s), (float)ox);
+                const float wy = O::add(O::mul((float)y, s), (float)oy);
+                const float wz = O::add(O::mul((float)z, s), (float)oz);
+                const float v = density<O, false>(p, T.perm, wx, wy, wz, nullptr);
+                rho[idx] = v;
+                inside |= !(v > p.iso_level);
+            }
+        }
+    }
+    const int any_inside = bar_or(kBarCompute, ncomp, inside);
+    // tell the control warp the noise is done: it now resolves the previous
+    // chunk's look-back while this chunk is classified
+    if (QUEUE) bar_arrive(kBarNoiseDone, nall);
+    if (samples_ok) {
+        float* dst = a.samples_out + d.sample_offset;
+        for (int idx = tid; idx < S * S * S; idx += ncomp) dst[idx] = rho[idx];
+    }
+
+    unsigned long long total = 0ull;
+    if (bad || !any_inside) {
+        if (QUEUE && tid == 0) lookback_publish(a, ticket, 0ull);
+        if (!bad && cases_ok)
+            for (int c = tid; c < NC; c += ncomp) a.cases[(size_t)d.cell_offset + c] = 0;
+    } else {
+        // ---- classify + count, contiguous runs of cells per thread ----
+        const int R = (NC + ncomp - 1) / ncomp;
+        const int c0 = min(tid * R, NC), c1 = min(c0 + R, NC);
+        unsigned long long mine = 0ull;
+        {
+            int x = c0 / (N * N), y = (c0 / N) % N, z = c0 % N;
+            const float iso = p.iso_level;
+            const int SS = S * S;
+            // the z+1 face of a cell is the z face of the next cell in the
+            // run: carry its 4 inside bits (corners 3,2,7,6 -> 0,1,4,5)
+            int lo = -1;
+            for (int c = c0; c < c1; ++c) {
+                const int b = (x * S + y) * S + z;
+                if (lo < 0)
+                    lo = (rho[b] < iso) | ((rho[b + SS] < iso) << 1) | ((rho[b + S] < iso) << 4) |
+                         ((rho[b + SS + S] < iso) << 5);
+                const int c3 = rho[b + 1] < iso, c2 = rho[b + SS + 1] < iso;
+                const int c7 = rho[b + S + 1] < iso, c6 = rho[b + SS + S + 1] < iso;
+                const int cs = lo | (c2 << 2) | (c3 << 3) | (c6 << 6) | (c7 << 7);
+                lo = (z + 1 < N) ? (c3 | (c2 << 1) | (c7 << 4) | (c6 << 5)) : -1;
+                cases[c] = (uint8_t)cs;
+                const int nt = T.ntri[cs];
+                if (nt) {
+                    const unsigned own = T.owned[oriented][boundary_flags(x, y, z, N)];
+                    const unsigned nv = __popc(T.edges[cs] & own);
+                    mine += (unsigned long long)nv | ((unsigned long long)(3 * nt) << kIndShift) | (1ull << kActShift);
+                }
+                if (++z == N) { z = 0; if (++y == N) { y = 0; ++x; } }
+            }
+        }
+        unsigned long long run = block_exclusive_scan(mine, T, total, ncomp);
+        // publish the aggregate as soon as the counts are known
+        if (QUEUE && tid == 0) lookback_publish(a, ticket, pack_counts(total));
+        {
+            // second pass over the same runs: each cell's first vertex id and
+            // the active-cell list with its first index position
+            int x = c0 / (N * N), y = (c0 / N) % N, z = c0 % N;
+            for (int c = c0; c < c1; ++c) {
+                const int cs = cases[c];
+                W.set_vbase(c, (uint32_t)(run & kField22));
+                const int nt = T.ntri[cs];
+                if (nt) {
+                    const uint32_t ar = (uint32_t)(run >> kActShift);
+                    W.set_active(ar, c);
+                    W.set_ibase(ar, (uint32_t)((run >> kIndShift) & kField22));
+                    const unsigned own = T.owned[oriented][boundary_flags(x, y, z, N)];
+                    run += (unsigned long long)__popc(T.edges[cs] & own) | ((unsigned long long)(3 * nt) << kIndShift) |
+                           (1ull << kActShift);
+                }
+                if (++z == N) { z = 0; if (++y == N) { y = 0; ++x; } }
+            }
+        }
+        if (cases_ok)
+            for (int c = tid; c < NC; c += ncomp) a.cases[(size_t)d.cell_offset + c] = cases[c];
+    }
+    if (tid == 0) {
+        ChunkInfo& ci = T.ci[buf];
+        ci.ticket = ticket;
+        ci.ox = ox; ci.oy = oy; ci.oz = oz;
+        ci.N = N;
+        ci.flags = (!bad && !any_inside) ? UWW_CHUNK_EARLY_BLANK : 0u;
+        ci.classified = !bad && any_inside;
+        ci.total = total;
+    }
+}
+
+// Emission of a chunk from workspace `buf`, given its offsets.  Every compute
+// thread must call it.
+template <class O>
+__device__ void chunk_emit(const DevParams& p, const BuildArgs& a, SmemTables& T, uint8_t* dyn_smem, int buf,
+                           const Offsets off, int ncomp)
+{
+    const int tid = threadIdx.x;
+    const ChunkInfo ci = T.ci[buf];
+    const uint32_t nV = (uint32_t)(ci.total & kField22);
+    const uint32_t nA = (uint32_t)(ci.total >> kActShift);
+    if (!(ci.classified && off.fits && nA > 0)) return;
+    const int oriented = p.dedup_mode == UWW_DEDUP_ORIENTED;
+    const bool want_color = (p.outputs & UWW_OUT_COLOR) != 0;
+    const bool want_normals = (p.outputs & UWW_OUT_NORMALS) != 0 && a.normals != nullptr;
+    const int N = ci.N, S = N + 1;
+    const uint32_t voff = (uint32_t)(off.excl & 0xffffffffull);
+    const uint32_t ioff = (uint32_t)(off.excl >> 32);
+    const Workspace W = workspace(a, dyn_smem, buf, N);
+    const float* rho = W.rho;
+    const uint8_t* cases = W.cases;
+    const int ox = ci.ox, oy = ci.oy, oz = ci.oz;
+    {
+        const float s = __fdiv_rn((float)p.chunk_size, (float)N);
+        const float iso = p.iso_level;
+        for (uint32_t ai = tid; ai < nA; ai += ncomp) {
+            const int c = W.get_active(ai);
+            const int x = c / (N * N), y = (c / N) % N, z = c % N;
+            const int cs = cases[c];
+            const int8_t* row = T.tri[cs];
+            const unsigned own_mask = T.owned[oriented][boundary_flags(x, y, z, N)];
+            const uint32_t vb = W.get_vbase(c);
+            const uint32_t ib = W.get_ibase(ai);
+            unsigned seen = 0;
+            uint32_t cnt = 0;
+            const int nidx = 3 * T.ntri[cs];
+            for (int i = 0; i < nidx; ++i) {
+                const int e = row[i];
+                const unsigned bit = 1u << e;
+                uint32_t id;
+                if (own_mask & bit) {
+                    if (!(seen & bit)) {
+                        seen |= bit;
+                        id = vb + cnt++;
+                        const int ca = T.corners[e][0], cb = T.corners[e][1];
+                        const int ax = x + ((0x66 >> ca) & 1), ay = y + (ca >> 2), az = z + ((0xcc >> ca) & 1);
+                        const int bx = x + ((0x66 >> cb) & 1), by = y + (cb >> 2), bz = z + ((0xcc >> cb) & 1);
+                        const float ia = rho[(ax * S + ay) * S + az];
+                        const float ibv = rho[(bx * S + by) * S + bz];
+                        const float sax = O::mul((float)ax, s), say = O::mul((float)ay, s), saz = O::mul((float)az, s);
+                        const float sbx = O::mul((float)bx, s), sby = O::mul((float)by, s), sbz = O::mul((float)bz, s);
+                        const float t = __fdiv_rn(O::sub(iso, ia), O::sub(ibv, ia));
+                        const float mx = O::add(sax, O::mul(t, O::sub(sbx, sax)));
+                        const float my = O::add(say, O::mul(t, O::sub(sby, say)));
+                        const float mz = O::add(saz, O::mul(t, O::sub(sbz, saz)));
+                        float2* v2 = reinterpret_cast<float2*>(a.verts + voff + id);
+                        v2[0] = make_float2(O::add(mx, (float)ox), O::add(my, (float)oy));
+                        // colour slot 0 carries the owner's corner b (the value ramp's
+                        // input, chunk.rs:215) to pass 2, which overwrites it
+                        v2[1] = make_float2(O::add(mz, (float)oz), (float)cb);
+                        v2[2] = make_float2(0.f, 0.f);
+                    } else {
+                        id = vb + rank_in_row(row, own_mask, e);
+                    }
+                } else {
+                    int qx, qy, qz;
+                    const int oe = find_owner(T, e, x, y, z, N, oriented, qx, qy, qz);
+                    const int oc = (qx * N + qy) * N + qz;
+                    const unsigned oown = T.owned[oriented][boundary_flags(qx, qy, qz, N)];
+                    id = W.get_vbase(oc) + rank_in_row(T.tri[cases[oc]], oown, oe);
+                }
+                a.inds[ioff + ib + i] = id;
+            }
+        }
+    }
+    if (want_color || want_normals) {
+        bar_sync(kBarCompute, ncomp);
+        for (uint32_t vid = tid; vid < nV; vid += ncomp) {
+            float2* v2 = reinterpret_cast<float2*>(a.verts + voff + vid);
+            const float2 p01 = v2[0], p2c = v2[1];
+            const int cb = (int)p2c.y;
+            if (want_color) {
+                float col[3];
+                vertex_color<O>(p, p2c.x, cb, col);
+                v2[1] = make_float2(p2c.x, col[0]);
+                v2[2] = make_float2(col[1], col[2]);
+            } else {
+                v2[1] = make_float2(p2c.x, 0.f);
+            }
+            if (want_normals) {
+                float g[3];
+                if constexpr (std::is_same<O, FastOps>::value)
+                    density_grad_fast(p, T.perm, T.gp, p01.x, p01.y, p2c.x, g);
+                else
+                    density<O, true>(p, T.perm, p01.x, p01.y, p2c.x, g);
+                safe_normalize<O>(g);
+                float* nn = a.normals + 3 * (size_t)(voff + vid);
+                nn[0] = g[0]; nn[1] = g[1]; nn[2] = g[2];
+            }
+        }
+    }
+}
+
+// Control warp: take a ticket from the work queue and stage its descriptor.
+__device__ __forceinline__ void take_ticket(const BuildArgs& a, Ticket& tk)
+{
+    const int lane = threadIdx.x & 31;
+    uint32_t t = 0;
+    if (lane == 0) t = atomicAdd(a.work_counter, 1u);
+    t = __shfl_sync(0xffffffffu, t, 0);
+    if (t < a.n && lane < 8)
+        reinterpret_cast<uint32_t*>(&tk.desc)[lane] = reinterpret_cast<const uint32_t*>(&a.chunks[t])[lane];
+    if (lane == 0) tk.ticket = t;
+    __syncwarp();
+}
+
+// MAXT/MINB: the launch bounds of an instantiation.  Chunks of up to 16 cells
+// per edge run with <= 224 threads (192 compute + the control warp) and at
+// least 4 CTAs per SM (<= 72
+// registers); larger chunks run with up to 544 threads.
+template <class O, bool QUEUE, int MAXT, int MINB>
+__global__ void __launch_bounds__(MAXT, MINB) build_kernel(const DevParams p, const BuildArgs a)
 {
     extern __shared__ __align__(16) uint8_t dyn_smem[];
     __shared__ SmemTables T;
     const int tid = threadIdx.x, nthr = blockDim.x;
+    // batched form: the last warp is the control warp
+    const int ncomp = QUEUE ? nthr - 32 : nthr;
 
     // ---- per-CTA setup: tables into shared memory ----
-    for (int i = tid; i < 256 * 16; i += nthr) (&T.tri[0][0])[i] = (&UWW_TRI_TABLE[0][0])[i];
+    {
+        const int4* src = reinterpret_cast<const int4*>(&UWW_TRI_TABLE[0][0]);
+        int4* dst = reinterpret_cast<int4*>(&T.tri[0][0]);
+        for (int i = tid; i < 256; i += nthr) dst[i] = src[i];
+    }
     for (int i = tid; i < 256; i += nthr) {
         T.edges[i] = UWW_CASE_EDGES[i];
         T.ntri[i] = UWW_CASE_NTRI[i];
         T.perm[i] = p.perm[i];
+        float gx, gy, gz;
+        grad_vec(p.perm[i], gx, gy, gz);
+        T.gp[i] = make_float4(gx, gy, gz, 0.f);
     }
+    for (int i = tid; i < 128; i += nthr) (&T.owned[0][0])[i] = (&UWW_OWNED_MASK[0][0])[i];
     for (int i = tid; i < 12 * 4 * 5; i += nthr) (&T.share[0][0][0])[i] = (&UWW_EDGE_SHARE[0][0][0])[i];
     for (int i = tid; i < 24; i += nthr) (&T.corners[0][0])[i] = (&UWW_EDGE_CORNERS[0][0])[i];
+    if (tid == 0) { T.errflags = 0; T.overflow = 0; }
     __syncthreads();
-    // owned-edge mask for each boundary situation; cells of a chunk with N >= 2
-    // only differ through the six "at a face" flags.
-    for (int i = tid; i < 128; i += nthr) {
-        const int oriented = i >> 6, f = i & 63;
-        // a representative cell with these flags in a large chunk
-        const int N = 4;
-        const int x = (f & 1) ? 0 : ((f & 8) ? N - 1 : 1);
-        const int y = (f & 2) ? 0 : ((f & 16) ? N - 1 : 1);
-        const int z = (f & 4) ? 0 : ((f & 32) ? N - 1 : 1);
-        unsigned m = 0;
-        for (int e = 0; e < 12; ++e) {
-            int ox, oy, oz;
-            const int oe = find_owner(T, e, x, y, z, N, oriented != 0, ox, oy, oz);
-            if (oe == e && ox == x && oy == y && oz == z) m |= 1u << e;
+
+    if (!QUEUE) {
+        chunk_front<O, QUEUE>(p, a, T, dyn_smem, a.chunks[0], 0u, 0, ncomp, 0);
+        bar_sync(kBarCompute, ncomp);
+        if (tid == 0) chunk_record(a, T, T.ci[0], 0ull, T.off[0], false);
+        bar_sync(kBarCompute, ncomp);
+        chunk_emit<O>(p, a, T, dyn_smem, 0, T.off[0], ncomp);
+        bar_sync(kBarCompute, ncomp);
+        if (tid == 0) {
+            a.totals[2] = T.overflow;
+            a.totals[3] = T.errflags;
         }
-        T.owned[oriented][f] = (uint16_t)m;
+        return;
+    }
+
+    if (tid >= ncomp) {
+        // ---- control warp ----
+        take_ticket(a, T.tk[0]);
+        for (int i = 0;; ++i) {
+            bar_sync(kBarTicket, nthr);  // ticket i staged; chunk i-1's counts visible
+            const bool valid = T.tk[i & 1].ticket < a.n;
+            // the look-back of chunk i-1 waits until chunk i's noise is done, so
+            // its predecessors have had a whole noise phase to publish
+            if (valid) bar_sync(kBarNoiseDone, nthr);
+            if (i > 0) {
+                const ChunkInfo ci = T.ci[(i - 1) & 1];
+                const unsigned long long ex = lookback_warp(a, ci.ticket, pack_counts(ci.total), &T.errflags);
+                if ((tid & 31) == 0) chunk_record(a, T, ci, ex, T.off[(i - 1) & 1], true);
+                __syncwarp();
+                bar_sync(kBarOffsets, nthr);
+            }
+            // take the next ticket only once chunk i-1 is emitted: a ticket's
+            // front half then starts as soon as it is taken, so the chunks
+            // that follow it in the queue do not wait on a late aggregate
+            if (!valid) break;
+            if (i > 0) bar_sync(kBarEmitDone, nthr);
+            take_ticket(a, T.tk[(i + 1) & 1]);
+        }
+    } else {
+        // ---- compute warps ----
+        for (int i = 0;; ++i) {
+            bar_sync(kBarTicket, nthr);
+            const Ticket tk = T.tk[i & 1];
+            const bool valid = tk.ticket < a.n;
+            if (valid) chunk_front<O, QUEUE>(p, a, T, dyn_smem, tk.desc, tk.ticket, i & 1, ncomp, nthr);
+            bar_sync(kBarCompute, ncomp);
+            if (i > 0) {
+                bar_sync(kBarOffsets, nthr);
+                chunk_emit<O>(p, a, T, dyn_smem, (i - 1) & 1, T.off[(i - 1) & 1], ncomp);
+                bar_sync(kBarCompute, ncomp);  // workspace (i-1)&1 is reused by chunk i+1
+                if (valid) bar_arrive(kBarEmitDone, nthr);
+            }
+            if (!valid) break;
+        }
+    }
+
+    // ---- end of launch: fold this CTA's counters; the last CTA publishes
+    // them and leaves the look-back state zeroed for the next launch ----
+    __syncthreads();
+    if (tid == 0) {
+        if (T.overflow) atomicAdd(&a.acc[0], (unsigned long long)T.overflow);
+        if (T.errflags) atomicOr(&a.acc[1], (unsigned long long)T.errflags);
+        __threadfence();
+        T.last = atomicAdd(&a.acc[2], 1ull) == (unsigned long long)gridDim.x - 1;
     }
     __syncthreads();
-
-    const bool oriented = p.dedup_mode == UWW_DEDUP_ORIENTED;
-    const bool want_color = (p.outputs & UWW_OUT_COLOR) != 0;
-    const bool want_normals = (p.outputs & UWW_OUT_NORMALS) != 0 && a.normals != nullptr;
-    const bool want_cases = (p.outputs & UWW_OUT_CASES) != 0 && a.cases != nullptr;
-
-    for (;;) {
-        if (tid == 0) T.ticket = QUEUE ? atomicAdd(a.work_counter, 1u) : 0u;
-        __syncthreads();
-        const uint32_t ticket = T.ticket;
-        if (ticket >= a.n) break;
-
-        const uww_chunk_desc d = a.chunks[ticket];
-        const int N = (int)d.cells;
-        const bool bad = N < 1 || N > (int)a.max_cells || N > UWW_MAX_CELLS;
-        const int S = N + 1;
-        const int NC = N * N * N;
-
-        uint8_t* ws = nullptr;
-        ChunkLayout L = chunk_layout(bad ? 1 : N);
-        if (!bad) ws = (uint32_t)N <= a.smem_cells ? dyn_smem : a.scratch + (size_t)blockIdx.x * a.scratch_slot_bytes;
-        float* rho = reinterpret_cast<float*>(ws + L.rho);
-        uint8_t* cases = ws + L.cases;
-        uint32_t* vbase = reinterpret_cast<uint32_t*>(ws + L.vbase);
-        uint16_t* active16 = reinterpret_cast<uint16_t*>(ws + L.active);
-        uint32_t* active32 = reinterpret_cast<uint32_t*>(ws + L.active);
-        uint32_t* ibase = reinterpret_cast<uint32_t*>(ws + L.ibase);
-
-        const int ox = d.pos[0] * p.chunk_size, oy = d.pos[1] * p.chunk_size, oz = d.pos[2] * p.chunk_size;
-
-        // ---- 1. density grid (build_iso) + early blank vote ----
-        int inside = 0;
-        if (!bad) {
-            const float s = __fdiv_rn((float)p.chunk_size, (float)N);  // SIZE_SCALE
-            const int S2 = S * S, S3 = S2 * S;
-            if (a.samples_in) {
-                const float* src = a.samples_in + d.sample_offset;
-                for (int idx = tid; idx < S3; idx += nthr) {
-                    const float v = src[idx];
-                    rho[idx] = v;
-                    inside |= !(v > p.iso_level);
-                }
-            } else {
-                for (int idx = tid; idx < S3; idx += nthr) {
-                    const int x = idx / S2, r = idx - x * S2, y = r / S, z = r - y * S;
-                    const float wx = O::add(O::mul((float)x, s), (float)ox);
-                    const float wy = O::add(O::mul((float)y, s), (float)oy);
-                    const float wz = O::add(O::mul((float)z, s), (float)oz);
-                    const float v = density<O, false>(p, T.perm, wx, wy, wz, nullptr);
-                    rho[idx] = v;
-                    inside |= !(v > p.iso_level);
-                }
-            }
-            if (a.samples_out) {
-                float* dst = a.samples_out + d.sample_offset;
-                for (int idx = tid; idx < S3; idx += nthr) dst[idx] = rho[idx];
-            }
+    if (T.last) {
+        __threadfence();
+        for (uint32_t i = tid; i < a.n; i += nthr) a.lookback[i] = 0ull;
+        if (tid == 0) {
+            a.totals[2] = atomicExch(&a.acc[0], 0ull);
+            a.totals[3] = atomicExch(&a.acc[1], 0ull);
+            atomicExch(&a.acc[2], 0ull);
+            atomicExch(a.work_counter, 0u);
         }
-        const int any_inside = __syncthreads_or(inside);
-
-        unsigned long long total = 0ull;
-        uint32_t flags = 0;
-        if (bad) {
-            if (tid == 0) atomicOr(&a.totals[3], kErrBadChunk);
-        } else if (!any_inside) {
-            flags = UWW_CHUNK_EARLY_BLANK;
-            if (want_cases)
-                for (int c = tid; c < NC; c += nthr) a.cases[(size_t)d.cell_offset + c] = 0;
-        } else {
-            // ---- 2. classify + count, contiguous runs of cells per thread ----
-            const int R = (NC + nthr - 1) / nthr;
-            const int c0 = min(tid * R, NC), c1 = min(c0 + R, NC);
-            unsigned long long mine = 0ull;
-            {
-                int x = c0 / (N * N), y = (c0 / N) % N, z = c0 % N;
-                for (int c = c0; c < c1; ++c) {
-                    const int b = (x * S + y) * S + z;
-                    const float iso = p.iso_level;
-                    int cs = 0;
-                    cs |= (rho[b] < iso) << 0;
-                    cs |= (rho[b + S * S] < iso) << 1;
-                    cs |= (rho[b + S * S + 1] < iso) << 2;
-                    cs |= (rho[b + 1] < iso) << 3;
-                    cs |= (rho[b + S] < iso) << 4;
-                    cs |= (rho[b + S * S + S] < iso) << 5;
-                    cs |= (rho[b + S * S + S + 1] < iso) << 6;
-                    cs |= (rho[b + S + 1] < iso) << 7;
-                    cases[c] = (uint8_t)cs;
-                    const int nt = T.ntri[cs];
-                    if (nt) {
-                        const unsigned own = T.owned[oriented][boundary_flags(x, y, z, N)];
-                        const unsigned nv = __popc(T.edges[cs] & own);
-                        mine += (unsigned long long)nv | ((unsigned long long)(3 * nt) << kIndShift) |
-                                (1ull << kActShift);
-                    }
-                    if (++z == N) { z = 0; if (++y == N) { y = 0; ++x; } }
-                }
-            }
-            unsigned long long run = block_exclusive_scan(mine, T, total);
-            {
-                for (int c = c0; c < c1; ++c) {
-                    const int cs = cases[c];
-                    vbase[c] = (uint32_t)(run & kField22);
-                    const int nt = T.ntri[cs];
-                    if (nt) {
-                        const uint32_t ar = (uint32_t)(run >> kActShift);
-                        if (L.active16) active16[ar] = (uint16_t)c; else active32[ar] = (uint32_t)c;
-                        ibase[ar] = (uint32_t)((run >> kIndShift) & kField22);
-                        const int x = c / (N * N), y = (c / N) % N, z = c % N;
-                        const unsigned own = T.owned[oriented][boundary_flags(x, y, z, N)];
-                        run += (unsigned long long)__popc(T.edges[cs] & own) |
-                               ((unsigned long long)(3 * nt) << kIndShift) | (1ull << kActShift);
-                    }
-                }
-            }
-            if (want_cases)
-                for (int c = tid; c < NC; c += nthr) a.cases[(size_t)d.cell_offset + c] = cases[c];
-        }
-
-        const uint32_t nV = (uint32_t)(total & kField22);
-        const uint32_t nI = (uint32_t)((total >> kIndShift) & kField22);
-        const uint32_t nA = (uint32_t)(total >> kActShift);
-
-        // ---- 3. output offsets ----
-        if (tid < 32) {
-            const unsigned long long own = (unsigned long long)nV | ((unsigned long long)nI << 30);
-            unsigned long long ex = 0ull;
-            if (QUEUE) ex = lookback(a, ticket, own);
-            if (tid == 0) {
-                const unsigned long long ev = ex & kLbVertMax, ei = (ex >> 30) & kLbIndMax;
-                const bool fits = ev + nV <= a.vert_capacity && ei + nI <= a.ind_capacity;
-                T.excl = ev | (ei << 32);
-                T.fits = fits;
-                if (nI > 0) flags |= UWW_CHUNK_HAS_MESH;
-                if (!fits) {
-                    flags |= UWW_CHUNK_OVERFLOW;
-                    if (QUEUE) atomicAdd(&a.totals[2], 1ull);
-                }
-                uww_chunk_record rec;
-                rec.num_verts = nV;
-                rec.num_inds = nI;
-                rec.vert_offset = (uint32_t)(ev > 0xffffffffull ? 0xffffffffull : ev);
-                rec.ind_offset = (uint32_t)(ei > 0xffffffffull ? 0xffffffffull : ei);
-                rec.flags = flags;
-                rec.num_active_cells = nA;
-                rec.reserved[0] = rec.reserved[1] = 0;
-                a.records[ticket] = rec;
-                if (!QUEUE) {
-                    a.totals[0] = nV;
-                    a.totals[1] = nI;
-                    a.totals[2] = fits ? 0ull : 1ull;
-                } else if (ticket == a.n - 1) {
-                    a.totals[0] = ev + nV;
-                    a.totals[1] = ei + nI;
-                }
-            }
-        }
-        __syncthreads();
-
-        // ---- 4. emission ----
-        if (!bad && any_inside && T.fits && nA > 0) {
-            const uint32_t voff = (uint32_t)(T.excl & 0xffffffffull);
-            const uint32_t ioff = (uint32_t)(T.excl >> 32);
-            const float s = __fdiv_rn((float)p.chunk_size, (float)N);
-            const float iso = p.iso_level;
-            for (uint32_t ai = tid; ai < nA; ai += nthr) {
-                const int c = L.active16 ? (int)active16[ai] : (int)active32[ai];
-                const int x = c / (N * N), y = (c / N) % N, z = c % N;
-                const int cs = cases[c];
-                const int8_t* row = T.tri[cs];
-                const unsigned own = T.owned[oriented][boundary_flags(x, y, z, N)];
-                const uint32_t vb = vbase[c];
-                const uint32_t ib = ibase[ai];
-                unsigned seen = 0;
-                uint32_t cnt = 0;
-                const int nidx = 3 * T.ntri[cs];
-                for (int i = 0; i < nidx; ++i) {
-                    const int e = row[i];
-                    const unsigned bit = 1u << e;
-                    uint32_t id;
-                    if (own & bit) {
-                        if (!(seen & bit)) {
-                            seen |= bit;
-                            id = vb + cnt++;
-                            // create the vertex (chunk.rs:176-231)
-                            const int ca = T.corners[e][0], cb = T.corners[e][1];
-                            const int ax = x + ((0x66 >> ca) & 1), ay = y + (ca >> 2), az = z + ((0xcc >> ca) & 1);
-                            const int bx = x + ((0x66 >> cb) & 1), by = y + (cb >> 2), bz = z + ((0xcc >> cb) & 1);
-                            const float ia = rho[(ax * S + ay) * S + az];
-                            const float ibv = rho[(bx * S + by) * S + bz];
-                            const float sax = O::mul((float)ax, s), say = O::mul((float)ay, s), saz = O::mul((float)az, s);
-                            const float sbx = O::mul((float)bx, s), sby = O::mul((float)by, s), sbz = O::mul((float)bz, s);
-                            const float t = __fdiv_rn(O::sub(iso, ia), O::sub(ibv, ia));
-                            const float mx = O::add(sax, O::mul(t, O::sub(sbx, sax)));
-                            const float my = O::add(say, O::mul(t, O::sub(sby, say)));
-                            const float mz = O::add(saz, O::mul(t, O::sub(sbz, saz)));
-                            const float wz = O::add(mz, (float)oz);
-                            float pos[3] = {O::add(mx, (float)ox), O::add(my, (float)oy), wz};
-                            float col[3] = {0.f, 0.f, 0.f};
-                            if (want_color) vertex_color<O>(p, wz, cb, col);
-                            uww_vert_color* vv = a.verts + voff + id;
-                            float2* v2 = reinterpret_cast<float2*>(vv);
-                            v2[0] = make_float2(pos[0], pos[1]);
-                            v2[1] = make_float2(pos[2], col[0]);
-                            v2[2] = make_float2(col[1], col[2]);
-                            if (want_normals) {
-                                float g[3];
-                                density<O, true>(p, T.perm, pos[0], pos[1], pos[2], g);
-                                safe_normalize<O>(g);
-                                float* nn = a.normals + 3 * (size_t)(voff + id);
-                                nn[0] = g[0]; nn[1] = g[1]; nn[2] = g[2];
-                            }
-                        } else {
-                            id = vb + rank_in_row(row, own, e);
-                        }
-                    } else {
-                        int qx, qy, qz;
-                        const int oe = find_owner(T, e, x, y, z, N, oriented, qx, qy, qz);
-                        const int oc = (qx * N + qy) * N + qz;
-                        const unsigned oown = T.owned[oriented][boundary_flags(qx, qy, qz, N)];
-                        id = vbase[oc] + rank_in_row(T.tri[cases[oc]], oown, oe);
-                    }
-                    a.inds[ioff + ib + i] = id;
-                }
-            }
-        }
-        if (!QUEUE) break;
-        __syncthreads();  // the working set is reused by the next ticket
     }
 }
 
@@ -462,45 +886,82 @@ __global__ void density_kernel(const DevParams p, const float* __restrict__ xyz,
         out[i] = density<O, false>(p, P, xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], nullptr);
 }
 
-template <class O, bool Q>
-cudaError_t set_smem_attr(size_t bytes)
+// FP32 peak probe: 8 independent FMA chains per thread, no memory traffic
+// except one store per thread to keep the chains live.
+__global__ void __launch_bounds__(256) fma_probe_kernel(uint32_t iters, float seed, float* __restrict__ sink)
 {
-    return cudaFuncSetAttribute(build_kernel<O, Q>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    float a0 = seed + threadIdx.x, a1 = a0 + 1.f, a2 = a0 + 2.f, a3 = a0 + 3.f;
+    float a4 = a0 + 4.f, a5 = a0 + 5.f, a6 = a0 + 6.f, a7 = a0 + 7.f;
+    const float m = 0.9999999f, c = 1e-7f;
+    for (uint32_t i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            a0 = fmaf(a0, m, c); a1 = fmaf(a1, m, c); a2 = fmaf(a2, m, c); a3 = fmaf(a3, m, c);
+            a4 = fmaf(a4, m, c); a5 = fmaf(a5, m, c); a6 = fmaf(a6, m, c); a7 = fmaf(a7, m, c);
+        }
+    }
+    sink[blockIdx.x * blockDim.x + threadIdx.x] = ((a0 + a1) + (a2 + a3)) + ((a4 + a5) + (a6 + a7));
+}
+
+using BuildFn = void (*)(const DevParams, const BuildArgs);
+
+// [exact][queue][large]
+BuildFn kernel_for(bool exact, bool queue, bool large)
+{
+    static const BuildFn table[2][2][2] = {
+        {{build_kernel<FastOps, false, 224, 4>, build_kernel<FastOps, false, 544, 1>},
+         {build_kernel<FastOps, true, 224, 4>, build_kernel<FastOps, true, 544, 1>}},
+        {{build_kernel<ExactOps, false, 224, 4>, build_kernel<ExactOps, false, 544, 1>},
+         {build_kernel<ExactOps, true, 224, 4>, build_kernel<ExactOps, true, 544, 1>}}};
+    return table[exact][queue][large];
+}
+
+size_t set_smem_attr(BuildFn fn, size_t optin)
+{
+    // The largest dynamic allocation the driver accepts next to this kernel's
+    // static shared memory: start from the opt-in limit and step down.
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, fn) != cudaSuccess) return 0;
+    size_t want = optin > fa.sharedSizeBytes ? (optin - fa.sharedSizeBytes) & ~size_t(15) : 0;
+    for (int i = 0; i < 16 && want >= 1024; ++i, want -= 1024) {
+        if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)want) == cudaSuccess)
+            return want;
+        (void)cudaGetLastError();
+    }
+    return 0;
 }
 
 }  // namespace
 
 size_t build_static_smem_bytes() { return sizeof(SmemTables); }
 
-cudaError_t prepare_build_kernels(size_t max_dyn_smem)
+cudaError_t prepare_build_kernels(size_t optin, size_t* max_dyn_smem)
 {
-    cudaError_t e;
-    if ((e = set_smem_attr<ExactOps, true>(max_dyn_smem)) != cudaSuccess) return e;
-    if ((e = set_smem_attr<ExactOps, false>(max_dyn_smem)) != cudaSuccess) return e;
-    if ((e = set_smem_attr<FastOps, true>(max_dyn_smem)) != cudaSuccess) return e;
-    return set_smem_attr<FastOps, false>(max_dyn_smem);
+    size_t m = ~size_t(0);
+    for (int e = 0; e < 2; ++e)
+        for (int q = 0; q < 2; ++q)
+            for (int l = 0; l < 2; ++l) m = std::min(m, set_smem_attr(kernel_for(e, q, l), optin));
+    *max_dyn_smem = m;
+    return m >= 16384 ? cudaSuccess : cudaErrorInvalidValue;
 }
 
 cudaError_t build_occupancy(bool queue, bool exact, int threads, size_t dyn_smem, int* blocks_per_sm)
 {
-    if (exact)
-        return queue ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, build_kernel<ExactOps, true>, threads, dyn_smem)
-                     : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, build_kernel<ExactOps, false>, threads, dyn_smem);
-    return queue ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, build_kernel<FastOps, true>, threads, dyn_smem)
-                 : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, build_kernel<FastOps, false>, threads, dyn_smem);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, kernel_for(exact, queue, threads > 224),
+                                                         threads, dyn_smem);
 }
 
 cudaError_t launch_build(const DevParams& p, const BuildArgs& a, bool queue, int grid, int threads, size_t dyn_smem,
                          cudaStream_t s)
 {
     const bool exact = p.math_mode == UWW_MATH_EXACT;
-    if (exact) {
-        if (queue) build_kernel<ExactOps, true><<<grid, threads, dyn_smem, s>>>(p, a);
-        else build_kernel<ExactOps, false><<<grid, threads, dyn_smem, s>>>(p, a);
-    } else {
-        if (queue) build_kernel<FastOps, true><<<grid, threads, dyn_smem, s>>>(p, a);
-        else build_kernel<FastOps, false><<<grid, threads, dyn_smem, s>>>(p, a);
-    }
+    kernel_for(exact, queue, threads > 224)<<<grid, threads, dyn_smem, s>>>(p, a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fma_probe(int blocks, uint32_t iters, float* sink, cudaStream_t s)
+{
+    fma_probe_kernel<<<blocks, 256, 0, s>>>(iters, 1.0f, sink);
     return cudaGetLastError();
 }
 

@@ -14,6 +14,8 @@
 #pragma once
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "uww.h"
 
 namespace uww {
@@ -233,6 +235,73 @@ __device__ __forceinline__ float density(const DevParams& p, const uint8_t* P, f
     return f;
 }
 
+// Fast build: density gradient at a world point for vertex normals.  Same
+// Perlin/fBm maths, written as trilinear interpolation with FMA, the corner
+// gradient vectors read from gp (gradient of P[i], the last hash lookup):
+//   n      = sum_c w_c v_c,          v_c = g_c . (d - o_c),
+//   dn/dd  = sum_c w_c g_c + (da (Y1 - Y0), db (.), dc (.)),
+// where Y1 - Y0 is the difference of the two faces' bilinear interpolants.
+__device__ __forceinline__ void density_grad_fast(const DevParams& p, const uint8_t* P, const float4* gp, float wx,
+                                                  float wy, float wz, float g[3])
+{
+    const float bf = p.base_freq;
+    const float nx = (wx + p.offset[0]) * bf, ny = (wy + p.offset[1]) * bf, nz = (wz + p.offset[2]) * bf;
+    float gx = 0.f, gy = 0.f, gz = 0.f, msum = 0.f;
+    for (int k = 0; k < p.octaves; ++k) {
+        const float m = p.mult[k], am = p.amp[k];
+        msum += am;
+        const float qx = nx * m, qy = ny * m, qz = nz * m;
+        const float fx = floorf(qx), fy = floorf(qy), fz = floorf(qz);
+        const int ix = (int)fx, iy = (int)fy, iz = (int)fz;
+        const float dx = qx - fx, dy = qy - fy, dz = qz - fz;
+        const float dx1 = dx - 1.f, dy1 = dy - 1.f, dz1 = dz - 1.f;
+        const int a0 = P[ix & 255], a1 = P[(ix + 1) & 255];
+        const int b00 = P[a0 ^ (iy & 255)], b01 = P[a0 ^ ((iy + 1) & 255)];
+        const int b10 = P[a1 ^ (iy & 255)], b11 = P[a1 ^ ((iy + 1) & 255)];
+        const int z0 = iz & 255, z1 = (iz + 1) & 255;
+        // corner index bits: x 4, y 2, z 1
+        const float4 c0 = gp[b00 ^ z0], c1 = gp[b00 ^ z1], c2 = gp[b01 ^ z0], c3 = gp[b01 ^ z1];
+        const float4 c4 = gp[b10 ^ z0], c5 = gp[b10 ^ z1], c6 = gp[b11 ^ z0], c7 = gp[b11 ^ z1];
+        const float v0 = fmaf(c0.x, dx, fmaf(c0.y, dy, c0.z * dz));
+        const float v1 = fmaf(c1.x, dx, fmaf(c1.y, dy, c1.z * dz1));
+        const float v2 = fmaf(c2.x, dx, fmaf(c2.y, dy1, c2.z * dz));
+        const float v3 = fmaf(c3.x, dx, fmaf(c3.y, dy1, c3.z * dz1));
+        const float v4 = fmaf(c4.x, dx1, fmaf(c4.y, dy, c4.z * dz));
+        const float v5 = fmaf(c5.x, dx1, fmaf(c5.y, dy, c5.z * dz1));
+        const float v6 = fmaf(c6.x, dx1, fmaf(c6.y, dy1, c6.z * dz));
+        const float v7 = fmaf(c7.x, dx1, fmaf(c7.y, dy1, c7.z * dz1));
+        const float a = fade<FastOps>(dx), b = fade<FastOps>(dy), c = fade<FastOps>(dz);
+        const float da = dfade<FastOps>(dx), db = dfade<FastOps>(dy), dc = dfade<FastOps>(dz);
+        // trilinear weights as lerps: along z, then y, then x
+        auto lerp = [](float t, float u, float v) { return fmaf(t, v - u, u); };
+        const float z00 = lerp(c, v0, v1), z01 = lerp(c, v2, v3), z10 = lerp(c, v4, v5), z11 = lerp(c, v6, v7);
+        const float y0 = lerp(b, z00, z01), y1 = lerp(b, z10, z11);
+        // d/dx: da * (face x1 - face x0)
+        float tx = da * (y1 - y0);
+        // d/dy: db * lerp_x(z_y1 - z_y0)
+        float ty = db * lerp(a, z01 - z00, z11 - z10);
+        // d/dz: dc * lerp_x(lerp_y(v_z1 - v_z0))
+        float tz = dc * lerp(a, lerp(b, v1 - v0, v3 - v2), lerp(b, v5 - v4, v7 - v6));
+        // + sum_c w_c g_c, as trilinear interpolation of each component
+        auto tri = [&](float e0, float e1, float e2, float e3, float e4, float e5, float e6, float e7) {
+            return lerp(a, lerp(b, lerp(c, e0, e1), lerp(c, e2, e3)), lerp(b, lerp(c, e4, e5), lerp(c, e6, e7)));
+        };
+        tx += tri(c0.x, c1.x, c2.x, c3.x, c4.x, c5.x, c6.x, c7.x);
+        ty += tri(c0.y, c1.y, c2.y, c3.y, c4.y, c5.y, c6.y, c7.y);
+        tz += tri(c0.z, c1.z, c2.z, c3.z, c4.z, c5.z, c6.z, c7.z);
+        const float s = am * m;
+        gx = fmaf(tx, s, gx);
+        gy = fmaf(ty, s, gy);
+        gz = fmaf(tz, s, gz);
+    }
+    float scale = kPerlinScale * bf;
+    if (p.normalize) scale = scale / msum;
+    g[0] = gx * scale;
+    g[1] = gy * scale;
+    g[2] = gz * scale;
+    if (p.bias_mode == UWW_BIAS_LINEAR) g[2] += p.bias_a;
+}
+
 // Unit normal from the density gradient (util.rs:61-64 safe_normalize).
 template <class O>
 __device__ __forceinline__ void safe_normalize(float g[3])
@@ -270,7 +339,11 @@ __device__ __forceinline__ void vertex_color(const DevParams& p, float world_z, 
     const float rgb[3] = {O::mul(O::add(r, m), 255.0f), O::mul(O::add(gg, m), 255.0f), O::mul(O::add(b, m), 255.0f)};
 #pragma unroll
     for (int i = 0; i < 3; ++i)
-        out[i] = powf(__fdiv_rn(O::add(__fdiv_rn(rgb[i], 255.0f), 0.055f), 1.055f), 2.4f);
+    {
+        const float base = __fdiv_rn(O::add(__fdiv_rn(rgb[i], 255.0f), 0.055f), 1.055f);
+        // parity build: powf; fast build: the hardware exp2/log2 pair (base > 0)
+        out[i] = std::is_same<O, FastOps>::value ? __powf(base, 2.4f) : powf(base, 2.4f);
+    }
 }
 
 }  // namespace uww

@@ -14,11 +14,12 @@ namespace uww {
 struct ChunkLayout {
     uint32_t rho;      // (N+1)^3 f32 samples, index (x*S + y)*S + z
     uint32_t cases;    // N^3 u8 case indices, cell order x, y, z
-    uint32_t vbase;    // N^3 u32: first chunk-local vertex id created by each cell
-    uint32_t active;   // active-cell list (u16 when N^3 <= 65536, else u32)
-    uint32_t ibase;    // per active cell: first index position (u32)
+    uint32_t vbase;    // N^3: first chunk-local vertex id created by each cell (u16 when idx16)
+    uint32_t active;   // active-cell list (u16 when active16)
+    uint32_t ibase;    // per active cell: first index position (u16 when idx16)
     uint32_t total;
     bool active16;
+    bool idx16;
 };
 
 __host__ __device__ inline uint32_t align16(uint32_t v) { return (v + 15u) & ~15u; }
@@ -28,14 +29,25 @@ __host__ __device__ inline ChunkLayout chunk_layout(int N)
     ChunkLayout L;
     const uint32_t S = (uint32_t)N + 1, NC = (uint32_t)N * N * N;
     L.active16 = NC <= 65536u;
+    // at most 15 indices per cell, and fewer vertices than indices
+    L.idx16 = 15u * NC < 65536u;
+    const uint32_t ib = L.idx16 ? 2u : 4u;
     uint32_t o = 0;
     L.rho = o;    o = align16(o + S * S * S * 4u);
     L.cases = o;  o = align16(o + NC);
-    L.vbase = o;  o = align16(o + NC * 4u);
+    L.vbase = o;  o = align16(o + NC * ib);
     L.active = o; o = align16(o + NC * (L.active16 ? 2u : 4u));
-    L.ibase = o;  o = align16(o + NC * 4u);
+    L.ibase = o;  o = align16(o + NC * ib);
     L.total = o;
     return L;
+}
+
+// Bytes of the fast build's per-chunk z tables for S samples per edge:
+// (dz, fade) and (first z, cell) per octave and z, run counts, z bias.
+__host__ __device__ inline size_t ztable_bytes(int S, int octaves)
+{
+    return (size_t)octaves * S * (sizeof(float2) + sizeof(int2)) + (size_t)octaves * sizeof(int) +
+           (size_t)S * sizeof(float) + 16;
 }
 
 // Lookback word: [63:62] status, [61:30] indices, [29:0] vertices.
@@ -45,8 +57,9 @@ constexpr unsigned long long kLbVertMax = (1ull << 30) - 1;
 constexpr unsigned long long kLbIndMax = (1ull << 32) - 1;
 
 // totals[3] error bits
-constexpr unsigned long long kErrTimeout = 1ull;
-constexpr unsigned long long kErrBadChunk = 2ull;
+constexpr unsigned long long kErrTimeout = UWW_ERRFLAG_TIMEOUT;
+constexpr unsigned long long kErrBadChunk = UWW_ERRFLAG_BAD;
+constexpr unsigned long long kErrRange = UWW_ERRFLAG_RANGE;
 
 struct BuildArgs {
     const uww_chunk_desc* chunks;
@@ -58,14 +71,21 @@ struct BuildArgs {
     uint8_t* cases;
     float* samples_out;              // optional copy of each chunk's density samples
     const float* samples_in;         // when set, samples are read instead of computed
+    unsigned long long case_capacity;     // bytes at cases
+    unsigned long long sample_capacity;   // floats at samples_out
+    unsigned long long samples_in_count;  // floats at samples_in
     uww_chunk_record* records;
     unsigned long long* totals;      // never NULL inside the kernel
     uint32_t vert_capacity;
     uint32_t ind_capacity;
-    unsigned long long* lookback;    // n words, zeroed before the launch (queue mode)
-    unsigned int* work_counter;      // zeroed before the launch (queue mode)
+    unsigned long long* lookback;    // n words, zero at launch; the last CTA re-zeroes them (queue mode)
+    unsigned int* work_counter;      // zero at launch; reset by the last CTA (queue mode)
+    unsigned long long* acc;         // [0] overflow count, [1] error flags, [2] CTAs finished (queue mode)
     uint8_t* scratch;                // per-CTA slots for chunks above smem_cells
     size_t scratch_slot_bytes;
+    uint32_t slots_per_cta;          // workspaces per CTA (2 in the pipelined batched form)
+    size_t smem_buf_bytes;           // bytes of one shared-memory workspace
+    size_t ztable_offset;            // fast build: per-chunk z tables, after the workspaces
     uint32_t smem_cells;             // chunks with cells <= smem_cells work in shared memory
     long long spin_limit_cycles;     // bound on every device-side wait
 };
@@ -75,7 +95,8 @@ size_t build_static_smem_bytes();
 cudaError_t launch_build(const DevParams& p, const BuildArgs& a, bool queue, int grid, int threads,
                          size_t dyn_smem, cudaStream_t s);
 cudaError_t build_occupancy(bool queue, bool exact, int threads, size_t dyn_smem, int* blocks_per_sm);
-cudaError_t prepare_build_kernels(size_t max_dyn_smem);
+cudaError_t prepare_build_kernels(size_t optin, size_t* max_dyn_smem);
 cudaError_t launch_density(const DevParams& p, const float* xyz, uint32_t n, float* out, cudaStream_t s);
+cudaError_t launch_fma_probe(int blocks, uint32_t iters, float* sink, cudaStream_t s);
 
 }  // namespace uww
