@@ -176,6 +176,24 @@ int   uww_ctx_sync(uww_ctx* ctx);
 int uww_build_chunks(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n,
                      uint32_t max_cells, const uww_mesh_out* out);
 
+/* Batched build for callers that cannot allocate device memory.  No
+ * counterpart in the reference (its chunks are built on the CPU).  For an
+ * engine whose allocator owns all device memory, or code that must not call
+ * cudaMalloc on its frame path: no context (creating one allocates) and no
+ * allocation of any kind.  The caller passes descriptors and output buffers
+ * it already owns; the build's scratch (work-queue counter and the look-back
+ * words of the device-wide prefix sum) is a fixed 512 KB array that the
+ * library holds on every GPU that loads it, for the life of the process.
+ * Limits: n <= 65536 chunks, and each chunk's working set must fit in shared
+ * memory (up to about 18 cells per edge); otherwise UWW_ERR_INVALID_ARG.
+ * Every call shares that array and clears the part it uses first, so calls
+ * that overlap on the GPU race: serialise them.  The first call on a device
+ * looks up the array's address and sets kernel attributes; make it before any
+ * stream capture.  Otherwise as uww_build_chunks, asynchronous on `stream`
+ * (a cudaStream_t, NULL for the legacy default stream). */
+int uww_build_chunks_noalloc(const uww_params* p, void* stream, const uww_chunk_desc* d_chunks, uint32_t n,
+                             uint32_t max_cells, const uww_mesh_out* out);
+
 /* Marching cubes over caller-provided density samples instead of the noise:
  * chunk i reads (cells+1)^3 f32 at d_samples + desc.sample_offset, laid out
  * (x*S + y)*S + z like Build::isos (chunk.rs:43, 351-353).  Otherwise as

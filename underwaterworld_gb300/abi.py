@@ -100,6 +100,7 @@ _SIGS = {
     "uww_ctx_sync": (C.c_int, [P]),
     "uww_build_chunks": (C.c_int, [P, P, C.c_uint32, C.c_uint32, C.POINTER(MeshOut)]),
     "uww_build_chunk_plain": (C.c_int, [P, P, C.c_uint32, C.POINTER(MeshOut)]),
+    "uww_build_chunks_noalloc": (C.c_int, [C.POINTER(Params), P, P, C.c_uint32, C.c_uint32, C.POINTER(MeshOut)]),
     "uww_build_chunks_host": (C.c_int, [P, P, C.c_uint32, C.POINTER(MeshOut)]),
     "uww_ctx_set_tuning": (C.c_int, [P, C.POINTER(Tuning)]),
     "uww_ctx_get_tuning": (C.c_int, [P, C.POINTER(Tuning)]),

@@ -195,8 +195,7 @@ int plan_launch(uww_ctx* ctx, uint32_t n, uint32_t max_cells, bool queue, Launch
     // compute threads: by default about one per (x, y) sample column of the
     // largest chunk, rounded so the last round of columns fills its warps;
     // the batched form adds one control warp
-    const int compute = ctx->threads > 0 ? ctx->threads
-                      : max_cells <= 12 ? 192 : max_cells <= 24 ? 320 : 512;
+    const int compute = ctx->threads > 0 ? ctx->threads : default_compute_threads(max_cells);
     cfg->threads = compute + (queue ? 32 : 0);
     cfg->scratch_slot = max_cells > smem_cells ? chunk_layout((int)max_cells).total : 0;
     if (!queue) {
@@ -275,6 +274,14 @@ int check_out(const uww_mesh_out* out)
 }
 
 }  // namespace
+
+namespace uww {
+int check_params(const uww_params* p) { return validate_params(p); }
+void dev_params_from(const uww_params* p, DevParams* d) { make_dev_params(p, d); }
+int status_from_cuda(cudaError_t e, const char* where) { return cuda_status(e, where); }
+long long spin_limit_cycles() { return kSpinLimitCycles; }
+int default_compute_threads(uint32_t max_cells) { return max_cells <= 12 ? 192 : max_cells <= 24 ? 320 : 512; }
+}  // namespace uww
 
 #pragma GCC visibility push(default)
 extern "C" {

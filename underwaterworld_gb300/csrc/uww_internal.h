@@ -90,6 +90,14 @@ struct BuildArgs {
     long long spin_limit_cycles;     // bound on every device-side wait
 };
 
+// Host helpers shared by the entry points (uww_api.cu).
+int check_params(const uww_params* p);
+void dev_params_from(const uww_params* p, DevParams* d);
+int status_from_cuda(cudaError_t e, const char* where);  // records the CUDA error text
+long long spin_limit_cycles();
+// compute threads per CTA for a batch whose largest chunk has max_cells per edge
+int default_compute_threads(uint32_t max_cells);
+
 // Launch helpers (uww_build.cu).
 size_t build_static_smem_bytes();
 cudaError_t launch_build(const DevParams& p, const BuildArgs& a, bool queue, int grid, int threads,
