@@ -41,12 +41,20 @@ METRIC = "chunks/s (noise+MC, batched vs per-chunk) & fwd+adjoint Mvox/s on 1 GB
 UNIT = "chunks/s"
 N_SEEDS = 10
 
-# Algorithmic FP32 work of the noise stage, counted on the reference
-# formulation (one flop per add/sub/mul/div/floor):
+# Algorithmic FP32 work, counted on the parity kernel's formulation (one flop
+# per add/sub/mul/div/floor, an FMA as 2), independent of how the fast kernel
+# factors it:
 FLOPS_PER_OCTAVE = 83          # one Perlin evaluation + fBm accumulate
 FLOPS_PER_SAMPLE_EXTRA = 16    # world coordinates, normalisation, linear bias
 FLOPS_PER_OCTAVE_GRAD = 254    # Perlin value + analytic gradient + accumulate (normals)
 FLOPS_PER_VERTEX_EXTRA = 60    # interpolation, colour ramp, normalisation
+
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one build_kernel
+# launch on this workload, from an ncu capture of this script's own step
+# (--steps 5 --warmup 3 --quick --no-cpu, launches 5 and 6: 710.1 KB, 715.3 KB).
+# The outputs stay in L2 (write-back) when the kernel ends, so this is below
+# the algorithmic output bytes.
+NCU_DRAM_BYTES_PER_LAUNCH = 712_700
 
 
 def parse():
@@ -370,6 +378,15 @@ def main():
     flops = samples * (oct_ * FLOPS_PER_OCTAVE + FLOPS_PER_SAMPLE_EXTRA) + \
         mean_v * (oct_ * FLOPS_PER_OCTAVE_GRAD + FLOPS_PER_VERTEX_EXTRA)
     achieved = flops / (t_total / args.steps) / 1e12
+    # algorithmic bytes of the mesh emission: VertColor + normal per vertex, u32
+    # per index, the record per chunk written; the descriptor per chunk read
+    out_bytes = mean_v * (24 + 12) + mean_i * 4 + n * (32 + 32)
+    hbm_peak, hbm_src = 6800.0, "fallback"
+    try:
+        hbm_peak = float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["hbm_gbs"])
+        hbm_src = "measured (copy bandwidth)"
+    except (OSError, ValueError, KeyError):
+        pass
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -387,9 +404,14 @@ def main():
         "gpu_launches": args.steps,
         "clocks": clk,
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
-                     "frac": achieved / fp32_peak, "traffic": None,
-                     "peak_source": "measured live: FMA probe kernel (uww_probe_fma), 152x8 CTAs",
-                     "flops_per_step": flops},
+                     "frac": achieved / fp32_peak, "traffic": NCU_DRAM_BYTES_PER_LAUNCH,
+                     "peak_source": "measured live: FMA probe kernel (uww_probe_fma), 152x8 CTAs "
+                                    "(no FP32 entry in the measured-peaks file)",
+                     "flops_per_step": flops,
+                     "emission": {"bound": "hbm", "achieved": out_bytes / (t_total / args.steps) / 1e9,
+                                  "peak": hbm_peak, "unit": "GB/s",
+                                  "frac": out_bytes / (t_total / args.steps) / 1e9 / hbm_peak,
+                                  "bytes_per_step": out_bytes, "peak_source": hbm_src}},
     }
     line.update({k: v for k, v in extra.items() if k != "e2e"})
     if "e2e" in extra:
@@ -398,10 +420,11 @@ def main():
         line["batched_over_plain"] = value / world / extra["plain_chunks_per_s"]
 
     if rank == 0 and not args.no_cpu and not args.quick:
-        cv, cn, cel = cpu_reference(descs, [0], 1, budget_s=30.0)
+        cv, cn, cel = cpu_reference(descs, list(range(N_SEEDS)), 1, budget_s=12.0)
         line["cpu_baseline"] = {"value": cv, "unit": UNIT, "cores": 1, "kind": "port",
-                                "sample": f"{cn} chunks (full seed-0 grid) in {cel:.1f} s, oracle f64 reference "
-                                          f"semantics with linear dedup search, 1 thread, CPU: {cpu_model()}"}
+                                "sample": f"{cn} chunks ({cn // n} full 4096-chunk grids, seeds 0..) in {cel:.1f} s, "
+                                          f"oracle f64 reference semantics with linear dedup search, 1 thread, "
+                                          f"CPU: {cpu_model()}"}
     if rank == 0:
         print(json.dumps(line))
     ctx.close()
