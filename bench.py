@@ -68,6 +68,8 @@ def parse():
     ap.add_argument("--quick", action="store_true", help="skip plain/exact/e2e legs (profiling runs)")
     ap.add_argument("--threads", type=int, default=0, help="threads per CTA (0: tuned/automatic)")
     ap.add_argument("--bps", type=int, default=0, help="resident CTAs per SM (0: tuned/automatic)")
+    ap.add_argument("--no-fit", action="store_true", help="skip the terrain-fitting leg")
+    ap.add_argument("--fit-steps", type=int, default=200, help="Adam steps of the terrain-fitting leg")
     return ap.parse_args()
 
 
@@ -185,6 +187,147 @@ def run_reference(args):
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
+
+
+def timed(stream, fn, flush=None):
+    """Device time of fn() on stream, in seconds (L2 flushed first if given)."""
+    import torch
+    if flush is not None:
+        flush.zero_()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    fn()
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1) * 1e-3
+
+
+def leg_frame_graph(ctx, params, descs, steps, warmup):
+    """Uniform grid as a per-frame CUDA graph: descriptor + count upload, build,
+    record + totals download, one graph launch per frame; host wall time."""
+    from underwaterworld_gb300.frame import FrameBuilder
+    n = len(descs)
+    ctx.set_params(params)
+    fb = FrameBuilder(ctx, n, 12, 1 << 20, 1 << 22)
+    for _ in range(warmup):
+        fb.build(descs)
+    t = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        fb.build(descs)
+        t.append(time.perf_counter() - t0)
+    fb.close()
+    return {"chunks_per_s": n / statistics.median(t), "ms_per_frame": 1e3 * statistics.median(t),
+            "h2d_bytes_per_frame": n * 32 + 4, "d2h_bytes_per_frame": n * 32 + 32,
+            "note": "uww_frame_launch + sync, host wall clock, median"}
+
+
+def leg_mixed_lod(stream, flush, steps, warmup):
+    """Uneven LOD batch (2048 chunks, 12^3/24^3/48^3 at 50/35/15 %, 6-octave fBm)
+    in one persistent launch, autotuned (cached per config); p50/p99 latency."""
+    import torch
+    from underwaterworld_gb300 import abi, workloads
+    from underwaterworld_gb300.chunk import Context
+    from underwaterworld_gb300.frame import autotune
+    p, d = workloads.mixed_lod(seed=0, outputs=abi.UWW_OUT_COLOR | abi.UWW_OUT_NORMALS)
+    p.math_mode = abi.UWW_MATH_FAST
+    n = len(d)
+    ctx = Context(p, stream=stream.cuda_stream)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    vcap, icap = 1 << 23, 1 << 25
+    bufs = {k: torch.empty(b, dtype=torch.uint8, device=dev) for k, b in
+            (("v", vcap * 24), ("nrm", vcap * 12), ("i", icap * 4), ("r", n * 32), ("t", 32))}
+    d_desc = torch.from_numpy(d.view(np.uint8).copy()).to(dev)
+    out = abi.MeshOut(bufs["v"].data_ptr(), bufs["nrm"].data_ptr(), bufs["i"].data_ptr(), None, None,
+                      bufs["r"].data_ptr(), bufs["t"].data_ptr(), vcap, icap, 0, 0)
+    cache = ROOT / "underwaterworld_gb300" / "_build" / "tune_cache.txt"
+    tun, tuned_us = autotune(ctx, d_desc.data_ptr(), n, 48, out, str(cache))
+    L = abi.lib()
+
+    def step():
+        abi.check(L.uww_build_chunks(ctx.h, C.c_void_p(d_desc.data_ptr()), n, 48, C.byref(out)), "mixed build")
+
+    for _ in range(warmup):
+        step()
+    lat = [timed(stream, step, flush) for _ in range(steps)]
+    tot = bufs["t"].view(torch.int64).cpu().numpy()
+    assert int(tot[2]) == 0 and int(tot[3]) == 0, tot
+    cells = int((d["cells"].astype(np.int64) ** 3).sum())
+    samples = int(((d["cells"].astype(np.int64) + 1) ** 3).sum())
+    ctx.close()
+    lat_ms = np.array(lat) * 1e3
+    mean = float(np.mean(lat))
+    return {"chunks": n, "cells": cells, "samples": samples, "chunks_per_s": n / mean,
+            "mvoxels_per_s": cells / mean / 1e6, "p50_ms": float(np.percentile(lat_ms, 50)),
+            "p99_ms": float(np.percentile(lat_ms, 99)), "steps": steps,
+            "tuning": {"threads": tun.threads, "blocks_per_sm": tun.blocks_per_sm, "smem_cells": tun.smem_cells,
+                       "tuned_us": tuned_us},
+            "verts": int(tot[0]), "inds": int(tot[1])}
+
+
+def leg_adjoint(stream, flush, steps, warmup):
+    """Adjoint batch: 512 chunks of 24^3 cells, 4-octave fBm; forward (build +
+    edge ids) then backward (dL/dtheta, dL/dsamples) with seeded cotangents."""
+    from underwaterworld_gb300 import abi, workloads
+    from underwaterworld_gb300.adjoint import Adjoint
+    from underwaterworld_gb300.chunk import Context
+    p, d = workloads.adjoint_batch(seed=0)
+    p.math_mode = abi.UWW_MATH_FAST
+    ctx = Context(p, stream=stream.cuda_stream)
+    a = Adjoint(ctx, d, 1 << 21, 1 << 23, sample_grad=True)
+    a.forward()
+    f = a.fetch_forward()
+    a.set_pos_grad(workloads.cotangents(f["records"], f["edge_ids"], seed=0))
+
+    def fb():
+        a.forward()
+        a.backward()
+
+    for _ in range(warmup):
+        fb()
+    tf = [timed(stream, a.forward, flush) for _ in range(steps)]
+    tb = [timed(stream, a.backward, flush) for _ in range(steps)]
+    tfb = [timed(stream, fb, flush) for _ in range(steps)]
+    g = a.theta_grad()
+    cells = len(d) * 24 ** 3
+    ctx.close()
+    m = statistics.mean(tfb)
+    return {"chunks": len(d), "cells": cells, "verts": int(f["totals"][0]),
+            "fwd_ms": 1e3 * statistics.mean(tf), "bwd_ms": 1e3 * statistics.mean(tb), "fwd_bwd_ms": 1e3 * m,
+            "fwd_adjoint_mvoxels_per_s": cells / m / 1e6, "theta_grad_finite": bool(np.all(np.isfinite(g)))}
+
+
+def leg_terrain_fit(stream, steps=200):
+    """Terrain fitting: 512^3 cells as 32^3 chunks of 16^3, 8-octave fBm; Adam
+    (lr 1e-2) on theta for `steps` steps toward an 8-Gaussian heightmap."""
+    import torch
+    from underwaterworld_gb300.adjoint import TerrainFit, gaussian_heightmap, terrain_volume
+    from underwaterworld_gb300.chunk import Context
+    p, d = terrain_volume(chunks_per_edge=32, cells=16, octaves=8, seed=0)
+    free0, total = torch.cuda.mem_get_info()
+    ctx = Context(p, stream=stream.cuda_stream)
+    target = gaussian_heightmap(16, 32.0, n_bumps=8, seed=0, base=128.0)
+    fit = TerrainFit(ctx, d, target, 32.0, vert_capacity=1 << 23, ind_capacity=1 << 25, lr=1e-2)
+    min_free = torch.cuda.mem_get_info()[0]
+    losses, t0 = [], time.perf_counter()
+    for _ in range(steps):
+        loss, _ = fit.step()
+        losses.append(loss)
+        min_free = min(min_free, torch.cuda.mem_get_info()[0])
+    el = time.perf_counter() - t0
+    # device time of one forward+backward at the final theta
+    def fb():
+        fit.adj.forward()
+        fit.adj.backward()
+    fb()
+    tfb = statistics.mean([timed(stream, fb) for _ in range(5)])
+    cells = len(d) * 16 ** 3
+    rmse0, rmse1 = float(np.sqrt(losses[0])), float(np.sqrt(losses[-1]))
+    ctx.close()
+    return {"cells": cells, "steps": steps, "seconds": el, "step_ms": 1e3 * el / steps,
+            "fwd_bwd_ms": 1e3 * tfb, "fwd_adjoint_mvoxels_per_s": cells / tfb / 1e6,
+            "loss_first": losses[0], "loss_last": losses[-1], "rms_height_error_first": rmse0,
+            "rms_height_error_last": rmse1, "peak_device_bytes": int(free0 - min_free)}
 
 
 def main():
@@ -356,6 +499,13 @@ def main():
         extra["e2e"] = {"value": world * n / statistics.mean(e2e_t), "unit": UNIT,
                         "h2d_bytes_per_step": h2d // k, "d2h_bytes_per_step": d2h // k}
 
+    if not args.quick:
+        extra["frame_graph"] = leg_frame_graph(ctx, params[0], descs, max(5, min(args.steps, 50)), 3)
+        extra["mixed_lod"] = leg_mixed_lod(stream, flush, max(10, min(args.steps, 200)), 3)
+        extra["adjoint"] = leg_adjoint(stream, flush, max(5, min(args.steps, 50)), 3)
+        if not args.no_fit:
+            extra["terrain_fit"] = leg_terrain_fit(stream, args.fit_steps)
+
     # ---- FP32 peak probe (roofline denominator) ----
     sink = torch.empty(152 * 8 * 256, dtype=torch.float32, device=dev)
     fl = C.c_double()
@@ -414,6 +564,8 @@ def main():
                                   "bytes_per_step": out_bytes, "peak_source": hbm_src}},
     }
     line.update({k: v for k, v in extra.items() if k != "e2e"})
+    if "adjoint" in extra:
+        line["fwd_adjoint_mvoxels_per_s"] = extra["adjoint"]["fwd_adjoint_mvoxels_per_s"]
     if "e2e" in extra:
         line["e2e"] = extra["e2e"]
     if "plain_chunks_per_s" in extra:

@@ -25,7 +25,7 @@
 extern "C" {
 #endif
 
-#define UWW_ABI_VERSION 1
+#define UWW_ABI_VERSION 2
 
 /* ---- status codes --------------------------------------------------------- */
 #define UWW_OK               0
@@ -224,6 +224,79 @@ typedef struct uww_tuning {
 } uww_tuning;
 int uww_ctx_set_tuning(uww_ctx* ctx, const uww_tuning* t);
 int uww_ctx_get_tuning(const uww_ctx* ctx, uww_tuning* t);
+
+/* Autotuner (no counterpart in the reference, whose chunk build has no launch
+ * shape): times the batched build of these chunks under each candidate tuning
+ * -- compute threads per CTA (64..192, and 256..512 when chunks exceed 12
+ * cells per edge), CTAs per SM up to the occupancy limit, and the LOD above
+ * which chunks work in a global scratch slot instead of shared memory --
+ * keeps the fastest, sets it on the context and returns it (*best_us: its
+ * time in microseconds).  With cache_path, the result is first looked up in
+ * and then appended to that text file, one line per key; the key is the
+ * device, the batch size (power of two), the LOD histogram (5 % steps) and
+ * the parameters that change the kernel's cost (octaves, outputs, math and
+ * dedup modes, normalisation, bias).  Synchronises the context stream; the
+ * outputs hold the last timed build.  UWW_ERR_CAPACITY if they overflow. */
+int uww_autotune(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint32_t max_cells,
+                 const uww_mesh_out* out, const char* cache_path, uww_tuning* best, float* best_us);
+
+/* ---- per-frame build as a CUDA graph -------------------------------------------- */
+/* Replaces World::build_step's per-frame slice of chunk builds (world.rs:113-145)
+ * with one graph launch: copy h_chunks[0..max_chunks) and *h_count (page-locked
+ * host memory the caller fills each frame) to the device, run the batched
+ * build over the first *h_count descriptors (the kernel reads the count on
+ * the device), and copy the records (if h_records) and totals (if h_totals,
+ * page-locked) back.  The mesh stays in d_out's device buffers.  The graph is
+ * captured once, on the context stream, with the context's parameters;
+ * uww_frame_set_params recaptures it and updates the instantiated graph. */
+typedef struct uww_frame uww_frame;
+int uww_frame_create(uww_ctx* ctx, uint32_t max_chunks, uint32_t max_cells, const uww_chunk_desc* h_chunks,
+                     const uint32_t* h_count, const uww_mesh_out* d_out, uww_chunk_record* h_records,
+                     uint64_t* h_totals, uww_frame** out);
+int uww_frame_launch(uww_frame* f);          /* asynchronous; then uww_ctx_sync */
+int uww_frame_set_params(uww_frame* f, const uww_params* p);
+int uww_frame_destroy(uww_frame* f);
+
+/* ---- topology-frozen adjoint (no counterpart in the reference) ---------------- */
+/* theta = (a_0 .. a_{K-1}, base_freq, offset[0], offset[1], offset[2], iso_level),
+ * K = params.octaves, UWW_THETA_COUNT(K) floats.  a_k are the effective
+ * per-octave amplitudes (amps[k] with explicit_amps, else amplitude * persistence^k). */
+#define UWW_THETA_COUNT(octaves) ((octaves) + 5)
+
+/* Edge id of a vertex: (s << 3) | dir, s = the chunk-local index (x*S + y)*S + z
+ * (S = cells + 1) of the sample the vertex is interpolated from (t = 0 there),
+ * dir = 0..5 the direction (+x, -x, +y, -y, +z, -z) of the other sample. */
+#define UWW_EDGE_SAMPLE(id) ((id) >> 3)
+#define UWW_EDGE_DIR(id)    ((id) & 7u)
+
+/* Forward: uww_build_chunks plus d_edge_ids[v] for every output vertex v (indexed
+ * like out->verts; out->vert_capacity entries).  With the per-cell cases
+ * (UWW_OUT_CASES) this is all the backward keeps: the field is not stored. */
+int uww_forward(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint32_t max_cells,
+                const uww_mesh_out* out, uint32_t* d_edge_ids);
+
+/* Backward of a loss L(vertex positions) with the topology of the forward held
+ * fixed.  d_pos_grad = dL/d(position), 3 floats per vertex indexed like the
+ * forward's verts; d_records and d_edge_ids are the forward's.  Writes
+ * d_theta_grad[UWW_THETA_COUNT(octaves)] = dL/dtheta and, if d_sample_grad is
+ * not NULL, dL/d(density sample) at desc.sample_offset (the array is zeroed
+ * over sample_capacity floats first).  The density and its analytic spatial
+ * and parameter derivatives are recomputed at each vertex's two samples.  The
+ * context's parameters must be the forward's.  An edge id outside its chunk
+ * makes every theta_grad entry NaN.  Asynchronous. */
+int uww_backward(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint32_t max_cells,
+                 const uww_chunk_record* d_records, const uint32_t* d_edge_ids, const float* d_pos_grad,
+                 float* d_theta_grad, float* d_sample_grad, uint64_t sample_capacity);
+
+/* Heightmap loss of the terrain-fitting loop: vertices (count from d_totals[0])
+ * are binned into square xy columns of `column` world units starting at
+ * (x0, y0), cols_x by cols_y; L = sum over columns holding a vertex of
+ * (mean vertex z - d_target[col])^2 / (cols_x * cols_y), col = cy * cols_x + cx.
+ * Writes *d_loss and d_pos_grad = dL/d(position) (3 floats per vertex);
+ * d_work: 2 * cols_x * cols_y floats of scratch.  Asynchronous. */
+int uww_height_loss(uww_ctx* ctx, const uww_vert_color* d_verts, const uint64_t* d_totals, uint32_t vert_capacity,
+                    float x0, float y0, float column, uint32_t cols_x, uint32_t cols_y, const float* d_target,
+                    float* d_work, float* d_pos_grad, float* d_loss);
 
 /* ---- memory helpers for callers without their own CUDA binding --------------- */
 int uww_device_alloc(size_t bytes, void** out);

@@ -49,6 +49,8 @@ def lib():
         L.oracle_density_at.restype = C.c_int
         L.oracle_perlin.argtypes = [C.c_uint32, C.c_int, P, C.c_uint32, P]
         L.oracle_perlin.restype = C.c_int
+        L.oracle_adjoint64.argtypes = [C.POINTER(abi.Params), P, P, C.c_uint32, P, P, P, P, P, P, P, P, P, P]
+        L.oracle_adjoint64.restype = C.c_int
         _lib = L
     return _lib
 
@@ -119,3 +121,106 @@ def perlin(seed: int, xyz: np.ndarray, precision: int = F64) -> np.ndarray:
     lib().oracle_perlin(seed, precision, xyz.ctypes.data_as(C.c_void_p), xyz.shape[0],
                         out.ctypes.data_as(C.c_void_p))
     return out
+
+
+# ---- topology-frozen adjoint (FP64 reference) ---------------------------------
+def theta_of(params: abi.Params) -> np.ndarray:
+    """theta = (effective per-octave amplitudes, base_freq, offset xyz, iso) in f64."""
+    K = int(params.octaves)
+    amps, a = [], np.float32(params.amplitude)
+    for k in range(K):
+        amps.append(float(params.amps[k]) if params.explicit_amps else float(a))
+        a = np.float32(a * np.float32(params.persistence))
+    return np.array(amps + [params.base_freq, *params.offset, params.iso_level], dtype=np.float64)
+
+
+def adjoint64(params: abi.Params, descs: np.ndarray, records: np.ndarray, edge_ids: np.ndarray,
+              pos_grad: np.ndarray, theta: np.ndarray | None = None, samples_in: np.ndarray | None = None,
+              want_theta: bool = True, want_samples: bool = False, want_positions: bool = False,
+              want_dmax: bool = False, want_pole: bool = False) -> dict:
+    """FP64 loss sum_v pos_grad[v] . p_v over the given edges, and its gradients."""
+    descs = np.ascontiguousarray(descs, dtype=abi.CHUNK_DESC_DTYPE)
+    records = np.ascontiguousarray(records, dtype=abi.CHUNK_RECORD_DTYPE)
+    edge_ids = np.ascontiguousarray(edge_ids, dtype=np.uint32)
+    pos_grad = np.ascontiguousarray(pos_grad, dtype=np.float32).reshape(-1, 3)
+    K = int(params.octaves)
+    th = np.ascontiguousarray(theta, dtype=np.float64) if theta is not None else None
+    sin = np.ascontiguousarray(samples_in, dtype=np.float64) if samples_in is not None else None
+    loss = C.c_double()
+    tg = np.zeros(K + 5) if want_theta else None
+    sg = np.zeros(total_samples(descs)) if want_samples else None
+    pos = np.zeros((edge_ids.size, 3)) if want_positions else None
+    dmax = np.zeros(K + 5) if want_dmax else None
+    pole = np.zeros(K + 5) if want_pole else None
+
+    def ptr(a):
+        return a.ctypes.data if a is not None else None
+
+    st = lib().oracle_adjoint64(C.byref(params), ptr(th), descs.ctypes.data, descs.shape[0], records.ctypes.data,
+                                edge_ids.ctypes.data, pos_grad.ctypes.data, ptr(sin), C.byref(loss), ptr(tg),
+                                ptr(sg), ptr(pos), ptr(dmax), ptr(pole))
+    if st:
+        raise RuntimeError(f"oracle_adjoint64 failed: {st}")
+    return {"loss": loss.value, "theta_grad": tg, "sample_grad": sg, "positions": pos, "dmax": dmax, "pole": pole}
+
+
+def fd_theta(params: abi.Params, descs, records, edge_ids, pos_grad, h: float = 1e-4, theta=None,
+             richardson: bool = False, pole_frac: float = 0.02) -> tuple:
+    """FP64 central differences of the loss in theta.  The step of parameter i
+    is h in units of its effect on the density: h / max|d rho/d theta_i| over
+    the samples the vertices use (so no sample moves by more than h; for the
+    iso level and amplitudes that is about h itself), and at most pole_frac of
+    the distance in theta_i to the nearest degenerate edge (where t has a
+    pole: the loss is rational in each theta_i, and a stencil wider than the
+    pole distance differentiates across the pole).  With richardson, the
+    central differences at h and h/2 are combined to cancel the h^2 error term.
+    Returns (fd, steps)."""
+    th = theta_of(params) if theta is None else np.asarray(theta, np.float64)
+    r = adjoint64(params, descs, records, edge_ids, pos_grad, theta=th, want_theta=False, want_dmax=True,
+                  want_pole=True)
+    steps = np.minimum(h / np.maximum(r["dmax"], 1.0), pole_frac * r["pole"])
+
+    def central(i, s):
+        tp, tm = th.copy(), th.copy()
+        tp[i] += s
+        tm[i] -= s
+        lp = adjoint64(params, descs, records, edge_ids, pos_grad, theta=tp, want_theta=False)["loss"]
+        lm = adjoint64(params, descs, records, edge_ids, pos_grad, theta=tm, want_theta=False)["loss"]
+        return (lp - lm) / (2 * s)
+
+    fd = np.zeros_like(th)
+    for i in range(th.size):
+        fd[i] = central(i, steps[i])
+        if richardson:  # (4 D(h/2) - D(h)) / 3 cancels the h^2 term
+            fd[i] = (4 * central(i, steps[i] / 2) - fd[i]) / 3
+    return fd, steps
+
+
+def crossing_edges(params: abi.Params, descs: np.ndarray, samples: np.ndarray):
+    """Every grid edge whose two samples lie on opposite sides of the iso-level
+    (one vertex per edge), as records + edge ids in the forward's encoding:
+    id = (sample index << 3) | dir, from the lower sample in direction +axis."""
+    descs = np.ascontiguousarray(descs, dtype=abi.CHUNK_DESC_DTYPE)
+    iso = np.float32(params.iso_level)
+    recs = np.zeros(descs.shape[0], dtype=abi.CHUNK_RECORD_DTYPE)
+    ids, off = [], 0
+    for i, d in enumerate(descs):
+        S = int(d["cells"]) + 1
+        rho = samples[int(d["sample_offset"]):int(d["sample_offset"]) + S ** 3].reshape(S, S, S)
+        inside = rho < iso
+        idx = np.arange(S ** 3, dtype=np.uint32).reshape(S, S, S)
+        mine = []
+        for axis in range(3):
+            lo = [slice(None)] * 3
+            hi = [slice(None)] * 3
+            lo[axis] = slice(0, S - 1)
+            hi[axis] = slice(1, S)
+            cross = inside[tuple(lo)] != inside[tuple(hi)]
+            mine.append((idx[tuple(lo)][cross] << 3) | np.uint32(2 * axis))
+        e = np.concatenate(mine).astype(np.uint32)
+        recs[i]["num_verts"] = e.size
+        recs[i]["vert_offset"] = off
+        recs[i]["flags"] = abi.UWW_CHUNK_HAS_MESH if e.size else 0
+        ids.append(e)
+        off += e.size
+    return recs, (np.concatenate(ids) if ids else np.zeros(0, np.uint32))

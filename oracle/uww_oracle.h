@@ -26,6 +26,22 @@ int    oracle_sample_grid(const uww_params* p, int precision, const uww_chunk_de
 int    oracle_density_at(const uww_params* p, int precision, const float* xyz, uint32_t n, float* out,
                          float* grad);
 int    oracle_perlin(uint32_t seed, int precision, const double* xyz, uint32_t n, double* out);
+/* FP64 reference of the topology-frozen adjoint (uww_oracle_adjoint.c): loss
+ * L = sum_v pos_grad[v] . p_v over the vertices named by (records, edge_ids),
+ * its dL/dtheta (theta_grad, octaves + 5), dL/d(sample) (sample_grad, added
+ * at desc.sample_offset) and the f64 positions (3 per vertex); any output but
+ * loss may be NULL.  theta (octaves + 5 doubles) overrides the parameters'
+ * amplitudes, frequency, offset and iso level when not NULL; samples_in
+ * (doubles at desc.sample_offset) replaces the noise when not NULL.  dmax
+ * (optional, octaves + 5) receives max |d rho / d theta_i| over the samples
+ * evaluated (1 for the iso level): the scale of each parameter's effect.
+ * pole (optional, octaves + 5) receives min over vertices of |D| / |dD/dtheta_i|,
+ * D = rho_B - rho_A: how far theta_i can move before some edge degenerates
+ * (t has a pole there), which bounds a meaningful finite-difference step. */
+int    oracle_adjoint64(const uww_params* p, const double* theta, const uww_chunk_desc* chunks, uint32_t n,
+                        const uww_chunk_record* records, const uint32_t* edge_ids, const float* pos_grad,
+                        const double* samples_in, double* loss, double* theta_grad, double* sample_grad,
+                        double* positions, double* dmax, double* pole);
 double oracle_density64_full(const uww_params* p, const uint8_t* P, double wx, double wy, double wz,
                              double* grad);
 

@@ -21,7 +21,7 @@ def test_library_exports_every_declared_symbol(built_lib):
 
 
 def test_abi_version_and_status_strings(built_lib):
-    assert abi.lib().uww_abi_version() == 1
+    assert abi.lib().uww_abi_version() == 2
     assert abi.status_string(abi.UWW_ERR_CAPACITY) == "output capacity exceeded"
 
 

@@ -112,7 +112,22 @@ _SIGS = {
     "uww_memset": (C.c_int, [P, P, C.c_int, C.c_size_t]),
     "uww_density_at": (C.c_int, [P, P, C.c_uint32, P]),
     "uww_probe_fma": (C.c_int, [P, C.c_uint32, C.c_uint32, P, C.POINTER(C.c_double)]),
+    "uww_autotune": (C.c_int, [P, P, C.c_uint32, C.c_uint32, C.POINTER(MeshOut), C.c_char_p, C.POINTER(Tuning),
+                               C.POINTER(C.c_float)]),
+    "uww_frame_create": (C.c_int, [P, C.c_uint32, C.c_uint32, P, P, C.POINTER(MeshOut), P, P, C.POINTER(P)]),
+    "uww_frame_launch": (C.c_int, [P]),
+    "uww_frame_set_params": (C.c_int, [P, C.POINTER(Params)]),
+    "uww_frame_destroy": (C.c_int, [P]),
+    "uww_forward": (C.c_int, [P, P, C.c_uint32, C.c_uint32, C.POINTER(MeshOut), P]),
+    "uww_backward": (C.c_int, [P, P, C.c_uint32, C.c_uint32, P, P, P, P, P, C.c_uint64]),
+    "uww_height_loss": (C.c_int, [P, P, P, C.c_uint32, C.c_float, C.c_float, C.c_float, C.c_uint32, C.c_uint32,
+                                  P, P, P, P]),
 }
+
+
+def theta_count(octaves: int) -> int:
+    """UWW_THETA_COUNT: per-octave amplitudes, base frequency, offset xyz, iso level."""
+    return int(octaves) + 5
 
 _lib = None
 

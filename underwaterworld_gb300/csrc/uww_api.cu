@@ -14,42 +14,8 @@
 
 using namespace uww;
 
-struct uww_ctx {
-    uww_params params;
-    DevParams dev;
-    cudaStream_t stream = nullptr;
-    bool own_stream = false;
-    int device = 0;
-    int num_sms = 0;
-    size_t smem_optin = 0;
-    size_t smem_dyn_max = 0;
+// struct uww_ctx is defined in uww_internal.h (shared with the adjoint and tuner).
 
-    // tuning (0 = automatic)
-    int threads = 0;
-    int blocks_per_sm = 0;
-    int smem_cells = 0;
-
-    // device work state
-    unsigned long long* d_lookback = nullptr;
-    size_t lookback_cap = 0;
-    unsigned long long* d_state = nullptr;
-    unsigned int* d_counter = nullptr;
-    unsigned long long* d_acc = nullptr;
-    unsigned long long* d_totals = nullptr;
-    uint8_t* d_scratch = nullptr;
-    size_t scratch_cap = 0;
-
-    // buffers of the host-buffer path
-    uww_chunk_desc* d_chunks = nullptr;
-    size_t chunks_cap = 0;
-    void* d_verts = nullptr;     size_t verts_cap = 0;
-    void* d_normals = nullptr;   size_t normals_cap = 0;
-    void* d_inds = nullptr;      size_t inds_cap = 0;
-    void* d_cases = nullptr;     size_t cases_cap = 0;
-    void* d_samples = nullptr;   size_t samples_cap = 0;
-    void* d_records = nullptr;   size_t records_cap = 0;
-    unsigned long long* h_totals = nullptr;
-};
 
 namespace {
 
@@ -214,7 +180,8 @@ int plan_launch(uww_ctx* ctx, uint32_t n, uint32_t max_cells, bool queue, Launch
 }
 
 int launch(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint32_t max_cells, const uww_mesh_out* out,
-           bool queue, const float* samples_in = nullptr, unsigned long long samples_in_count = 0)
+           bool queue, const float* samples_in = nullptr, unsigned long long samples_in_count = 0,
+           uint32_t* edge_ids = nullptr, const uint32_t* n_dev = nullptr, bool prepare_only = false)
 {
     LaunchCfg cfg;
     int st = plan_launch(ctx, n, max_cells, queue, &cfg);
@@ -223,6 +190,7 @@ int launch(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint32_t ma
         st = ensure_device(&ctx->d_scratch, &ctx->scratch_cap, cfg.scratch_slot * cfg.slots * (size_t)cfg.grid);
         if (st) return st;
     }
+    if (prepare_only && !queue) return UWW_OK;
     BuildArgs a;
     std::memset(&a, 0, sizeof(a));
     a.chunks = d_chunks;
@@ -248,6 +216,8 @@ int launch(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint32_t ma
     a.ztable_offset = cfg.ztable_offset;
     a.smem_cells = cfg.smem_cells;
     a.spin_limit_cycles = kSpinLimitCycles;
+    a.edge_ids = edge_ids;
+    a.n_dev = n_dev;
     if (queue) {
         // The look-back words, ticket counter and accumulators are zero when a
         // launch starts: zeroed once here on (re)allocation, and reset by the
@@ -263,6 +233,7 @@ int launch(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint32_t ma
         a.work_counter = ctx->d_counter;
         a.acc = ctx->d_acc;
     }
+    if (prepare_only) return UWW_OK;
     return cuda_status(launch_build(ctx->dev, a, queue, cfg.grid, cfg.threads, cfg.dyn_smem, ctx->stream), "build kernel launch");
 }
 
@@ -281,6 +252,27 @@ void dev_params_from(const uww_params* p, DevParams* d) { make_dev_params(p, d);
 int status_from_cuda(cudaError_t e, const char* where) { return cuda_status(e, where); }
 long long spin_limit_cycles() { return kSpinLimitCycles; }
 int default_compute_threads(uint32_t max_cells) { return max_cells <= 12 ? 192 : max_cells <= 24 ? 320 : 512; }
+int ensure_device_bytes(void** ptr, size_t* cap, size_t bytes) { return ensure_device(ptr, cap, bytes); }
+int launch_batched(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint32_t max_cells,
+                   const uww_mesh_out* out, uint32_t* edge_ids, const uint32_t* n_dev)
+{
+    return launch(ctx, d_chunks, n, max_cells, out, true, nullptr, 0, edge_ids, n_dev);
+}
+int check_mesh_out(const uww_mesh_out* out) { return check_out(out); }
+int prepare_batched(uww_ctx* ctx, uint32_t n, uint32_t max_cells, const uww_mesh_out* out)
+{
+    return launch(ctx, nullptr, n, max_cells, out, true, nullptr, 0, nullptr, nullptr, true);
+}
+int plan_batched(uww_ctx* ctx, uint32_t n, uint32_t max_cells, int* threads, int* grid, size_t* dyn_smem)
+{
+    LaunchCfg cfg;
+    const int st = plan_launch(ctx, n, max_cells, true, &cfg);
+    if (st) return st;
+    *threads = cfg.threads;
+    *grid = cfg.grid;
+    *dyn_smem = cfg.dyn_smem;
+    return UWW_OK;
+}
 }  // namespace uww
 
 #pragma GCC visibility push(default)
@@ -412,6 +404,8 @@ int uww_ctx_destroy(uww_ctx* ctx)
     cudaFree(ctx->d_cases);
     cudaFree(ctx->d_samples);
     cudaFree(ctx->d_records);
+    cudaFree(ctx->d_adj_part);
+    cudaFree(ctx->d_adj_counter);
     if (ctx->h_totals) cudaFreeHost(ctx->h_totals);
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;

@@ -122,6 +122,7 @@ struct SmemTables {
     uint32_t overflow;            // chunks of this CTA that did not fit (control warp)
     uint32_t errflags;            // UWW_ERRFLAG_* raised by this CTA
     uint32_t last;                // this CTA is the last of the launch to finish
+    uint32_t n;                   // chunks in this launch (min of the device count and BuildArgs::n)
 };
 
 __device__ __forceinline__ int boundary_flags(int x, int y, int z, int N)
@@ -458,7 +459,7 @@ __device__ __forceinline__ void chunk_record(const BuildArgs& a, SmemTables& T, 
     rec.num_active_cells = nA;
     rec.reserved[0] = rec.reserved[1] = 0;
     a.records[ci.ticket] = rec;
-    if (!queue || ci.ticket == a.n - 1) {
+    if (!queue || ci.ticket == T.n - 1) {
         a.totals[0] = ev + nV;
         a.totals[1] = ei + nI;
     }
@@ -705,6 +706,11 @@ __device__ void chunk_emit(const DevParams& p, const BuildArgs& a, SmemTables& T
                         const float mx = O::add(sax, O::mul(t, O::sub(sbx, sax)));
                         const float my = O::add(say, O::mul(t, O::sub(sby, say)));
                         const float mz = O::add(saz, O::mul(t, O::sub(sbz, saz)));
+                        if (a.edge_ids) {
+                            // direction of corner b from corner a: +x -x +y -y +z -z
+                            const int dir = bx != ax ? (bx < ax) : by != ay ? 2 + (by < ay) : 4 + (bz < az);
+                            a.edge_ids[voff + id] = ((uint32_t)((ax * S + ay) * S + az) << 3) | (uint32_t)dir;
+                        }
                         float2* v2 = reinterpret_cast<float2*>(a.verts + voff + id);
                         v2[0] = make_float2(O::add(mx, (float)ox), O::add(my, (float)oy));
                         // colour slot 0 carries the owner's corner b (the value ramp's
@@ -754,13 +760,13 @@ __device__ void chunk_emit(const DevParams& p, const BuildArgs& a, SmemTables& T
 }
 
 // Control warp: take a ticket from the work queue and stage its descriptor.
-__device__ __forceinline__ void take_ticket(const BuildArgs& a, Ticket& tk)
+__device__ __forceinline__ void take_ticket(const BuildArgs& a, uint32_t n, Ticket& tk)
 {
     const int lane = threadIdx.x & 31;
     uint32_t t = 0;
     if (lane == 0) t = atomicAdd(a.work_counter, 1u);
     t = __shfl_sync(0xffffffffu, t, 0);
-    if (t < a.n && lane < 8)
+    if (t < n && lane < 8)
         reinterpret_cast<uint32_t*>(&tk.desc)[lane] = reinterpret_cast<const uint32_t*>(&a.chunks[t])[lane];
     if (lane == 0) tk.ticket = t;
     __syncwarp();
@@ -796,7 +802,11 @@ __global__ void __launch_bounds__(MAXT, MINB) build_kernel(const DevParams p, co
     for (int i = tid; i < 128; i += nthr) (&T.owned[0][0])[i] = (&UWW_OWNED_MASK[0][0])[i];
     for (int i = tid; i < 12 * 4 * 5; i += nthr) (&T.share[0][0][0])[i] = (&UWW_EDGE_SHARE[0][0][0])[i];
     for (int i = tid; i < 24; i += nthr) (&T.corners[0][0])[i] = (&UWW_EDGE_CORNERS[0][0])[i];
-    if (tid == 0) { T.errflags = 0; T.overflow = 0; }
+    if (tid == 0) {
+        T.errflags = 0;
+        T.overflow = 0;
+        T.n = a.n_dev ? min(*a.n_dev, a.n) : a.n;
+    }
     __syncthreads();
 
     if (!QUEUE) {
@@ -815,10 +825,10 @@ __global__ void __launch_bounds__(MAXT, MINB) build_kernel(const DevParams p, co
 
     if (tid >= ncomp) {
         // ---- control warp ----
-        take_ticket(a, T.tk[0]);
+        take_ticket(a, T.n, T.tk[0]);
         for (int i = 0;; ++i) {
             bar_sync(kBarTicket, nthr);  // ticket i staged; chunk i-1's counts visible
-            const bool valid = T.tk[i & 1].ticket < a.n;
+            const bool valid = T.tk[i & 1].ticket < T.n;
             // the look-back of chunk i-1 waits until chunk i's noise is done, so
             // its predecessors have had a whole noise phase to publish
             if (valid) bar_sync(kBarNoiseDone, nthr);
@@ -834,14 +844,14 @@ __global__ void __launch_bounds__(MAXT, MINB) build_kernel(const DevParams p, co
             // that follow it in the queue do not wait on a late aggregate
             if (!valid) break;
             if (i > 0) bar_sync(kBarEmitDone, nthr);
-            take_ticket(a, T.tk[(i + 1) & 1]);
+            take_ticket(a, T.n, T.tk[(i + 1) & 1]);
         }
     } else {
         // ---- compute warps ----
         for (int i = 0;; ++i) {
             bar_sync(kBarTicket, nthr);
             const Ticket tk = T.tk[i & 1];
-            const bool valid = tk.ticket < a.n;
+            const bool valid = tk.ticket < T.n;
             if (valid) chunk_front<O, QUEUE>(p, a, T, dyn_smem, tk.desc, tk.ticket, i & 1, ncomp, nthr);
             bar_sync(kBarCompute, ncomp);
             if (i > 0) {
@@ -866,8 +876,9 @@ __global__ void __launch_bounds__(MAXT, MINB) build_kernel(const DevParams p, co
     __syncthreads();
     if (T.last) {
         __threadfence();
-        for (uint32_t i = tid; i < a.n; i += nthr) a.lookback[i] = 0ull;
+        for (uint32_t i = tid; i < T.n; i += nthr) a.lookback[i] = 0ull;
         if (tid == 0) {
+            if (T.n == 0) { a.totals[0] = 0ull; a.totals[1] = 0ull; }
             a.totals[2] = atomicExch(&a.acc[0], 0ull);
             a.totals[3] = atomicExch(&a.acc[1], 0ull);
             atomicExch(&a.acc[2], 0ull);

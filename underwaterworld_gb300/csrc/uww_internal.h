@@ -88,6 +88,8 @@ struct BuildArgs {
     size_t ztable_offset;            // fast build: per-chunk z tables, after the workspaces
     uint32_t smem_cells;             // chunks with cells <= smem_cells work in shared memory
     long long spin_limit_cycles;     // bound on every device-side wait
+    uint32_t* edge_ids;              // optional, per output vertex: (first corner sample << 3) | direction
+    const uint32_t* n_dev;           // optional device chunk count; the launch builds min(*n_dev, n)
 };
 
 // Host helpers shared by the entry points (uww_api.cu).
@@ -107,4 +109,64 @@ cudaError_t prepare_build_kernels(size_t optin, size_t* max_dyn_smem);
 cudaError_t launch_density(const DevParams& p, const float* xyz, uint32_t n, float* out, cudaStream_t s);
 cudaError_t launch_fma_probe(int blocks, uint32_t iters, float* sink, cudaStream_t s);
 
+// Batched build on the context (uww_api.cu); edge_ids and n_dev as in BuildArgs.
+int launch_batched(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint32_t max_cells,
+                   const uww_mesh_out* out, uint32_t* edge_ids, const uint32_t* n_dev);
+int check_mesh_out(const uww_mesh_out* out);
+// allocate what a batched build of n chunks needs, without launching (so that
+// a later launch can be captured into a CUDA graph)
+int prepare_batched(uww_ctx* ctx, uint32_t n, uint32_t max_cells, const uww_mesh_out* out);
+// the launch shape a batched build of n chunks would use
+int plan_batched(uww_ctx* ctx, uint32_t n, uint32_t max_cells, int* threads, int* grid, size_t* dyn_smem);
+// (re)allocate *ptr to at least `bytes` of device memory (contents not kept)
+int ensure_device_bytes(void** ptr, size_t* cap, size_t bytes);
+template <class T>
+int ensure_device_of(T** ptr, size_t* cap, size_t bytes)
+{
+    return ensure_device_bytes(reinterpret_cast<void**>(ptr), cap, bytes);
+}
+
 }  // namespace uww
+
+// The context behind the opaque uww_ctx handle.
+struct uww_ctx {
+    uww_params params;
+    uww::DevParams dev;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int device = 0;
+    int num_sms = 0;
+    size_t smem_optin = 0;
+    size_t smem_dyn_max = 0;
+
+    // tuning (0 = automatic)
+    int threads = 0;
+    int blocks_per_sm = 0;
+    int smem_cells = 0;
+
+    // device work state
+    unsigned long long* d_lookback = nullptr;
+    size_t lookback_cap = 0;
+    unsigned long long* d_state = nullptr;
+    unsigned int* d_counter = nullptr;
+    unsigned long long* d_acc = nullptr;
+    unsigned long long* d_totals = nullptr;
+    uint8_t* d_scratch = nullptr;
+    size_t scratch_cap = 0;
+
+    // buffers of the host-buffer path
+    uww_chunk_desc* d_chunks = nullptr;
+    size_t chunks_cap = 0;
+    void* d_verts = nullptr;     size_t verts_cap = 0;
+    void* d_normals = nullptr;   size_t normals_cap = 0;
+    void* d_inds = nullptr;      size_t inds_cap = 0;
+    void* d_cases = nullptr;     size_t cases_cap = 0;
+    void* d_samples = nullptr;   size_t samples_cap = 0;
+    void* d_records = nullptr;   size_t records_cap = 0;
+    unsigned long long* h_totals = nullptr;
+
+    // adjoint: per-chunk dL/dtheta partials and the arrival counter of the
+    // backward's final reduction (zero between launches)
+    float* d_adj_part = nullptr;     size_t adj_part_cap = 0;
+    unsigned int* d_adj_counter = nullptr;
+};

@@ -11,6 +11,10 @@
   {12: 50%, 24: 35%, 48: 15%}, positions drawn without replacement from a
   64x64x16-chunk region (z from -8 to 7, so the surface near z = 0 lies
   inside it); 6-octave fBm (frequency 0.03) plus 0.02 * z; iso-level 0.
+* ``adjoint_batch``   -- 8x8x8 = 512 chunks of 24^3 cells across the surface
+  of the uniform grid's density (x, y 0..7, z 4..11), 4-octave fBm, for the
+  adjoint check; ``cotangents`` gives its per-vertex dL/dp ~ N(0, I3) seeded
+  by (chunk id, edge id).
 """
 from __future__ import annotations
 
@@ -63,3 +67,38 @@ def mixed_lod(seed: int = 0, n: int = 2048, outputs: int = abi.UWW_OUT_COLOR):
     pos = np.stack([flat // (64 * 16) - 32, (flat // 16) % 64 - 32, flat % 16 - 8], -1)
     cells = rng.choice(np.array([12, 24, 48]), size=n, p=[0.5, 0.35, 0.15])
     return p, make_descs(pos, cells)
+
+
+def adjoint_batch(seed: int = 0, side: int = 8, cells: int = 24, outputs: int = abi.UWW_OUT_CASES):
+    p = fbm_params(seed, 4, 0.04, -0.03, 128.0, 0.0, outputs)
+    g = np.arange(side)
+    pos = np.stack(np.meshgrid(g, g, g + 8 - side // 2, indexing="ij"), -1).reshape(-1, 3)
+    return p, make_descs(pos, cells)
+
+
+def _splitmix64(x: np.ndarray) -> np.ndarray:
+    x = (x + np.uint64(0x9E3779B97F4A7C15)) & np.uint64(0xFFFFFFFFFFFFFFFF)
+    z = x
+    z = ((z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)) & np.uint64(0xFFFFFFFFFFFFFFFF)
+    z = ((z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)) & np.uint64(0xFFFFFFFFFFFFFFFF)
+    return z ^ (z >> np.uint64(31))
+
+
+def cotangents(records: np.ndarray, edge_ids: np.ndarray, seed: int = 0) -> np.ndarray:
+    """Per-vertex cotangents c_v ~ N(0, I3), a function of (seed, chunk id, edge
+    id) only: splitmix64 counters, Box-Muller.  Shape (num_verts, 3), f32."""
+    nv = edge_ids.size
+    chunk = np.zeros(nv, dtype=np.uint64)
+    for i, r in enumerate(records):
+        o, n = int(r["vert_offset"]), int(r["num_verts"])
+        if n and not (int(r["flags"]) & abi.UWW_CHUNK_OVERFLOW):
+            chunk[o:o + n] = i
+    with np.errstate(over="ignore"):
+        key = (np.uint64(seed) << np.uint64(56)) ^ (chunk << np.uint64(32)) ^ edge_ids.astype(np.uint64)
+        u = []
+        for j in range(4):
+            h = _splitmix64(key * np.uint64(4) + np.uint64(j))
+            u.append(((h >> np.uint64(11)).astype(np.float64) + 0.5) / float(1 << 53))
+    r0, r1 = np.sqrt(-2 * np.log(u[0])), np.sqrt(-2 * np.log(u[2]))
+    c = np.stack([r0 * np.cos(2 * np.pi * u[1]), r0 * np.sin(2 * np.pi * u[1]), r1 * np.cos(2 * np.pi * u[3])], 1)
+    return c.astype(np.float32)
