@@ -72,3 +72,23 @@ def test_edge_share_table():
         assert seen_self
         keys = [tuple(s[:3]) for s in share[e]]
         assert keys == sorted(keys), "candidates must be in cell order"
+
+
+def test_edge_before_is_first_reference_order():
+    """UWW_EDGE_BEFORE[c][e] = edges first referenced before e's first reference,
+    so popcount(owned & before) is the rank of e's vertex among a cell's new ones."""
+    _, tri, ntri, emask, _ = tables()
+    before = np.array(_array("UWW_EDGE_BEFORE"), dtype=int).reshape(256, 12)
+    rng = np.random.default_rng(0)
+    for c in range(256):
+        row = [int(v) for v in tri[c][:3 * ntri[c]]]
+        order = list(dict.fromkeys(row))
+        for e in range(12):
+            want = sum(1 << f for f in order[:order.index(e)]) if e in order else 0
+            assert before[c][e] == want, (c, e)
+        # rank of an edge among owned edges == position among owned first references
+        for _ in range(4):
+            owned = int(rng.integers(0, 1 << 12))
+            seen = [e for e in order if owned >> e & 1]
+            for k, e in enumerate(seen):
+                assert bin(owned & before[c][e]).count("1") == k

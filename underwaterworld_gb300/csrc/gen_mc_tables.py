@@ -7,7 +7,11 @@ instead of being typed in, so the CUDA kernels and the CPU oracle use exactly
 the rows the reference walks.  Two derived tables are added:
 
 * ``UWW_CASE_NTRI[256]``  -- triangles per case (row length before -1, / 3);
-* ``UWW_CASE_EDGES[256]`` -- 12-bit mask of the edges a case's row references.
+* ``UWW_CASE_EDGES[256]`` -- 12-bit mask of the edges a case's row references;
+* ``UWW_EDGE_BEFORE[256][12]`` -- per case and edge, the mask of the edges the
+  row references for the first time before edge e's first reference, so a
+  cell's k-th new vertex (in first-reference order) has rank
+  popcount(owned & before[case][e]).
 
 Usage: ``python gen_mc_tables.py <path to marching_table.rs> [out.h]``.
 The generated header is committed; this script only runs when the tables
@@ -28,6 +32,23 @@ def parse(src: str):
     assert len(edges) == 12 and all(len(e) == 2 for e in edges)
     assert len(rows) == 256 and all(len(r) == 16 for r in rows)
     return edges, rows
+
+
+def first_before(rows):
+    out = []
+    for r in rows:
+        order = []
+        for e in r:
+            if e < 0:
+                break
+            if e not in order:
+                order.append(e)
+        masks = [0] * 12
+        for i, e in enumerate(order):
+            for f in order[:i]:
+                masks[e] |= 1 << f
+        out.append(masks)
+    return out
 
 
 def derive(rows):
@@ -151,6 +172,12 @@ def emit(edges, rows, ntri, emask) -> str:
             "UWW_TABLE_QUAL static const uint16_t UWW_OWNED_MASK[2][64] = {"]
     om = owned_masks(edges)
     out.append(",\n".join("    {" + ", ".join(f"0x{v:03x}" for v in r) + "}" for r in om))
+    out += ["};", "",
+            "// Per case and edge e: mask of the edges the row references for the first time before",
+            "// e's first reference (derived).  A cell numbers the vertices of its owned edges in",
+            "// first-reference order, so edge e's vertex is popcount(owned & before[case][e]).",
+            "UWW_TABLE_QUAL static const uint16_t UWW_EDGE_BEFORE[256][12] __attribute__((aligned(16))) = {"]
+    out.append(",\n".join("    {" + ", ".join(f"0x{v:03x}" for v in r) + "}" for r in first_before(rows)))
     out += ["};", ""]
     return "\n".join(out)
 

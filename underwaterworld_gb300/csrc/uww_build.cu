@@ -36,7 +36,10 @@
 #include <algorithm>
 #include <type_traits>
 
-#define UWW_TABLE_QUAL __constant__
+// The tables live in global memory: every CTA copies them into shared memory
+// once with coalesced loads (from the constant bank, per-thread addresses
+// would be serialised).
+#define UWW_TABLE_QUAL __device__
 #include "mc_tables.h"
 #include "uww_internal.h"
 
@@ -149,20 +152,6 @@ __device__ __forceinline__ int find_owner(const SmemTables& T, int e, int x, int
     return e;
 }
 
-// Number of distinct owned edges first referenced in `row` before edge e.
-__device__ __forceinline__ int rank_in_row(const int8_t* row, unsigned owned, int e)
-{
-    unsigned seen = 0;
-    int r = 0;
-    for (int j = 0; j < 16; ++j) {
-        const int ej = row[j];
-        if (ej < 0 || ej == e) break;
-        const unsigned bit = 1u << ej;
-        if ((owned & bit) && !(seen & bit)) { seen |= bit; ++r; }
-    }
-    return r;
-}
-
 // ---------------------------------------------------------------------------
 // Fast-build density grid, one compute thread per (x, y) column of samples.
 //
@@ -170,14 +159,15 @@ __device__ __forceinline__ int rank_in_row(const int8_t* row, unsigned owned, in
 // every octave depend on z alone: they are tabulated once per chunk in shared
 // memory, together with each octave's runs of consecutive samples that share
 // a z lattice cell.  Per column and octave the x/y lattice coordinates,
-// fades, partial hashes and bilinear weights are computed once; per run the 8
-// corner gradients are fetched (from gp, the gradient of P[i]) and reduced to
-// the run's polynomial in dz:
+// fades, partial hashes and bilinear weights are computed once; per run the
+// corner gradients (from gp, the gradient of P[i]) of the run's two z lattice
+// planes are reduced to the run's polynomial in dz:
 //   A = g.xy . (d - o).xy and G = g.z per corner,
+//   SA_c = sum_xy w A_xyc,  SG_c = sum_xy w G_xyc  (plane c = 0, 1),
 //   n(dz) = al + be dz + fade(dz) (ga + de dz),
-//   al = sum_xy w A_xy0,  be = sum_xy w G_xy0,
-//   ga = sum_xy w (A_xy1 - G_xy1 - A_xy0),  de = sum_xy w (G_xy1 - G_xy0),
-// so a sample costs three FMAs plus its accumulate.  Same Perlin/fBm maths as
+//   al = SA_0,  be = SG_0,  ga = SA_1 - SG_1 - SA_0,  de = SG_1 - SG_0,
+// so a sample costs three FMAs plus its accumulate, and a run whose lower
+// plane is the previous run's upper plane reads only four gradients.  Same Perlin/fBm maths as
 // the parity build (trilinear interpolation == the k-polynomial) in a
 // different operation order with FMA contraction.  The depth bias seeds the
 // first octave; the early blank vote reads the last.  Returns whether any of
@@ -274,23 +264,31 @@ __device__ __forceinline__ int sample_columns_fast(const DevParams& p, const uin
             const int2* runs = Z.runs + k * S;
             const int nr = Z.nruns[k];
             const bool first = k == 0, last = k == K - 1;
+            // weighted face sums over the four xy corners of z lattice plane c:
+            // SA = sum w (g.xy . (d - o).xy), SG = sum w g.z
+            auto face = [&](int c, float& SA, float& SG) {
+                const float4 g00 = gp[h00 ^ c], g01 = gp[h01 ^ c], g10 = gp[h10 ^ c], g11 = gp[h11 ^ c];
+                SA = fmaf(w00, fmaf(g00.x, dx, g00.y * dy),
+                          fmaf(w01, fmaf(g01.x, dx, g01.y * dy1),
+                               fmaf(w10, fmaf(g10.x, dx1, g10.y * dy), w11 * fmaf(g11.x, dx1, g11.y * dy1))));
+                SG = fmaf(w00, g00.z, fmaf(w01, g01.z, fmaf(w10, g10.z, w11 * g11.z)));
+            };
+            // consecutive runs usually sit in consecutive z cells, whose shared
+            // plane is then read once (the condition is the same for every column)
+            float SA0 = 0.f, SG0 = 0.f, SA1 = 0.f, SG1 = 0.f;
+            int prev = 0;
             for (int r = 0; r < nr; ++r) {
                 const int2 run = runs[r];
                 const int zb = run.x, ze = r + 1 < nr ? runs[r + 1].x : S;
-                const int z0 = run.y & 255, z1 = (run.y + 1) & 255;
-                float4 g;
-                g = gp[h00 ^ z0]; const float A0 = fmaf(g.x, dx, g.y * dy), G0 = g.z;
-                g = gp[h00 ^ z1]; const float A1 = fmaf(g.x, dx, g.y * dy), G1 = g.z;
-                g = gp[h01 ^ z0]; const float A2 = fmaf(g.x, dx, g.y * dy1), G2 = g.z;
-                g = gp[h01 ^ z1]; const float A3 = fmaf(g.x, dx, g.y * dy1), G3 = g.z;
-                g = gp[h10 ^ z0]; const float A4 = fmaf(g.x, dx1, g.y * dy), G4 = g.z;
-                g = gp[h10 ^ z1]; const float A5 = fmaf(g.x, dx1, g.y * dy), G5 = g.z;
-                g = gp[h11 ^ z0]; const float A6 = fmaf(g.x, dx1, g.y * dy1), G6 = g.z;
-                g = gp[h11 ^ z1]; const float A7 = fmaf(g.x, dx1, g.y * dy1), G7 = g.z;
-                const float al = fmaf(w00, A0, fmaf(w01, A2, fmaf(w10, A4, w11 * A6)));
-                const float be = fmaf(w00, G0, fmaf(w01, G2, fmaf(w10, G4, w11 * G6)));
-                const float ga = fmaf(w00, A1 - G1 - A0, fmaf(w01, A3 - G3 - A2, fmaf(w10, A5 - G5 - A4, w11 * (A7 - G7 - A6))));
-                const float de = fmaf(w00, G1 - G0, fmaf(w01, G3 - G2, fmaf(w10, G5 - G4, w11 * (G7 - G6))));
+                if (r > 0 && run.y == prev + 1) {
+                    SA0 = SA1;
+                    SG0 = SG1;
+                } else {
+                    face(run.y & 255, SA0, SG0);
+                }
+                face((run.y + 1) & 255, SA1, SG1);
+                prev = run.y;
+                const float al = SA0, be = SG0, ga = SA1 - SG1 - SA0, de = SG1 - SG0;
 #pragma unroll 2
                 for (int z = zb; z < ze; ++z) {
                     const float2 t = dzc[z];
@@ -557,8 +555,8 @@ __device__ void chunk_front(const DevParams& p, const BuildArgs& a, SmemTables& 
                 inside |= !(v > p.iso_level);
             }
         } else if constexpr (std::is_same<O, FastOps>::value) {
-            inside = sample_columns_fast(p, T.perm, T.gp, ztable_at(dyn_smem + a.ztable_offset, S, p.octaves), rho, N,
-                                         ox, oy, oz, ncomp);
+            const ZTable zt = ztable_at(dyn_smem + a.ztable_offset, S, p.octaves);
+            inside = sample_columns_fast(p, T.perm, T.gp, zt, rho, N, ox, oy, oz, ncomp);
         } else {
             for (int idx = tid; idx < S3; idx += ncomp) {
                 const int x = idx / S2, r = idx - x * S2, y = r / S, z = r - y * S;
@@ -685,16 +683,17 @@ __device__ void chunk_emit(const DevParams& p, const BuildArgs& a, SmemTables& T
             const uint32_t vb = W.get_vbase(c);
             const uint32_t ib = W.get_ibase(ai);
             unsigned seen = 0;
-            uint32_t cnt = 0;
+            const uint16_t* before = UWW_EDGE_BEFORE[cs];
             const int nidx = 3 * T.ntri[cs];
             for (int i = 0; i < nidx; ++i) {
                 const int e = row[i];
                 const unsigned bit = 1u << e;
                 uint32_t id;
                 if (own_mask & bit) {
+                    // the cell numbers its owned edges' vertices in first-reference order
+                    id = vb + __popc(own_mask & __ldg(before + e));
                     if (!(seen & bit)) {
                         seen |= bit;
-                        id = vb + cnt++;
                         const int ca = T.corners[e][0], cb = T.corners[e][1];
                         const int ax = x + ((0x66 >> ca) & 1), ay = y + (ca >> 2), az = z + ((0xcc >> ca) & 1);
                         const int bx = x + ((0x66 >> cb) & 1), by = y + (cb >> 2), bz = z + ((0xcc >> cb) & 1);
@@ -717,15 +716,13 @@ __device__ void chunk_emit(const DevParams& p, const BuildArgs& a, SmemTables& T
                         // input, chunk.rs:215) to pass 2, which overwrites it
                         v2[1] = make_float2(O::add(mz, (float)oz), (float)cb);
                         v2[2] = make_float2(0.f, 0.f);
-                    } else {
-                        id = vb + rank_in_row(row, own_mask, e);
                     }
                 } else {
                     int qx, qy, qz;
                     const int oe = find_owner(T, e, x, y, z, N, oriented, qx, qy, qz);
                     const int oc = (qx * N + qy) * N + qz;
                     const unsigned oown = T.owned[oriented][boundary_flags(qx, qy, qz, N)];
-                    id = W.get_vbase(oc) + rank_in_row(T.tri[cases[oc]], oown, oe);
+                    id = W.get_vbase(oc) + __popc(oown & __ldg(&UWW_EDGE_BEFORE[cases[oc]][oe]));
                 }
                 a.inds[ioff + ib + i] = id;
             }
@@ -789,19 +786,23 @@ __global__ void __launch_bounds__(MAXT, MINB) build_kernel(const DevParams p, co
     {
         const int4* src = reinterpret_cast<const int4*>(&UWW_TRI_TABLE[0][0]);
         int4* dst = reinterpret_cast<int4*>(&T.tri[0][0]);
-        for (int i = tid; i < 256; i += nthr) dst[i] = src[i];
+        for (int i = tid; i < 256; i += nthr) dst[i] = __ldg(src + i);
     }
     for (int i = tid; i < 256; i += nthr) {
-        T.edges[i] = UWW_CASE_EDGES[i];
-        T.ntri[i] = UWW_CASE_NTRI[i];
-        T.perm[i] = p.perm[i];
+        T.edges[i] = __ldg(&UWW_CASE_EDGES[i]);
+        T.ntri[i] = __ldg(&UWW_CASE_NTRI[i]);
+    }
+    // the permutation arrives in the parameter (constant) bank: read it as words
+    for (int i = tid; i < 64; i += nthr) reinterpret_cast<uint32_t*>(T.perm)[i] = reinterpret_cast<const uint32_t*>(p.perm)[i];
+    for (int i = tid; i < 128; i += nthr) (&T.owned[0][0])[i] = __ldg(&UWW_OWNED_MASK[0][0] + i);
+    for (int i = tid; i < 12 * 4 * 5; i += nthr) (&T.share[0][0][0])[i] = __ldg(&UWW_EDGE_SHARE[0][0][0] + i);
+    for (int i = tid; i < 24; i += nthr) (&T.corners[0][0])[i] = __ldg(&UWW_EDGE_CORNERS[0][0] + i);
+    __syncthreads();
+    for (int i = tid; i < 256; i += nthr) {
         float gx, gy, gz;
-        grad_vec(p.perm[i], gx, gy, gz);
+        grad_vec(T.perm[i], gx, gy, gz);
         T.gp[i] = make_float4(gx, gy, gz, 0.f);
     }
-    for (int i = tid; i < 128; i += nthr) (&T.owned[0][0])[i] = (&UWW_OWNED_MASK[0][0])[i];
-    for (int i = tid; i < 12 * 4 * 5; i += nthr) (&T.share[0][0][0])[i] = (&UWW_EDGE_SHARE[0][0][0])[i];
-    for (int i = tid; i < 24; i += nthr) (&T.corners[0][0])[i] = (&UWW_EDGE_CORNERS[0][0])[i];
     if (tid == 0) {
         T.errflags = 0;
         T.overflow = 0;
