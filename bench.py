@@ -551,7 +551,7 @@ def main():
                    "mean_verts_per_step": mean_v, "mean_inds_per_step": mean_i},
         "mvoxels_per_s": value * 12 ** 3 / 1e6,
         "msamples_per_s": value * 13 ** 3 / 1e6,
-        "gpu_launches": args.steps,
+        "gpu_launches": args.steps * (2 if params[0].outputs & (abi.UWW_OUT_COLOR | abi.UWW_OUT_NORMALS) else 1),
         "clocks": clk,
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": achieved / fp32_peak, "traffic": NCU_DRAM_BYTES_PER_LAUNCH,

@@ -650,9 +650,40 @@ __device__ void chunk_front(const DevParams& p, const BuildArgs& a, SmemTables& 
     }
 }
 
+// Pass 2 of the emission for vertex v: pass 1 left its position and, in
+// colour slot 0, the owner's corner b (the value ramp's input, chunk.rs:215);
+// write its colour and unit normal.
+template <class O>
+__device__ __forceinline__ void finish_vertex(const DevParams& p, const uint8_t* P, const float4* gp,
+                                              uww_vert_color* verts, float* normals, uint32_t v, bool want_color,
+                                              bool want_normals)
+{
+    float2* v2 = reinterpret_cast<float2*>(verts + v);
+    const float2 p01 = v2[0], p2c = v2[1];
+    const int cb = (int)p2c.y;
+    if (want_color) {
+        float col[3];
+        vertex_color<O>(p, p2c.x, cb, col);
+        v2[1] = make_float2(p2c.x, col[0]);
+        v2[2] = make_float2(col[1], col[2]);
+    } else {
+        v2[1] = make_float2(p2c.x, 0.f);
+    }
+    if (want_normals) {
+        float g[3];
+        if constexpr (std::is_same<O, FastOps>::value)
+            density_grad_fast(p, P, gp, p01.x, p01.y, p2c.x, g);
+        else
+            density<O, true>(p, P, p01.x, p01.y, p2c.x, g);
+        safe_normalize<O>(g);
+        float* nn = normals + 3 * (size_t)v;
+        nn[0] = g[0]; nn[1] = g[1]; nn[2] = g[2];
+    }
+}
+
 // Emission of a chunk from workspace `buf`, given its offsets.  Every compute
 // thread must call it.
-template <class O>
+template <class O, bool QUEUE>
 __device__ void chunk_emit(const DevParams& p, const BuildArgs& a, SmemTables& T, uint8_t* dyn_smem, int buf,
                            const Offsets off, int ncomp)
 {
@@ -714,7 +745,7 @@ __device__ void chunk_emit(const DevParams& p, const BuildArgs& a, SmemTables& T
                         v2[0] = make_float2(O::add(mx, (float)ox), O::add(my, (float)oy));
                         // colour slot 0 carries the owner's corner b (the value ramp's
                         // input, chunk.rs:215) to pass 2, which overwrites it
-                        v2[1] = make_float2(O::add(mz, (float)oz), (float)cb);
+                        v2[1] = make_float2(O::add(mz, (float)oz), (want_color || want_normals) ? (float)cb : 0.f);
                         v2[2] = make_float2(0.f, 0.f);
                     }
                 } else {
@@ -728,31 +759,12 @@ __device__ void chunk_emit(const DevParams& p, const BuildArgs& a, SmemTables& T
             }
         }
     }
-    if (want_color || want_normals) {
+    // pass 2 (colour and normal per vertex): inline for one chunk per launch;
+    // the batched form runs it as vertex_kernel over the whole batch
+    if (!QUEUE && (want_color || want_normals)) {
         bar_sync(kBarCompute, ncomp);
-        for (uint32_t vid = tid; vid < nV; vid += ncomp) {
-            float2* v2 = reinterpret_cast<float2*>(a.verts + voff + vid);
-            const float2 p01 = v2[0], p2c = v2[1];
-            const int cb = (int)p2c.y;
-            if (want_color) {
-                float col[3];
-                vertex_color<O>(p, p2c.x, cb, col);
-                v2[1] = make_float2(p2c.x, col[0]);
-                v2[2] = make_float2(col[1], col[2]);
-            } else {
-                v2[1] = make_float2(p2c.x, 0.f);
-            }
-            if (want_normals) {
-                float g[3];
-                if constexpr (std::is_same<O, FastOps>::value)
-                    density_grad_fast(p, T.perm, T.gp, p01.x, p01.y, p2c.x, g);
-                else
-                    density<O, true>(p, T.perm, p01.x, p01.y, p2c.x, g);
-                safe_normalize<O>(g);
-                float* nn = a.normals + 3 * (size_t)(voff + vid);
-                nn[0] = g[0]; nn[1] = g[1]; nn[2] = g[2];
-            }
-        }
+        for (uint32_t vid = tid; vid < nV; vid += ncomp)
+            finish_vertex<O>(p, T.perm, T.gp, a.verts, a.normals, voff + vid, want_color, want_normals);
     }
 }
 
@@ -815,7 +827,7 @@ __global__ void __launch_bounds__(MAXT, MINB) build_kernel(const DevParams p, co
         bar_sync(kBarCompute, ncomp);
         if (tid == 0) chunk_record(a, T, T.ci[0], 0ull, T.off[0], false);
         bar_sync(kBarCompute, ncomp);
-        chunk_emit<O>(p, a, T, dyn_smem, 0, T.off[0], ncomp);
+        chunk_emit<O, QUEUE>(p, a, T, dyn_smem, 0, T.off[0], ncomp);
         bar_sync(kBarCompute, ncomp);
         if (tid == 0) {
             a.totals[2] = T.overflow;
@@ -857,7 +869,7 @@ __global__ void __launch_bounds__(MAXT, MINB) build_kernel(const DevParams p, co
             bar_sync(kBarCompute, ncomp);
             if (i > 0) {
                 bar_sync(kBarOffsets, nthr);
-                chunk_emit<O>(p, a, T, dyn_smem, (i - 1) & 1, T.off[(i - 1) & 1], ncomp);
+                chunk_emit<O, QUEUE>(p, a, T, dyn_smem, (i - 1) & 1, T.off[(i - 1) & 1], ncomp);
                 bar_sync(kBarCompute, ncomp);  // workspace (i-1)&1 is reused by chunk i+1
                 if (valid) bar_arrive(kBarEmitDone, nthr);
             }
@@ -886,6 +898,34 @@ __global__ void __launch_bounds__(MAXT, MINB) build_kernel(const DevParams p, co
             atomicExch(a.work_counter, 0u);
         }
     }
+}
+
+// Pass 2 of the batched build over every vertex of the batch: vertex counts
+// are very uneven across chunks, so the per-vertex colour and analytic-normal
+// work is spread over the whole GPU instead of staying with the CTA that
+// built the chunk.  The vertex count is read from totals[0].
+template <class O>
+__global__ void __launch_bounds__(256) vertex_kernel(const DevParams p, uww_vert_color* __restrict__ verts,
+                                                     float* __restrict__ normals,
+                                                     const unsigned long long* __restrict__ totals,
+                                                     uint32_t vert_capacity)
+{
+    __shared__ uint8_t P[256];
+    __shared__ float4 gp[256];
+    for (int i = threadIdx.x; i < 64; i += blockDim.x)
+        reinterpret_cast<uint32_t*>(P)[i] = reinterpret_cast<const uint32_t*>(p.perm)[i];
+    __syncthreads();
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) {
+        float gx, gy, gz;
+        grad_vec(P[i], gx, gy, gz);
+        gp[i] = make_float4(gx, gy, gz, 0.f);
+    }
+    __syncthreads();
+    const uint32_t nv = (uint32_t)min(*totals, (unsigned long long)vert_capacity);
+    const bool want_color = (p.outputs & UWW_OUT_COLOR) != 0;
+    const bool want_normals = (p.outputs & UWW_OUT_NORMALS) != 0 && normals != nullptr;
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += gridDim.x * blockDim.x)
+        finish_vertex<O>(p, P, gp, verts, normals, v, want_color, want_normals);
 }
 
 template <class O>
@@ -968,6 +1008,16 @@ cudaError_t launch_build(const DevParams& p, const BuildArgs& a, bool queue, int
 {
     const bool exact = p.math_mode == UWW_MATH_EXACT;
     kernel_for(exact, queue, threads > 224)<<<grid, threads, dyn_smem, s>>>(p, a);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess || !queue || !(p.outputs & (UWW_OUT_COLOR | UWW_OUT_NORMALS))) return e;
+    // the batched form's pass 2, over the whole batch
+    int dev = 0, sms = 0;
+    e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    const int vgrid = std::max(1, sms * 8);
+    if (exact) vertex_kernel<ExactOps><<<vgrid, 256, 0, s>>>(p, a.verts, a.normals, a.totals, a.vert_capacity);
+    else vertex_kernel<FastOps><<<vgrid, 256, 0, s>>>(p, a.verts, a.normals, a.totals, a.vert_capacity);
     return cudaGetLastError();
 }
 
