@@ -202,6 +202,32 @@ def timed(stream, fn, flush=None):
     return e0.elapsed_time(e1) * 1e-3
 
 
+def leg_noise_stage(ctx, stream, flush, params, descs, steps, warmup):
+    """The noise stage alone: uww_sample_chunks (Chunk::build_iso for the batch)
+    on the uniform grid, samples written to HBM; FP32 roofline of the algorithmic
+    count (FLOPS_PER_OCTAVE per sample-octave + FLOPS_PER_SAMPLE_EXTRA)."""
+    import torch
+    from underwaterworld_gb300 import abi
+    n = len(descs)
+    ctx.set_params(params)
+    ns = n * 13 ** 3
+    out = torch.empty(ns, dtype=torch.float32, device=stream.device)
+    d_desc = torch.from_numpy(descs.view(np.uint8).copy()).to(stream.device)
+    L = abi.lib()
+
+    def run():
+        abi.check(L.uww_sample_chunks(ctx.h, C.c_void_p(d_desc.data_ptr()), n, 12, C.c_void_p(out.data_ptr()), ns),
+                  "sample")
+
+    for _ in range(warmup):
+        run()
+    ts = [timed(stream, run, flush) for _ in range(steps)]
+    t = statistics.median(ts)
+    flops = ns * (params.octaves * FLOPS_PER_OCTAVE + FLOPS_PER_SAMPLE_EXTRA)
+    return {"us": t * 1e6, "samples": ns, "msamples_per_s": ns / t / 1e6, "tflops": flops / t / 1e12,
+            "flops_per_step": flops, "bytes_written": ns * 4}
+
+
 def leg_frame_graph(ctx, params, descs, steps, warmup):
     """Uniform grid as a per-frame CUDA graph: descriptor + count upload, build,
     record + totals download, one graph launch per frame; host wall time."""
@@ -499,6 +525,7 @@ def main():
         extra["e2e"] = {"value": world * n / statistics.mean(e2e_t), "unit": UNIT,
                         "h2d_bytes_per_step": h2d // k, "d2h_bytes_per_step": d2h // k}
 
+    extra["noise_stage"] = leg_noise_stage(ctx, stream, flush, params[0], descs, max(10, min(args.steps, 200)), 3)
     if not args.quick:
         extra["frame_graph"] = leg_frame_graph(ctx, params[0], descs, max(5, min(args.steps, 50)), 3)
         extra["mixed_lod"] = leg_mixed_lod(stream, flush, max(10, min(args.steps, 200)), 3)
@@ -563,6 +590,12 @@ def main():
                                   "frac": out_bytes / (t_total / args.steps) / 1e9 / hbm_peak,
                                   "bytes_per_step": out_bytes, "peak_source": hbm_src}},
     }
+    ns_leg = extra.get("noise_stage")
+    if ns_leg:
+        ns_leg["frac_of_fp32_peak"] = ns_leg["tflops"] / fp32_peak
+        line["roofline"]["noise_stage"] = {"bound": "fp32", "achieved": ns_leg["tflops"], "peak": fp32_peak,
+                                           "unit": "TFLOP/s", "frac": ns_leg["tflops"] / fp32_peak,
+                                           "kernel": "sample_kernel_fast (uww_sample_chunks), 4096 x 13^3 samples"}
     line.update({k: v for k, v in extra.items() if k != "e2e"})
     if "adjoint" in extra:
         line["fwd_adjoint_mvoxels_per_s"] = extra["adjoint"]["fwd_adjoint_mvoxels_per_s"]

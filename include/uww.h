@@ -307,6 +307,18 @@ int uww_host_free(void* p);
 int uww_memcpy(uww_ctx* ctx, void* dst, const void* src, size_t bytes, int kind);
 int uww_memset(uww_ctx* ctx, void* dst, int value, size_t bytes);
 
+/* ---- density samples without the mesher -------------------------------------- */
+/* Chunk::build_iso (chunk.rs:105-129) for a batch: the (cells+1)^3 f32 density
+ * samples of every chunk at d_samples + desc.sample_offset (laid out
+ * (x*S + y)*S + z as Build::isos, chunk.rs:351-353), sample_capacity floats
+ * available.  The same values as the batched build's UWW_OUT_SAMPLES in the
+ * same math mode.  Asynchronous; a descriptor with cells outside 1..max_cells
+ * or samples outside the capacity is skipped and flagged (uww_sample_status). */
+int uww_sample_chunks(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint32_t max_cells, float* d_samples,
+                      uint64_t sample_capacity);
+/* UWW_ERRFLAG_BAD / UWW_ERRFLAG_RANGE raised by the last uww_sample_chunks (synchronises). */
+int uww_sample_status(uww_ctx* ctx, uint32_t* flags);
+
 /* ---- point queries ------------------------------------------------------------ */
 /* density(world xyz) for n points: perlin_util::iso_at (perlin_util.rs:24-29) with
  * (x,y,z) = world / CHUNK_SIZE as in boid.rs:132-137.  d_xyz: 3n floats; d_out: n. */

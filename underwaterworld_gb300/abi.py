@@ -118,6 +118,8 @@ _SIGS = {
     "uww_frame_launch": (C.c_int, [P]),
     "uww_frame_set_params": (C.c_int, [P, C.POINTER(Params)]),
     "uww_frame_destroy": (C.c_int, [P]),
+    "uww_sample_chunks": (C.c_int, [P, P, C.c_uint32, C.c_uint32, P, C.c_uint64]),
+    "uww_sample_status": (C.c_int, [P, C.POINTER(C.c_uint32)]),
     "uww_forward": (C.c_int, [P, P, C.c_uint32, C.c_uint32, C.POINTER(MeshOut), P]),
     "uww_backward": (C.c_int, [P, P, C.c_uint32, C.c_uint32, P, P, P, P, P, C.c_uint64]),
     "uww_height_loss": (C.c_int, [P, P, P, C.c_uint32, C.c_float, C.c_float, C.c_float, C.c_uint32, C.c_uint32,

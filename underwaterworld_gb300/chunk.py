@@ -256,6 +256,23 @@ class Context:
         samples = self.download(d_samp, (nsamp,), np.float32) if d_samp else None
         return MeshBatch(records, verts, normals, inds, cases, totals, totals_status(totals), samples)
 
+    def sample_chunks(self, descs: np.ndarray) -> np.ndarray:
+        """Density samples of every chunk (uww_sample_chunks, Chunk::build_iso for a
+        batch), laid out at each descriptor's sample_offset."""
+        descs = np.ascontiguousarray(descs, dtype=abi.CHUNK_DESC_DTYPE)
+        n = descs.shape[0]
+        ns = total_samples(descs)
+        d_desc = self.upload(descs) if n else DeviceArray(32)
+        d_s = DeviceArray(max(ns, 1) * 4)
+        max_cells = int(descs["cells"].max()) if n else 1
+        check(lib().uww_sample_chunks(self.h, C.c_void_p(d_desc.ptr), n, max_cells, C.c_void_p(d_s.ptr), ns),
+              "uww_sample_chunks")
+        flags = C.c_uint32()
+        check(lib().uww_sample_status(self.h, C.byref(flags)), "uww_sample_status")
+        if flags.value:
+            raise abi.UWWError(abi.UWW_ERR_INVALID_ARG, f"uww_sample_chunks flags {flags.value}")
+        return self.download(d_s, (ns,), np.float32)
+
     def density_at(self, xyz: np.ndarray) -> np.ndarray:
         """Density at world points (n, 3) f32 -- iso_at with world = chunk units * CHUNK_SIZE."""
         xyz = np.ascontiguousarray(xyz, dtype=np.float32).reshape(-1, 3)

@@ -270,7 +270,7 @@ template <class O, int KMAX>
 __global__ void __launch_bounds__(kBwdThreads) backward_kernel(const DevParams p, const AdjointArgs a)
 {
     constexpr int NV = KMAX + 5;
-    __shared__ uint8_t P[256];
+    __shared__ __align__(16) uint8_t P[256];
     __shared__ float red[kBwdThreads / 32][NV];
     __shared__ unsigned int last;
     for (int i = threadIdx.x; i < 256; i += kBwdThreads) P[i] = p.perm[i];

@@ -406,6 +406,7 @@ int uww_ctx_destroy(uww_ctx* ctx)
     cudaFree(ctx->d_records);
     cudaFree(ctx->d_adj_part);
     cudaFree(ctx->d_adj_counter);
+    cudaFree(ctx->d_sample_err);
     if (ctx->h_totals) cudaFreeHost(ctx->h_totals);
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;

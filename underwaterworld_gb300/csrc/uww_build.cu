@@ -42,6 +42,7 @@
 #define UWW_TABLE_QUAL __device__
 #include "mc_tables.h"
 #include "uww_internal.h"
+#include "uww_noise.cuh"
 
 namespace uww {
 
@@ -52,38 +53,6 @@ constexpr int kIndShift = 22;
 constexpr int kActShift = 44;
 constexpr unsigned long long kField22 = (1ull << 22) - 1;
 
-// Named barriers: 0 = whole CTA, 1 = compute warps, 2 = ticket hand-off,
-// 3 = offsets hand-off, 4 = noise done, 5 = emission done (2-5: compute
-// warps + control warp).
-constexpr int kBarCompute = 1;
-constexpr int kBarTicket = 2;
-constexpr int kBarOffsets = 3;
-constexpr int kBarNoiseDone = 4;  // compute warps arrive (no wait) once a chunk's noise is done
-constexpr int kBarEmitDone = 5;   // compute warps arrive (no wait) once the previous chunk is emitted
-
-__device__ __forceinline__ void bar_arrive(int id, int count)
-{
-    asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void bar_sync(int id, int count)
-{
-    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ int bar_or(int id, int count, int pred)
-{
-    int r;
-    asm volatile(
-        "{\n\t.reg .pred p, q;\n\t"
-        "setp.ne.s32 p, %1, 0;\n\t"
-        "bar.red.or.pred q, %2, %3, p;\n\t"
-        "selp.s32 %0, 1, 0, q;\n\t}"
-        : "=r"(r)
-        : "r"(pred), "r"(id), "r"(count)
-        : "memory");
-    return r;
-}
 
 // Per in-flight chunk, kept in shared memory between the front and back halves.
 struct ChunkInfo {
@@ -150,157 +119,6 @@ __device__ __forceinline__ int find_owner(const SmemTables& T, int e, int x, int
     }
     ox = x; oy = y; oz = z;  // unreachable: the cell itself is always a candidate
     return e;
-}
-
-// ---------------------------------------------------------------------------
-// Fast-build density grid, one compute thread per (x, y) column of samples.
-//
-// Along a column only z varies, and the z lattice cell, fraction and fade of
-// every octave depend on z alone: they are tabulated once per chunk in shared
-// memory, together with each octave's runs of consecutive samples that share
-// a z lattice cell.  Per column and octave the x/y lattice coordinates,
-// fades, partial hashes and bilinear weights are computed once; per run the
-// corner gradients (from gp, the gradient of P[i]) of the run's two z lattice
-// planes are reduced to the run's polynomial in dz:
-//   A = g.xy . (d - o).xy and G = g.z per corner,
-//   SA_c = sum_xy w A_xyc,  SG_c = sum_xy w G_xyc  (plane c = 0, 1),
-//   n(dz) = al + be dz + fade(dz) (ga + de dz),
-//   al = SA_0,  be = SG_0,  ga = SA_1 - SG_1 - SA_0,  de = SG_1 - SG_0,
-// so a sample costs three FMAs plus its accumulate, and a run whose lower
-// plane is the previous run's upper plane reads only four gradients.  Same Perlin/fBm maths as
-// the parity build (trilinear interpolation == the k-polynomial) in a
-// different operation order with FMA contraction.  The depth bias seeds the
-// first octave; the early blank vote reads the last.  Returns whether any of
-// this thread's samples is at or below the iso-level.  Every compute thread
-// must call it.
-struct ZTable {
-    float2* dzc;   // [octave][z]: (dz, fade(dz))
-    int2* runs;    // [octave][run]: (first z, z lattice cell)
-    int* nruns;    // [octave]
-    float* bias;   // [z]
-};
-
-__device__ __forceinline__ ZTable ztable_at(uint8_t* base, int S, int octaves)
-{
-    ZTable t;
-    t.dzc = reinterpret_cast<float2*>(base);
-    t.runs = reinterpret_cast<int2*>(base + (size_t)octaves * S * sizeof(float2));
-    t.nruns = reinterpret_cast<int*>(base + (size_t)octaves * S * (sizeof(float2) + sizeof(int2)));
-    t.bias = reinterpret_cast<float*>(base + (size_t)octaves * S * (sizeof(float2) + sizeof(int2)) +
-                                      (size_t)octaves * sizeof(int));
-    return t;
-}
-
-__device__ __forceinline__ int sample_columns_fast(const DevParams& p, const uint8_t* __restrict__ P,
-                                                   const float4* __restrict__ gp, const ZTable Z,
-                                                   float* __restrict__ rho, int N, int ox, int oy, int oz,
-                                                   int ncomp)
-{
-    const int S = N + 1, SS = S * S, K = p.octaves;
-    const float s = __fdiv_rn((float)p.chunk_size, (float)N);
-    const float bf = p.base_freq;
-    float norm = kPerlinScale;
-    if (p.normalize) {
-        float mx = 0.f;
-        for (int k = 0; k < K; ++k) mx += p.amp[k];
-        norm = __fdiv_rn(kPerlinScale, mx);
-    }
-    const float zoff = (float)oz + p.offset[2];
-    const float iso = p.iso_level;
-
-    // ---- per-chunk z tables, shared by every column ----
-    for (int i = threadIdx.x; i < K * S; i += ncomp) {
-        const int k = i / S, z = i - k * S;
-        const float qz = fmaf((float)z, s, zoff) * (bf * p.mult[k]);
-        const float fz = floorf(qz);
-        const float dz = qz - fz;
-        Z.dzc[i] = make_float2(dz, fade<FastOps>(dz));
-        reinterpret_cast<int*>(Z.runs)[2 * i + 1] = (int)fz;  // staged: cell of sample z
-        if (k == 0) {
-            const float wz = fmaf((float)z, s, (float)oz);
-            float b = 0.f;
-            if (p.bias_mode == UWW_BIAS_TERRACED) {
-                const float adj = __fdiv_rn((wz + p.offset[2]) * bf * p.bias_a, p.bias_b);
-                b = adj - fmodf(adj, p.bias_c);
-            } else if (p.bias_mode == UWW_BIAS_LINEAR) {
-                b = p.bias_a * (wz - p.bias_b);
-            }
-            Z.bias[z] = b;
-        }
-    }
-    bar_sync(kBarCompute, ncomp);
-    // compact each octave's cells into runs (one thread per octave)
-    for (int k = threadIdx.x; k < K; k += ncomp) {
-        int2* r = Z.runs + k * S;
-        int n = 0, prev = 0;
-        for (int z = 0; z < S; ++z) {
-            const int iz = r[z].y;  // staged value; r[n] with n <= z is already consumed
-            if (z == 0 || iz != prev) r[n++] = make_int2(z, iz);
-            prev = iz;
-        }
-        Z.nruns[k] = n;
-    }
-    bar_sync(kBarCompute, ncomp);
-
-    int inside = 0;
-    for (int col = threadIdx.x; col < SS; col += ncomp) {
-        const int x = col / S, y = col - x * S;
-        float* out = rho + col * S;
-        const float nx = (fmaf((float)x, s, (float)ox) + p.offset[0]) * bf;
-        const float ny = (fmaf((float)y, s, (float)oy) + p.offset[1]) * bf;
-        for (int k = 0; k < K; ++k) {
-            const float m = p.mult[k], amp = p.amp[k] * norm;
-            const float qx = nx * m, qy = ny * m;
-            const float fx = floorf(qx), fy = floorf(qy);
-            const int ix = (int)fx, iy = (int)fy;
-            const float dx = qx - fx, dy = qy - fy, dx1 = dx - 1.f, dy1 = dy - 1.f;
-            const float a = fade<FastOps>(dx), b = fade<FastOps>(dy);
-            const float w00 = amp * (1.f - a) * (1.f - b), w10 = amp * a * (1.f - b);
-            const float w01 = amp * (1.f - a) * b, w11 = amp * a * b;
-            const int hx0 = P[ix & 255], hx1 = P[(ix + 1) & 255];
-            const int h00 = P[hx0 ^ (iy & 255)], h01 = P[hx0 ^ ((iy + 1) & 255)];
-            const int h10 = P[hx1 ^ (iy & 255)], h11 = P[hx1 ^ ((iy + 1) & 255)];
-            const float2* dzc = Z.dzc + k * S;
-            const int2* runs = Z.runs + k * S;
-            const int nr = Z.nruns[k];
-            const bool first = k == 0, last = k == K - 1;
-            // weighted face sums over the four xy corners of z lattice plane c:
-            // SA = sum w (g.xy . (d - o).xy), SG = sum w g.z
-            auto face = [&](int c, float& SA, float& SG) {
-                const float4 g00 = gp[h00 ^ c], g01 = gp[h01 ^ c], g10 = gp[h10 ^ c], g11 = gp[h11 ^ c];
-                SA = fmaf(w00, fmaf(g00.x, dx, g00.y * dy),
-                          fmaf(w01, fmaf(g01.x, dx, g01.y * dy1),
-                               fmaf(w10, fmaf(g10.x, dx1, g10.y * dy), w11 * fmaf(g11.x, dx1, g11.y * dy1))));
-                SG = fmaf(w00, g00.z, fmaf(w01, g01.z, fmaf(w10, g10.z, w11 * g11.z)));
-            };
-            // consecutive runs usually sit in consecutive z cells, whose shared
-            // plane is then read once (the condition is the same for every column)
-            float SA0 = 0.f, SG0 = 0.f, SA1 = 0.f, SG1 = 0.f;
-            int prev = 0;
-            for (int r = 0; r < nr; ++r) {
-                const int2 run = runs[r];
-                const int zb = run.x, ze = r + 1 < nr ? runs[r + 1].x : S;
-                if (r > 0 && run.y == prev + 1) {
-                    SA0 = SA1;
-                    SG0 = SG1;
-                } else {
-                    face(run.y & 255, SA0, SG0);
-                }
-                face((run.y + 1) & 255, SA1, SG1);
-                prev = run.y;
-                const float al = SA0, be = SG0, ga = SA1 - SG1 - SA0, de = SG1 - SG0;
-#pragma unroll 2
-                for (int z = zb; z < ze; ++z) {
-                    const float2 t = dzc[z];
-                    const float v = fmaf(t.y, fmaf(de, t.x, ga), fmaf(be, t.x, al));
-                    const float r0 = v + (first ? Z.bias[z] : out[z]);
-                    out[z] = r0;
-                    if (last) inside |= !(r0 > iso);
-                }
-            }
-        }
-    }
-    return inside;
 }
 
 // ---------------------------------------------------------------------------
@@ -910,7 +728,7 @@ __global__ void __launch_bounds__(256) vertex_kernel(const DevParams p, uww_vert
                                                      const unsigned long long* __restrict__ totals,
                                                      uint32_t vert_capacity)
 {
-    __shared__ uint8_t P[256];
+    __shared__ __align__(16) uint8_t P[256];
     __shared__ float4 gp[256];
     for (int i = threadIdx.x; i < 64; i += blockDim.x)
         reinterpret_cast<uint32_t*>(P)[i] = reinterpret_cast<const uint32_t*>(p.perm)[i];
@@ -931,7 +749,7 @@ __global__ void __launch_bounds__(256) vertex_kernel(const DevParams p, uww_vert
 template <class O>
 __global__ void density_kernel(const DevParams p, const float* __restrict__ xyz, uint32_t n, float* __restrict__ out)
 {
-    __shared__ uint8_t P[256];
+    __shared__ __align__(16) uint8_t P[256];
     for (int i = threadIdx.x; i < 256; i += blockDim.x) P[i] = p.perm[i];
     __syncthreads();
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)

@@ -169,4 +169,6 @@ struct uww_ctx {
     // backward's final reduction (zero between launches)
     float* d_adj_part = nullptr;     size_t adj_part_cap = 0;
     unsigned int* d_adj_counter = nullptr;
+    // uww_sample_chunks: UWW_ERRFLAG_* of the last call
+    unsigned int* d_sample_err = nullptr;
 };

@@ -1,0 +1,272 @@
+// uww_noise.cuh -- named-barrier helpers and the fast build's column noise,
+// shared by the batched build (uww_build.cu) and the sampling kernel
+// (uww_sample.cu).  Reference: perlin_util.rs:6-29 over the noise crate's
+// perlin_3d (perlin_util.rs:13), sampled as Chunk::build_iso (chunk.rs:105-129).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "uww_internal.h"
+
+namespace uww {
+namespace {
+
+// Named barriers: 0 = whole CTA, 1 = compute warps, 2 = ticket hand-off,
+// 3 = offsets hand-off, 4 = noise done, 5 = emission done (2-5: compute
+// warps + control warp).
+constexpr int kBarCompute = 1;
+constexpr int kBarTicket = 2;
+constexpr int kBarOffsets = 3;
+constexpr int kBarNoiseDone = 4;  // compute warps arrive (no wait) once a chunk's noise is done
+constexpr int kBarEmitDone = 5;   // compute warps arrive (no wait) once the previous chunk is emitted
+
+__device__ __forceinline__ void bar_arrive(int id, int count)
+{
+    asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void bar_sync(int id, int count)
+{
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ int bar_or(int id, int count, int pred)
+{
+    int r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.s32 p, %1, 0;\n\t"
+        "bar.red.or.pred q, %2, %3, p;\n\t"
+        "selp.s32 %0, 1, 0, q;\n\t}"
+        : "=r"(r)
+        : "r"(pred), "r"(id), "r"(count)
+        : "memory");
+    return r;
+}
+
+// ---------------------------------------------------------------------------
+// Fast-build density grid, one compute thread per (x, y) column of samples.
+//
+// Along a column only z varies, and the z lattice cell, fraction and fade of
+// every octave depend on z alone: they are tabulated once per chunk in shared
+// memory, together with each octave's runs of consecutive samples that share
+// a z lattice cell.  Per column and octave the x/y lattice coordinates,
+// fades, partial hashes and bilinear weights are computed once; per run the
+// corner gradients (from gp, the gradient of P[i]) of the run's two z lattice
+// planes are reduced to the run's polynomial in dz:
+//   A = g.xy . (d - o).xy and G = g.z per corner,
+//   SA_c = sum_xy w A_xyc,  SG_c = sum_xy w G_xyc  (plane c = 0, 1),
+//   n(dz) = al + be dz + fade(dz) (ga + de dz),
+//   al = SA_0,  be = SG_0,  ga = SA_1 - SG_1 - SA_0,  de = SG_1 - SG_0,
+// so a sample costs three FMAs plus its accumulate, and a run whose lower
+// plane is the previous run's upper plane reads only four gradients.  Same Perlin/fBm maths as
+// the parity build (trilinear interpolation == the k-polynomial) in a
+// different operation order with FMA contraction.  The depth bias seeds the
+// first octave; the early blank vote reads the last.  Returns whether any of
+// this thread's samples is at or below the iso-level.  Every compute thread
+// must call it.
+// ---- arithmetic shared by every fast-build noise path ---------------------
+// Only explicitly rounded operations (__fadd_rn, __fmul_rn, ...) and explicit
+// fmaf: the compiler cannot contract them differently in different kernels,
+// so the batched build and the sampling kernel produce the same samples.
+__device__ __forceinline__ float fade_fma(float t)
+{   // t^3 (t (6t - 15) + 10)
+    return __fmul_rn(__fmul_rn(__fmul_rn(t, t), t), fmaf(t, fmaf(t, 6.f, -15.f), 10.f));
+}
+
+// noise-space amplitude scale of the octave sum: 2/sqrt(3), divided by the
+// amplitude sum when normalised
+__device__ __forceinline__ float fbm_norm(const DevParams& p)
+{
+    if (!p.normalize) return kPerlinScale;
+    float mx = 0.f;
+    for (int k = 0; k < p.octaves; ++k) mx = __fadd_rn(mx, p.amp[k]);
+    return __fdiv_rn(kPerlinScale, mx);
+}
+
+// z-table entry of octave k at sample z: fraction, its fade, lattice cell
+__device__ __forceinline__ void z_entry(const DevParams& p, int k, int z, float s, float zoff, float& dz, float& fd,
+                                        int& cell)
+{
+    const float qz = __fmul_rn(fmaf((float)z, s, zoff), __fmul_rn(p.base_freq, p.mult[k]));
+    const float fz = floorf(qz);
+    dz = __fsub_rn(qz, fz);
+    fd = fade_fma(dz);
+    cell = (int)fz;
+}
+
+// depth bias at sample z
+__device__ __forceinline__ float z_bias(const DevParams& p, int z, float s, int oz)
+{
+    const float wz = fmaf((float)z, s, (float)oz);
+    if (p.bias_mode == UWW_BIAS_TERRACED) {
+        const float adj = __fdiv_rn(__fmul_rn(__fmul_rn(__fadd_rn(wz, p.offset[2]), p.base_freq), p.bias_a), p.bias_b);
+        return __fsub_rn(adj, fmodf(adj, p.bias_c));
+    }
+    if (p.bias_mode == UWW_BIAS_LINEAR) return __fmul_rn(p.bias_a, __fsub_rn(wz, p.bias_b));
+    return 0.f;
+}
+
+// noise coordinate of a column: (i s + o + offset) f
+__device__ __forceinline__ float column_coord(float i, float s, int o, float off, float f)
+{
+    return __fmul_rn(__fadd_rn(fmaf(i, s, (float)o), off), f);
+}
+
+// x/y part of one octave at one column: fractions, bilinear weights (times the
+// octave's amplitude), and the hashes of the four xy lattice corners
+struct ColumnOctave {
+    float dx, dy, dx1, dy1, w00, w01, w10, w11;
+    int h00, h01, h10, h11;
+};
+
+__device__ __forceinline__ ColumnOctave column_octave(const DevParams& p, const uint8_t* __restrict__ P, float nx,
+                                                      float ny, int k, float norm)
+{
+    ColumnOctave c;
+    const float m = p.mult[k], amp = __fmul_rn(p.amp[k], norm);
+    const float qx = __fmul_rn(nx, m), qy = __fmul_rn(ny, m);
+    const float fx = floorf(qx), fy = floorf(qy);
+    const int ix = (int)fx, iy = (int)fy;
+    c.dx = __fsub_rn(qx, fx);
+    c.dy = __fsub_rn(qy, fy);
+    c.dx1 = __fsub_rn(c.dx, 1.f);
+    c.dy1 = __fsub_rn(c.dy, 1.f);
+    const float a = fade_fma(c.dx), b = fade_fma(c.dy);
+    const float a0 = __fmul_rn(amp, __fsub_rn(1.f, a)), a1 = __fmul_rn(amp, a);
+    const float b0 = __fsub_rn(1.f, b);
+    c.w00 = __fmul_rn(a0, b0);
+    c.w10 = __fmul_rn(a1, b0);
+    c.w01 = __fmul_rn(a0, b);
+    c.w11 = __fmul_rn(a1, b);
+    const int hx0 = P[ix & 255], hx1 = P[(ix + 1) & 255];
+    c.h00 = P[hx0 ^ (iy & 255)];
+    c.h01 = P[hx0 ^ ((iy + 1) & 255)];
+    c.h10 = P[hx1 ^ (iy & 255)];
+    c.h11 = P[hx1 ^ ((iy + 1) & 255)];
+    return c;
+}
+
+// weighted face sums over the four xy corners of z lattice plane pl:
+// SA = sum w (g.xy . (d - o).xy), SG = sum w g.z
+__device__ __forceinline__ void column_face(const ColumnOctave& c, const float4* __restrict__ gp, int pl, float& SA,
+                                            float& SG)
+{
+    const float4 g00 = gp[c.h00 ^ pl], g01 = gp[c.h01 ^ pl], g10 = gp[c.h10 ^ pl], g11 = gp[c.h11 ^ pl];
+    SA = fmaf(c.w00, fmaf(g00.x, c.dx, __fmul_rn(g00.y, c.dy)),
+              fmaf(c.w01, fmaf(g01.x, c.dx, __fmul_rn(g01.y, c.dy1)),
+                   fmaf(c.w10, fmaf(g10.x, c.dx1, __fmul_rn(g10.y, c.dy)),
+                        __fmul_rn(c.w11, fmaf(g11.x, c.dx1, __fmul_rn(g11.y, c.dy1))))));
+    SG = fmaf(c.w00, g00.z, fmaf(c.w01, g01.z, fmaf(c.w10, g10.z, __fmul_rn(c.w11, g11.z))));
+}
+
+// a run's polynomial n(dz) = al + be dz + fade(dz) (ga + de dz) from the face
+// sums of its lower (0) and upper (1) planes, and its value at one sample
+struct RunPoly {
+    float al, be, ga, de;
+};
+__device__ __forceinline__ RunPoly run_poly(float SA0, float SG0, float SA1, float SG1)
+{
+    return {SA0, SG0, __fsub_rn(__fsub_rn(SA1, SG1), SA0), __fsub_rn(SG1, SG0)};
+}
+__device__ __forceinline__ float run_value(const RunPoly& q, float2 t)
+{
+    return fmaf(t.y, fmaf(q.de, t.x, q.ga), fmaf(q.be, t.x, q.al));
+}
+
+struct ZTable {
+    float2* dzc;   // [octave][z]: (dz, fade(dz))
+    int2* runs;    // [octave][run]: (first z, z lattice cell)
+    int* nruns;    // [octave]
+    float* bias;   // [z]
+};
+
+__device__ __forceinline__ ZTable ztable_at(uint8_t* base, int S, int octaves)
+{
+    ZTable t;
+    t.dzc = reinterpret_cast<float2*>(base);
+    t.runs = reinterpret_cast<int2*>(base + (size_t)octaves * S * sizeof(float2));
+    t.nruns = reinterpret_cast<int*>(base + (size_t)octaves * S * (sizeof(float2) + sizeof(int2)));
+    t.bias = reinterpret_cast<float*>(base + (size_t)octaves * S * (sizeof(float2) + sizeof(int2)) +
+                                      (size_t)octaves * sizeof(int));
+    return t;
+}
+
+__device__ __forceinline__ int sample_columns_fast(const DevParams& p, const uint8_t* __restrict__ P,
+                                                   const float4* __restrict__ gp, const ZTable Z,
+                                                   float* __restrict__ rho, int N, int ox, int oy, int oz,
+                                                   int ncomp)
+{
+    const int S = N + 1, SS = S * S, K = p.octaves;
+    const float s = __fdiv_rn((float)p.chunk_size, (float)N);
+    const float bf = p.base_freq;
+    const float norm = fbm_norm(p);
+    const float zoff = __fadd_rn((float)oz, p.offset[2]);
+    const float iso = p.iso_level;
+
+    // ---- per-chunk z tables, shared by every column ----
+    for (int i = threadIdx.x; i < K * S; i += ncomp) {
+        const int k = i / S, z = i - k * S;
+        float dz, fd;
+        int cell;
+        z_entry(p, k, z, s, zoff, dz, fd, cell);
+        Z.dzc[i] = make_float2(dz, fd);
+        reinterpret_cast<int*>(Z.runs)[2 * i + 1] = cell;  // staged: cell of sample z
+        if (k == 0) Z.bias[z] = z_bias(p, z, s, oz);
+    }
+    bar_sync(kBarCompute, ncomp);
+    // compact each octave's cells into runs (one thread per octave)
+    for (int k = threadIdx.x; k < K; k += ncomp) {
+        int2* r = Z.runs + k * S;
+        int n = 0, prev = 0;
+        for (int z = 0; z < S; ++z) {
+            const int iz = r[z].y;  // staged value; r[n] with n <= z is already consumed
+            if (z == 0 || iz != prev) r[n++] = make_int2(z, iz);
+            prev = iz;
+        }
+        Z.nruns[k] = n;
+    }
+    bar_sync(kBarCompute, ncomp);
+
+    int inside = 0;
+    for (int col = threadIdx.x; col < SS; col += ncomp) {
+        const int x = col / S, y = col - x * S;
+        float* out = rho + col * S;
+        const float nx = column_coord((float)x, s, ox, p.offset[0], bf);
+        const float ny = column_coord((float)y, s, oy, p.offset[1], bf);
+        for (int k = 0; k < K; ++k) {
+            const ColumnOctave co = column_octave(p, P, nx, ny, k, norm);
+            const float2* dzc = Z.dzc + k * S;
+            const int2* runs = Z.runs + k * S;
+            const int nr = Z.nruns[k];
+            const bool first = k == 0, last = k == K - 1;
+            // consecutive runs usually sit in consecutive z cells, whose shared
+            // plane is then read once (the condition is the same for every column)
+            float SA0 = 0.f, SG0 = 0.f, SA1 = 0.f, SG1 = 0.f;
+            int prev = 0;
+            for (int r = 0; r < nr; ++r) {
+                const int2 run = runs[r];
+                const int zb = run.x, ze = r + 1 < nr ? runs[r + 1].x : S;
+                if (r > 0 && run.y == prev + 1) {
+                    SA0 = SA1;
+                    SG0 = SG1;
+                } else {
+                    column_face(co, gp, run.y & 255, SA0, SG0);
+                }
+                column_face(co, gp, (run.y + 1) & 255, SA1, SG1);
+                prev = run.y;
+                const RunPoly q = run_poly(SA0, SG0, SA1, SG1);
+#pragma unroll 2
+                for (int z = zb; z < ze; ++z) {
+                    const float r0 = __fadd_rn(run_value(q, dzc[z]), first ? Z.bias[z] : out[z]);
+                    out[z] = r0;
+                    if (last) inside |= !(r0 > iso);
+                }
+            }
+        }
+    }
+    return inside;
+}
+
+
+}  // namespace
+}  // namespace uww
