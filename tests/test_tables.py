@@ -92,3 +92,26 @@ def test_edge_before_is_first_reference_order():
             seen = [e for e in order if owned >> e & 1]
             for k, e in enumerate(seen):
                 assert bin(owned & before[c][e]).count("1") == k
+
+
+def test_edge_owner_matches_first_sharing_cell():
+    """UWW_EDGE_OWNER[oriented][low flags][e] names the first cell in stream order
+    (inside the chunk, same orientation for oriented dedup) that holds edge e."""
+    _, _, _, _, share = tables()
+    owner = np.array(_array("UWW_EDGE_OWNER"), dtype=int).reshape(2, 8, 12)
+    for oriented in (0, 1):
+        for f in range(8):
+            lo = [bool(f & 1), bool(f & 2), bool(f & 4)]
+            for e in range(12):
+                want = None
+                for dx, dy, dz, e2, same in share[e]:
+                    if oriented and not same:
+                        continue
+                    d = (dx, dy, dz)
+                    if any((d[i] < 0 and lo[i]) for i in range(3)):
+                        continue
+                    want = (d, e2)
+                    break
+                o = owner[oriented][f][e]
+                got = ((-((o >> 4) & 1), -((o >> 5) & 1), -((o >> 6) & 1)), o & 15)
+                assert got == want, (oriented, f, e, got, want)

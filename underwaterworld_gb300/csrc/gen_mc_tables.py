@@ -34,6 +34,36 @@ def parse(src: str):
     return edges, rows
 
 
+def edge_owner(edges):
+    """[oriented dedup?][x==0 | y==0 << 1 | z==0 << 2][e] -> the cell that creates
+    the vertex of a cell's edge e: bits 0-3 its edge id e', bits 4/5/6 set when
+    it lies one cell back in x/y/z.  Only earlier cells (offsets -1 or 0) can
+    own an edge, so the low-side boundary flags decide."""
+    share = edge_share(edges)
+    out = []
+    for oriented in (0, 1):
+        row = []
+        for f in range(8):
+            lo = [bool(f & 1), bool(f & 2), bool(f & 4)]
+            ents = []
+            for e in range(12):
+                for dx, dy, dz, e2, same in share[e]:
+                    if oriented and not same:
+                        continue
+                    d = (dx, dy, dz)
+                    if any(d[i] > 0 for i in range(3)):
+                        continue
+                    if any(d[i] < 0 and lo[i] for i in range(3)):
+                        continue
+                    ents.append(e2 | ((dx < 0) << 4) | ((dy < 0) << 5) | ((dz < 0) << 6))
+                    break
+                else:
+                    raise AssertionError("every edge has an owner")
+            row.append(ents)
+        out.append(row)
+    return out
+
+
 def first_before(rows):
     out = []
     for r in rows:
@@ -172,6 +202,13 @@ def emit(edges, rows, ntri, emask) -> str:
             "UWW_TABLE_QUAL static const uint16_t UWW_OWNED_MASK[2][64] = {"]
     om = owned_masks(edges)
     out.append(",\n".join("    {" + ", ".join(f"0x{v:03x}" for v in r) + "}" for r in om))
+    out += ["};", "",
+            "// Owner of a cell's edge e by [oriented dedup][x==0 | y==0 << 1 | z==0 << 2]: bits 0-3 the",
+            "// owner's edge id, bits 4/5/6 the owner one cell back in x/y/z (derived from UWW_EDGE_SHARE).",
+            "UWW_TABLE_QUAL static const uint8_t UWW_EDGE_OWNER[2][8][12] = {"]
+    own = edge_owner(edges)
+    out.append(",\n".join("    {" + ", ".join("{" + ", ".join(f"0x{v:02x}" for v in r) + "}" for r in m) + "}"
+                          for m in own))
     out += ["};", "",
             "// Per case and edge e: mask of the edges the row references for the first time before",
             "// e's first reference (derived).  A cell numbers the vertices of its owned edges in",

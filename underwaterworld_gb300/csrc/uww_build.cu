@@ -83,7 +83,7 @@ struct SmemTables {
     uint16_t edges[256];
     uint8_t ntri[256];
     uint8_t perm[256];
-    int8_t share[12][4][5];
+    uint8_t owner[2][8][12];      // UWW_EDGE_OWNER
     uint8_t corners[12][2];
     uint16_t owned[2][64];        // [oriented?][boundary flags] -> owned edge mask
     unsigned long long warp_sums[32];
@@ -103,23 +103,6 @@ __device__ __forceinline__ int boundary_flags(int x, int y, int z, int N)
            ((z == N - 1) << 5);
 }
 
-// First cell (in stream order) holding edge e of cell (x,y,z) -- with the same
-// orientation when `oriented` -- and that cell's local edge id.
-__device__ __forceinline__ int find_owner(const SmemTables& T, int e, int x, int y, int z, int N, bool oriented,
-                                          int& ox, int& oy, int& oz)
-{
-#pragma unroll
-    for (int c = 0; c < 4; ++c) {
-        const int8_t* s = T.share[e][c];
-        if (oriented && !s[4]) continue;
-        const int cx = x + s[0], cy = y + s[1], cz = z + s[2];
-        if (cx < 0 || cy < 0 || cz < 0 || cx >= N || cy >= N || cz >= N) continue;
-        ox = cx; oy = cy; oz = cz;
-        return s[3];
-    }
-    ox = x; oy = y; oz = z;  // unreachable: the cell itself is always a candidate
-    return e;
-}
 
 // ---------------------------------------------------------------------------
 // The look-back words carry their own payload (no other data is published
@@ -550,7 +533,7 @@ __device__ void chunk_emit(const DevParams& p, const BuildArgs& a, SmemTables& T
                         const float ibv = rho[(bx * S + by) * S + bz];
                         const float sax = O::mul((float)ax, s), say = O::mul((float)ay, s), saz = O::mul((float)az, s);
                         const float sbx = O::mul((float)bx, s), sby = O::mul((float)by, s), sbz = O::mul((float)bz, s);
-                        const float t = __fdiv_rn(O::sub(iso, ia), O::sub(ibv, ia));
+                        const float t = O::div(O::sub(iso, ia), O::sub(ibv, ia));
                         const float mx = O::add(sax, O::mul(t, O::sub(sbx, sax)));
                         const float my = O::add(say, O::mul(t, O::sub(sby, say)));
                         const float mz = O::add(saz, O::mul(t, O::sub(sbz, saz)));
@@ -567,8 +550,10 @@ __device__ void chunk_emit(const DevParams& p, const BuildArgs& a, SmemTables& T
                         v2[2] = make_float2(0.f, 0.f);
                     }
                 } else {
-                    int qx, qy, qz;
-                    const int oe = find_owner(T, e, x, y, z, N, oriented, qx, qy, qz);
+                    // the owner: the first cell in stream order holding this edge
+                    const int ow = T.owner[oriented][(x == 0) | ((y == 0) << 1) | ((z == 0) << 2)][e];
+                    const int qx = x - ((ow >> 4) & 1), qy = y - ((ow >> 5) & 1), qz = z - ((ow >> 6) & 1);
+                    const int oe = ow & 15;
                     const int oc = (qx * N + qy) * N + qz;
                     const unsigned oown = T.owned[oriented][boundary_flags(qx, qy, qz, N)];
                     id = W.get_vbase(oc) + __popc(oown & __ldg(&UWW_EDGE_BEFORE[cases[oc]][oe]));
@@ -625,7 +610,7 @@ __global__ void __launch_bounds__(MAXT, MINB) build_kernel(const DevParams p, co
     // the permutation arrives in the parameter (constant) bank: read it as words
     for (int i = tid; i < 64; i += nthr) reinterpret_cast<uint32_t*>(T.perm)[i] = reinterpret_cast<const uint32_t*>(p.perm)[i];
     for (int i = tid; i < 128; i += nthr) (&T.owned[0][0])[i] = __ldg(&UWW_OWNED_MASK[0][0] + i);
-    for (int i = tid; i < 12 * 4 * 5; i += nthr) (&T.share[0][0][0])[i] = __ldg(&UWW_EDGE_SHARE[0][0][0] + i);
+    for (int i = tid; i < 2 * 8 * 12; i += nthr) (&T.owner[0][0][0])[i] = __ldg(&UWW_EDGE_OWNER[0][0][0] + i);
     for (int i = tid; i < 24; i += nthr) (&T.corners[0][0])[i] = __ldg(&UWW_EDGE_CORNERS[0][0] + i);
     __syncthreads();
     for (int i = tid; i < 256; i += nthr) {

@@ -6,7 +6,9 @@
 //               (__fadd_rn/__fsub_rn/__fmul_rn are never contracted to FMA),
 //               in the reference's operation order.  This is the parity build.
 //   FastOps  -- plain operators; nvcc contracts them to FMA (fast build).
-// Division, sqrt, floor and fmod are IEEE-exact in both.
+// sqrt, floor and fmod are IEEE-exact in both; division is IEEE in the parity
+// build and the hardware approximate quotient (O::div) in the fast build's
+// edge interpolation.
 //
 // Reference: perlin_util.rs:6-29 (fBm + terraced bias), the noise 0.8.2
 // crate's perlin_3d behind noise::Perlin::get (perlin_util.rs:13), and the
@@ -44,12 +46,15 @@ struct ExactOps {
     static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
     static __device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
     static __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+    static __device__ __forceinline__ float div(float a, float b) { return __fdiv_rn(a, b); }
 };
 
 struct FastOps {
     static __device__ __forceinline__ float add(float a, float b) { return a + b; }
     static __device__ __forceinline__ float sub(float a, float b) { return a - b; }
     static __device__ __forceinline__ float mul(float a, float b) { return a * b; }
+    // the hardware reciprocal-based quotient (about 2 ulp), for |b| < 2^126
+    static __device__ __forceinline__ float div(float a, float b) { return __fdividef(a, b); }
 };
 
 // Gradient table of the noise crate: 16 entries over the 12 cube-edge
