@@ -319,6 +319,44 @@ int uww_sample_chunks(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, 
 /* UWW_ERRFLAG_BAD / UWW_ERRFLAG_RANGE raised by the last uww_sample_chunks (synchronises). */
 int uww_sample_status(uww_ctx* ctx, uint32_t* flags);
 
+/* ---- queries against built chunks ---------------------------------------------- */
+/* Per-cell triangle ranges for Chunk::tris_around (chunk.rs:315-342): for every
+ * cell of every chunk, the chunk-local position in the index buffer of its first
+ * triangle (cells are emitted in stream order, 3 * ntri(case) indices each),
+ * written at d_first + desc.cell_offset from the build's cases (UWW_OUT_CASES).
+ * A chunk whose cells lie outside case_capacity is skipped and flagged
+ * (uww_sample_status). */
+int uww_cell_tri_offsets(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, const uint8_t* d_cases,
+                         uint64_t case_capacity, uint32_t* d_first);
+
+/* Device index of chunk positions (World::get_chunk, world.rs:89-91): an open-
+ * addressing table of table_size (a power of two >= n) u32 slots holding
+ * chunk index + 1.  A position that appears twice keeps one of its chunks. */
+int uww_chunk_index(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint32_t* d_table, uint32_t table_size);
+
+/* A built batch, as the ray query reads it (all device pointers, one build). */
+typedef struct uww_ray_scene {
+    const uww_chunk_desc*   chunks;
+    const uww_chunk_record* records;
+    const uww_vert_color*   verts;
+    const uint32_t*         inds;
+    const uint8_t*          cases;       /* UWW_OUT_CASES of the build                */
+    const uint32_t*         cell_first;  /* uww_cell_tri_offsets of those cases        */
+    const uint32_t*         table;       /* uww_chunk_index of the chunks              */
+    uint32_t                n;
+    uint32_t                table_size;
+} uww_ray_scene;
+
+/* The boids' wall-avoidance ray casts (boid.rs:175-244), batched: for query q
+ * at d_origins[q] (world xyz) and its nrays (<= 32) directions d_dirs[q][k],
+ * the triangles of the cells within `range` cells of the point
+ * (Chunk::tris_around) in every chunk within `range` world units
+ * (boid.rs:176-207) are cast against each ray with util::Tri::intersects
+ * (util.rs:23-58, max distance `range`); d_t[q][k] = the nearest hit distance,
+ * or -1.  f32 with the reference's operation order (no FMA). */
+int uww_ray_query(uww_ctx* ctx, const uww_ray_scene* scene, const float* d_origins, uint32_t nq, const float* d_dirs,
+                  uint32_t nrays, int32_t range, float* d_t);
+
 /* ---- point queries ------------------------------------------------------------ */
 /* density(world xyz) for n points: perlin_util::iso_at (perlin_util.rs:24-29) with
  * (x,y,z) = world / CHUNK_SIZE as in boid.rs:132-137.  d_xyz: 3n floats; d_out: n. */

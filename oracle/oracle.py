@@ -51,6 +51,11 @@ def lib():
         L.oracle_perlin.restype = C.c_int
         L.oracle_adjoint64.argtypes = [C.POINTER(abi.Params), P, P, C.c_uint32, P, P, P, P, P, P, P, P, P, P]
         L.oracle_adjoint64.restype = C.c_int
+        L.oracle_cell_tri_offsets.argtypes = [P, C.c_uint32, P, P]
+        L.oracle_cell_tri_offsets.restype = C.c_int
+        L.oracle_ray_query.argtypes = [C.POINTER(abi.Params), P, C.c_uint32, P, P, P, P, P, C.c_uint32, P,
+                                       C.c_uint32, C.c_int32, P]
+        L.oracle_ray_query.restype = C.c_int
         _lib = L
     return _lib
 
@@ -224,3 +229,32 @@ def crossing_edges(params: abi.Params, descs: np.ndarray, samples: np.ndarray):
         ids.append(e)
         off += e.size
     return recs, (np.concatenate(ids) if ids else np.zeros(0, np.uint32))
+
+
+# ---- queries against built chunks ------------------------------------------------
+def cell_tri_offsets(descs: np.ndarray, cases: np.ndarray) -> np.ndarray:
+    descs = np.ascontiguousarray(descs, dtype=abi.CHUNK_DESC_DTYPE)
+    cases = np.ascontiguousarray(cases, dtype=np.uint8)
+    first = np.zeros(cases.size, np.uint32)
+    lib().oracle_cell_tri_offsets(descs.ctypes.data, descs.shape[0], cases.ctypes.data, first.ctypes.data)
+    return first
+
+
+def ray_query(params: abi.Params, descs, batch: MeshBatch, origins: np.ndarray, dirs: np.ndarray, rng: int):
+    """Nearest hit per (query, ray) against the triangles around each query point."""
+    descs = np.ascontiguousarray(descs, dtype=abi.CHUNK_DESC_DTYPE)
+    origins = np.ascontiguousarray(origins, dtype=np.float32).reshape(-1, 3)
+    nq = origins.shape[0]
+    dirs = np.ascontiguousarray(dirs, dtype=np.float32).reshape(nq, -1, 3)
+    nr = dirs.shape[1]
+    out = np.zeros((nq, nr), np.float32)
+    recs = np.ascontiguousarray(batch.records)
+    verts = np.ascontiguousarray(batch.verts)
+    inds = np.ascontiguousarray(batch.inds)
+    cases = np.ascontiguousarray(batch.cases)
+    st = lib().oracle_ray_query(C.byref(params), descs.ctypes.data, descs.shape[0], recs.ctypes.data, verts.ctypes.data,
+                                inds.ctypes.data, cases.ctypes.data, origins.ctypes.data, nq, dirs.ctypes.data, nr,
+                                rng, out.ctypes.data)
+    if st:
+        raise RuntimeError(f"oracle_ray_query failed: {st}")
+    return out

@@ -42,6 +42,12 @@ int    oracle_adjoint64(const uww_params* p, const double* theta, const uww_chun
                         const uww_chunk_record* records, const uint32_t* edge_ids, const float* pos_grad,
                         const double* samples_in, double* loss, double* theta_grad, double* sample_grad,
                         double* positions, double* dmax, double* pole);
+/* uww_oracle_query.c: per-cell first index from the cases, and the boids'
+ * wall-avoidance ray casts (nearest hit per ray, -1 when none). */
+int    oracle_cell_tri_offsets(const uww_chunk_desc* chunks, uint32_t n, const uint8_t* cases, uint32_t* first);
+int    oracle_ray_query(const uww_params* p, const uww_chunk_desc* chunks, uint32_t n, const uww_chunk_record* records,
+                        const uww_vert_color* verts, const uint32_t* inds, const uint8_t* cases, const float* origins,
+                        uint32_t nq, const float* dirs, uint32_t nrays, int32_t range, float* out);
 double oracle_density64_full(const uww_params* p, const uint8_t* P, double wx, double wy, double wz,
                              double* grad);
 

@@ -1,0 +1,146 @@
+/*
+ * uww_oracle_query.c -- CPU restatement of the queries against built chunks
+ * (uww_cell_tri_offsets / uww_ray_query of libuww_gb300.so).
+ * TEST INFRASTRUCTURE ONLY: the product never links this file.
+ *
+ * Follows, in f32 with every operation separately rounded (the Makefile
+ * builds with -ffp-contract=off; Rust's cgmath does not fuse either):
+ *   boid.rs:175-207   the chunk window around a boid and the local position
+ *                     handed to tris_around;
+ *   chunk.rs:315-342  Chunk::tris_around, the cells within `range` of it;
+ *   util.rs:12-21     Tri::new, face normal safe_normalize((b-a) x (c-a));
+ *   util.rs:23-58     Tri::intersects, the hit distance along a ray.
+ * A cell's triangles are the build's indices 3*ntri(case) at the cell's
+ * running offset in stream order (the order build_mesh visits cells,
+ * chunk.rs:135-264).  The nearest hit per ray is what boid.rs:209-244 needs:
+ * it tests "some hit closer than the range" and "no hit within the range".
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "uww.h"
+#include "mc_tables.h"
+#include "uww_oracle.h"
+
+typedef struct {
+    float x, y, z;
+} v3;
+
+static v3 sub3(v3 a, v3 b) { v3 r = {a.x - b.x, a.y - b.y, a.z - b.z}; return r; }
+static float dot3(v3 a, v3 b)
+{
+    float r = a.x * b.x;
+    r = r + a.y * b.y;
+    return r + a.z * b.z;
+}
+static v3 cross3(v3 a, v3 b)
+{
+    v3 r = {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+    return r;
+}
+
+/* util.rs:23-58 */
+static float tri_intersects(v3 a, v3 b, v3 c, v3 n, v3 o, v3 d, float range)
+{
+    const float dn = dot3(n, d);
+    if (fabsf(dn) < 1e-5f) return -1.f;
+    const float t = dot3(n, sub3(a, o)) / dn;
+    if (t < 0.f || t > range) return -1.f;
+    v3 p = {o.x + d.x * t, o.y + d.y * t, o.z + d.z * t};
+    const float d0 = dot3(cross3(sub3(b, a), sub3(p, a)), n);
+    const float d1 = dot3(cross3(sub3(c, b), sub3(p, b)), n);
+    const float d2 = dot3(cross3(sub3(a, c), sub3(p, c)), n);
+    if (d0 >= 0.f && d1 >= 0.f && d2 >= 0.f) return t == 0.f ? 0.f : t;
+    return -1.f;
+}
+
+int oracle_cell_tri_offsets(const uww_chunk_desc* chunks, uint32_t n, const uint8_t* cases, uint32_t* first)
+{
+    for (uint32_t c = 0; c < n; ++c) {
+        const uint64_t NC = (uint64_t)chunks[c].cells * chunks[c].cells * chunks[c].cells;
+        uint32_t run = 0;
+        for (uint64_t i = 0; i < NC; ++i) {
+            first[chunks[c].cell_offset + i] = run;
+            run += 3u * UWW_CASE_NTRI[cases[chunks[c].cell_offset + i]];
+        }
+    }
+    return UWW_OK;
+}
+
+int oracle_ray_query(const uww_params* p, const uww_chunk_desc* chunks, uint32_t n, const uww_chunk_record* records,
+                     const uww_vert_color* verts, const uint32_t* inds, const uint8_t* cases, const float* origins,
+                     uint32_t nq, const float* dirs, uint32_t nrays, int32_t range, float* out)
+{
+    const float cs = (float)p->chunk_size, rf = (float)range;
+    uint32_t* first = NULL;
+    uint64_t total = 0;
+    for (uint32_t c = 0; c < n; ++c) {
+        const uint64_t e = chunks[c].cell_offset + (uint64_t)chunks[c].cells * chunks[c].cells * chunks[c].cells;
+        if (e > total) total = e;
+    }
+    first = (uint32_t*)malloc((size_t)(total ? total : 1) * sizeof(uint32_t));
+    if (!first) return UWW_ERR_OOM;
+    oracle_cell_tri_offsets(chunks, n, cases, first);
+    for (uint32_t q = 0; q < nq; ++q) {
+        const v3 o = {origins[3 * q], origins[3 * q + 1], origins[3 * q + 2]};
+        for (uint32_t k = 0; k < nrays; ++k) out[(size_t)q * nrays + k] = -1.f;
+        /* boid.rs:176-182 */
+        const int sx = (int)floorf((o.x - rf) / cs), ex = (int)floorf((o.x + rf) / cs);
+        const int sy = (int)floorf((o.y - rf) / cs), ey = (int)floorf((o.y + rf) / cs);
+        const int sz = (int)floorf((o.z - rf) / cs), ez = (int)floorf((o.z + rf) / cs);
+        for (int a = sx; a <= ex; ++a)
+            for (int b = sy; b <= ey; ++b)
+                for (int cz = sz; cz <= ez; ++cz) {
+                    int ci = -1; /* World::get_chunk */
+                    for (uint32_t i = 0; i < n; ++i)
+                        if (chunks[i].pos[0] == a && chunks[i].pos[1] == b && chunks[i].pos[2] == cz) { ci = (int)i; break; }
+                    if (ci < 0) continue;
+                    const uww_chunk_desc* d = &chunks[ci];
+                    const uww_chunk_record* r = &records[ci];
+                    if (!(r->flags & UWW_CHUNK_HAS_MESH) || (r->flags & UWW_CHUNK_OVERFLOW)) continue;
+                    const int N = (int)d->cells;
+                    const float nf = (float)N;
+                    /* boid.rs:185-204: local position as a fraction of the chunk */
+                    const float px = (o.x - (float)a * cs) / cs;
+                    const float py = (o.y - (float)b * cs) / cs;
+                    const float pz = (o.z - (float)cz * cs) / cs;
+                    /* chunk.rs:316-326 */
+                    const int mx = (int)floorf(px * nf), my = (int)floorf(py * nf), mz = (int)floorf(pz * nf);
+                    const int x0 = mx - range > 0 ? mx - range : 0, y0 = my - range > 0 ? my - range : 0,
+                              z0 = mz - range > 0 ? mz - range : 0;
+                    const int x1 = mx + range < N - 1 ? mx + range : N - 1, y1 = my + range < N - 1 ? my + range : N - 1,
+                              z1 = mz + range < N - 1 ? mz + range : N - 1;
+                    for (int x = x0; x <= x1; ++x)
+                        for (int y = y0; y <= y1; ++y)
+                            for (int z = z0; z <= z1; ++z) {
+                                const uint32_t cell = d->cell_offset + (uint32_t)((x * N + y) * N + z);
+                                const int nt = UWW_CASE_NTRI[cases[cell]];
+                                const uint32_t f = r->ind_offset + first[cell];
+                                for (int j = 0; j < nt; ++j) {
+                                    v3 vv[3];
+                                    for (int m = 0; m < 3; ++m) {
+                                        const uww_vert_color* vc = &verts[r->vert_offset + inds[f + 3 * j + m]];
+                                        vv[m].x = vc->pos[0];
+                                        vv[m].y = vc->pos[1];
+                                        vv[m].z = vc->pos[2];
+                                    }
+                                    /* util.rs:12-21 */
+                                    v3 nn = cross3(sub3(vv[1], vv[0]), sub3(vv[2], vv[0]));
+                                    const float mag = sqrtf(dot3(nn, nn));
+                                    if (mag != 0.f) { nn.x = nn.x / mag; nn.y = nn.y / mag; nn.z = nn.z / mag; }
+                                    for (uint32_t k = 0; k < nrays; ++k) {
+                                        const size_t di = 3 * ((size_t)q * nrays + k);
+                                        const v3 dir = {dirs[di], dirs[di + 1], dirs[di + 2]};
+                                        const float t = tri_intersects(vv[0], vv[1], vv[2], nn, o, dir, rf);
+                                        float* best = &out[(size_t)q * nrays + k];
+                                        if (t >= 0.f && (*best < 0.f || t < *best)) *best = t;
+                                    }
+                                }
+                            }
+                }
+    }
+    free(first);
+    return UWW_OK;
+}

@@ -63,6 +63,12 @@ class MeshOut(C.Structure):
                 ("case_capacity", C.c_uint64), ("sample_capacity", C.c_uint64)]
 
 
+class RayScene(C.Structure):
+    _fields_ = [("chunks", C.c_void_p), ("records", C.c_void_p), ("verts", C.c_void_p), ("inds", C.c_void_p),
+                ("cases", C.c_void_p), ("cell_first", C.c_void_p), ("table", C.c_void_p), ("n", C.c_uint32),
+                ("table_size", C.c_uint32)]
+
+
 class Tuning(C.Structure):
     _fields_ = [("threads", C.c_int32), ("blocks_per_sm", C.c_int32), ("smem_cells", C.c_int32),
                 ("reserved", C.c_int32)]
@@ -120,6 +126,9 @@ _SIGS = {
     "uww_frame_destroy": (C.c_int, [P]),
     "uww_sample_chunks": (C.c_int, [P, P, C.c_uint32, C.c_uint32, P, C.c_uint64]),
     "uww_sample_status": (C.c_int, [P, C.POINTER(C.c_uint32)]),
+    "uww_cell_tri_offsets": (C.c_int, [P, P, C.c_uint32, P, C.c_uint64, P]),
+    "uww_chunk_index": (C.c_int, [P, P, C.c_uint32, P, C.c_uint32]),
+    "uww_ray_query": (C.c_int, [P, C.POINTER(RayScene), P, C.c_uint32, P, C.c_uint32, C.c_int32, P]),
     "uww_forward": (C.c_int, [P, P, C.c_uint32, C.c_uint32, C.POINTER(MeshOut), P]),
     "uww_backward": (C.c_int, [P, P, C.c_uint32, C.c_uint32, P, P, P, P, P, C.c_uint64]),
     "uww_height_loss": (C.c_int, [P, P, P, C.c_uint32, C.c_float, C.c_float, C.c_float, C.c_uint32, C.c_uint32,
