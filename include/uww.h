@@ -357,6 +357,37 @@ typedef struct uww_ray_scene {
 int uww_ray_query(uww_ctx* ctx, const uww_ray_scene* scene, const float* d_origins, uint32_t nq, const float* d_dirs,
                   uint32_t nrays, int32_t range, float* d_t);
 
+/* ---- the chunk scheduler's feed ------------------------------------------------- */
+/* World::update_nearby (world.rs:148-234) on the GPU: every chunk position in
+ * the box around the sub (x, y in sub_chunk +- generation_dist, z clamped to
+ * [min_z, max_z]) within generation_dist chunk lengths of sub_pos is tested
+ * against the two frusta (util::in_frustum, util.rs:77-85: clip = M (p, 1),
+ * divide by w, |x|, |y| <= 1, 0 <= z <= 1; M column-major as cgmath's, the
+ * camera's chunk_generation_frustum_matrix).  A position with a known chunk
+ * (d_known_table: uww_chunk_index of d_known, NULL for none) that has a mesh,
+ * lies within view_dist chunk lengths and is in the view frustum goes to
+ * d_render (x, y, z triples, loop order); an unknown one goes to d_generate as
+ * a descriptor of `cells` cells (offsets laid out as uww_layout_cells), in
+ * GenPrio order (world.rs:33-58): in view first, then in the generation
+ * frustum, then ascending dist^2 + z, ties by loop order -- the order the
+ * batched build's work queue takes, so in-view chunks finish first.
+ * d_counts[0], [1]: the lists' true lengths (entries beyond the capacities are
+ * not written).  At most 4096 candidate positions. */
+typedef struct uww_schedule_params {
+    float    sub_pos[3];
+    int32_t  sub_chunk[3];
+    float    view_proj[16];      /* VIEW_FRUST_FOVY matrix (world.rs:16)      */
+    float    gen_proj[16];       /* GENERATE_FRUST_FOVY matrix (world.rs:17)  */
+    int32_t  generation_dist;    /* GENERATION_DIST = 5 (world.rs:9)          */
+    int32_t  view_dist;          /* VIEW_DIST = 4 (world.rs:8)                */
+    int32_t  min_z, max_z;       /* world::MIN_Z, MAX_Z (world.rs:11-12)      */
+    uint32_t cells;              /* cells per edge of the generated chunks    */
+} uww_schedule_params;
+int uww_schedule_chunks(uww_ctx* ctx, const uww_schedule_params* sp, const uww_chunk_desc* d_known,
+                        const uww_chunk_record* d_known_records, const uint32_t* d_known_table,
+                        uint32_t known_table_size, uww_chunk_desc* d_generate, uint32_t generate_capacity,
+                        int32_t* d_render, uint32_t render_capacity, uint32_t* d_counts);
+
 /* ---- point queries ------------------------------------------------------------ */
 /* density(world xyz) for n points: perlin_util::iso_at (perlin_util.rs:24-29) with
  * (x,y,z) = world / CHUNK_SIZE as in boid.rs:132-137.  d_xyz: 3n floats; d_out: n. */

@@ -56,6 +56,9 @@ def lib():
         L.oracle_ray_query.argtypes = [C.POINTER(abi.Params), P, C.c_uint32, P, P, P, P, P, C.c_uint32, P,
                                        C.c_uint32, C.c_int32, P]
         L.oracle_ray_query.restype = C.c_int
+        L.oracle_schedule_chunks.argtypes = [C.POINTER(abi.Params), C.POINTER(abi.ScheduleParams), P, P, C.c_uint32,
+                                             P, C.c_uint32, P, C.c_uint32, P]
+        L.oracle_schedule_chunks.restype = C.c_int
         _lib = L
     return _lib
 
@@ -258,3 +261,19 @@ def ray_query(params: abi.Params, descs, batch: MeshBatch, origins: np.ndarray, 
     if st:
         raise RuntimeError(f"oracle_ray_query failed: {st}")
     return out
+
+
+def schedule_chunks(params: abi.Params, sp, known_descs=None, known_records=None, cap: int = 4096):
+    """World::update_nearby: (generation list descriptors in GenPrio order, render list (m, 3))."""
+    n_known = 0 if known_descs is None else len(known_descs)
+    kd = np.ascontiguousarray(known_descs if n_known else np.zeros(1, abi.CHUNK_DESC_DTYPE), dtype=abi.CHUNK_DESC_DTYPE)
+    kr = np.ascontiguousarray(known_records if n_known else np.zeros(1, abi.CHUNK_RECORD_DTYPE),
+                              dtype=abi.CHUNK_RECORD_DTYPE)
+    gen = np.zeros(cap, abi.CHUNK_DESC_DTYPE)
+    ren = np.zeros((cap, 3), np.int32)
+    counts = np.zeros(2, np.uint32)
+    st = lib().oracle_schedule_chunks(C.byref(params), C.byref(sp), kd.ctypes.data, kr.ctypes.data, n_known,
+                                      gen.ctypes.data, cap, ren.ctypes.data, cap, counts.ctypes.data)
+    if st:
+        raise RuntimeError(f"oracle_schedule_chunks failed: {st}")
+    return gen[:counts[0]], ren[:counts[1]]

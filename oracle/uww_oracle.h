@@ -48,6 +48,9 @@ int    oracle_cell_tri_offsets(const uww_chunk_desc* chunks, uint32_t n, const u
 int    oracle_ray_query(const uww_params* p, const uww_chunk_desc* chunks, uint32_t n, const uww_chunk_record* records,
                         const uww_vert_color* verts, const uint32_t* inds, const uint8_t* cases, const float* origins,
                         uint32_t nq, const float* dirs, uint32_t nrays, int32_t range, float* out);
+int    oracle_schedule_chunks(const uww_params* p, const uww_schedule_params* sp, const uww_chunk_desc* known,
+                              const uww_chunk_record* known_records, uint32_t n_known, uww_chunk_desc* gen_out,
+                              uint32_t gen_cap, int32_t* render_out, uint32_t render_cap, uint32_t* counts);
 double oracle_density64_full(const uww_params* p, const uint8_t* P, double wx, double wy, double wz,
                              double* grad);
 

@@ -144,3 +144,112 @@ int oracle_ray_query(const uww_params* p, const uww_chunk_desc* chunks, uint32_t
     free(first);
     return UWW_OK;
 }
+
+/* ---- World::update_nearby (world.rs:148-234) ---------------------------------- */
+static int in_frustum_f(const float* m, float x, float y, float z)
+{
+    float c[4];
+    for (int i = 0; i < 4; ++i) {
+        float r = m[i] * x;
+        r = r + m[4 + i] * y;
+        r = r + m[8 + i] * z;
+        c[i] = r + m[12 + i] * 1.0f;
+    }
+    const float w = c[3];
+    const float cx = c[0] / w, cy = c[1] / w, cz = c[2] / w;
+    return fabsf(cx) <= 1.0f && fabsf(cy) <= 1.0f && cz >= 0.0f && cz <= 1.0f;
+}
+
+typedef struct {
+    int cls;
+    float prio;
+    int idx;
+} gen_entry;
+
+static int gen_cmp(const void* a, const void* b)
+{
+    const gen_entry* x = (const gen_entry*)a;
+    const gen_entry* y = (const gen_entry*)b;
+    if (x->cls != y->cls) return x->cls < y->cls ? -1 : 1;
+    if (x->prio != y->prio) return x->prio < y->prio ? -1 : 1;
+    return x->idx < y->idx ? -1 : (x->idx > y->idx);
+}
+
+int oracle_schedule_chunks(const uww_params* p, const uww_schedule_params* sp, const uww_chunk_desc* known,
+                           const uww_chunk_record* known_records, uint32_t n_known, uww_chunk_desc* gen_out,
+                           uint32_t gen_cap, int32_t* render_out, uint32_t render_cap, uint32_t* counts)
+{
+    const int G = sp->generation_dist;
+    const int sz = sp->sub_chunk[2] - G > sp->min_z ? sp->sub_chunk[2] - G : sp->min_z;
+    const int ez = sp->sub_chunk[2] + G < sp->max_z ? sp->sub_chunk[2] + G : sp->max_z;
+    const int nz = ez - sz + 1 > 0 ? ez - sz + 1 : 0;
+    const float cs = (float)p->chunk_size;
+    const float max_view = (float)sp->view_dist * cs, max_gen = (float)G * cs;
+    const int total = 4 * G * G * nz;
+    gen_entry* gens = (gen_entry*)malloc((size_t)(total ? total : 1) * sizeof(gen_entry));
+    if (!gens) return UWW_ERR_OOM;
+    uint32_t ng = 0, nr = 0;
+    int i = 0;
+    for (int x = -G; x < G; ++x)
+        for (int y = -G; y < G; ++y)
+            for (int z = sz; z <= ez; ++z, ++i) {
+                const int cx = sp->sub_chunk[0] + x, cy = sp->sub_chunk[1] + y;
+                const float mx = ((float)cx + 0.5f) * cs, my = ((float)cy + 0.5f) * cs, mz = ((float)z + 0.5f) * cs;
+                const float dx = sp->sub_pos[0] - mx, dy = sp->sub_pos[1] - my, dz = sp->sub_pos[2] - mz;
+                float d2 = dx * dx;
+                d2 = d2 + dy * dy;
+                d2 = d2 + dz * dz;
+                const float dist = sqrtf(d2);
+                if (dist > max_gen) continue;
+                int in_view = 0, in_gen = 0;
+                static const float corners[8][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {1, 1, 0},
+                                                    {0, 0, 1}, {1, 0, 1}, {0, 1, 1}, {1, 1, 1}};
+                for (int k = 0; k < 8; ++k) {
+                    const float px = ((float)cx + corners[k][0]) * cs, py = ((float)cy + corners[k][1]) * cs,
+                                pz = ((float)z + corners[k][2]) * cs;
+                    if (in_frustum_f(sp->gen_proj, px, py, pz)) {
+                        in_gen = 1;
+                        if (in_frustum_f(sp->view_proj, px, py, pz)) { in_view = 1; break; }
+                    }
+                }
+                int kc = -1; /* World::get_chunk */
+                for (uint32_t j = 0; j < n_known; ++j)
+                    if (known[j].pos[0] == cx && known[j].pos[1] == cy && known[j].pos[2] == z) { kc = (int)j; break; }
+                if (kc >= 0) {
+                    const int not_blank = (known_records[kc].flags & UWW_CHUNK_HAS_MESH) != 0;
+                    if (dist < max_view && not_blank && in_view) {
+                        if (nr < render_cap) {
+                            render_out[3 * nr] = cx;
+                            render_out[3 * nr + 1] = cy;
+                            render_out[3 * nr + 2] = z;
+                        }
+                        ++nr;
+                    }
+                } else {
+                    gens[ng].cls = in_view ? 0 : in_gen ? 1 : 2;
+                    gens[ng].prio = dist * dist + (float)z * cs;
+                    gens[ng].idx = i;
+                    ++ng;
+                }
+            }
+    /* GenPrio order: the reference sorts descending and pops from the end */
+    qsort(gens, ng, sizeof(gen_entry), gen_cmp);
+    const uint32_t cells = sp->cells, nc = cells * cells * cells, ns = (cells + 1) * (cells + 1) * (cells + 1);
+    for (uint32_t r = 0; r < ng && r < gen_cap; ++r) {
+        const int idx = gens[r].idx;
+        const int xi = idx / (2 * G * nz), yi = (idx / nz) % (2 * G), zi = idx % nz;
+        uww_chunk_desc d;
+        memset(&d, 0, sizeof(d));
+        d.pos[0] = sp->sub_chunk[0] - G + xi;
+        d.pos[1] = sp->sub_chunk[1] - G + yi;
+        d.pos[2] = sz + zi;
+        d.cells = cells;
+        d.cell_offset = r * nc;
+        d.sample_offset = r * ns;
+        gen_out[r] = d;
+    }
+    counts[0] = ng;
+    counts[1] = nr;
+    free(gens);
+    return UWW_OK;
+}

@@ -69,6 +69,12 @@ class RayScene(C.Structure):
                 ("table_size", C.c_uint32)]
 
 
+class ScheduleParams(C.Structure):
+    _fields_ = [("sub_pos", C.c_float * 3), ("sub_chunk", C.c_int32 * 3), ("view_proj", C.c_float * 16),
+                ("gen_proj", C.c_float * 16), ("generation_dist", C.c_int32), ("view_dist", C.c_int32),
+                ("min_z", C.c_int32), ("max_z", C.c_int32), ("cells", C.c_uint32)]
+
+
 class Tuning(C.Structure):
     _fields_ = [("threads", C.c_int32), ("blocks_per_sm", C.c_int32), ("smem_cells", C.c_int32),
                 ("reserved", C.c_int32)]
@@ -129,6 +135,8 @@ _SIGS = {
     "uww_cell_tri_offsets": (C.c_int, [P, P, C.c_uint32, P, C.c_uint64, P]),
     "uww_chunk_index": (C.c_int, [P, P, C.c_uint32, P, C.c_uint32]),
     "uww_ray_query": (C.c_int, [P, C.POINTER(RayScene), P, C.c_uint32, P, C.c_uint32, C.c_int32, P]),
+    "uww_schedule_chunks": (C.c_int, [P, C.POINTER(ScheduleParams), P, P, P, C.c_uint32, P, C.c_uint32, P,
+                                      C.c_uint32, P]),
     "uww_forward": (C.c_int, [P, P, C.c_uint32, C.c_uint32, C.POINTER(MeshOut), P]),
     "uww_backward": (C.c_int, [P, P, C.c_uint32, C.c_uint32, P, P, P, P, P, C.c_uint64]),
     "uww_height_loss": (C.c_int, [P, P, P, C.c_uint32, C.c_float, C.c_float, C.c_float, C.c_uint32, C.c_uint32,
