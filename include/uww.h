@@ -388,6 +388,30 @@ int uww_schedule_chunks(uww_ctx* ctx, const uww_schedule_params* sp, const uww_c
                         uint32_t known_table_size, uww_chunk_desc* d_generate, uint32_t generate_capacity,
                         int32_t* d_render, uint32_t render_capacity, uint32_t* d_counts);
 
+/* ---- terrain shading arithmetic (headless) -------------------------------------- */
+/* camera::CameraUniform (camera.rs:69-79): view_proj column-major, fog colour,
+ * sub position and forward vector, each vec3 padded to 16 bytes. */
+typedef struct uww_camera_uniform {
+    float view_proj[16];
+    float fog_color[3];
+    float pad1;
+    float sub_pos[3];
+    float pad2;
+    float sub_forward[3];
+    float pad3;
+} uww_camera_uniform;
+
+/* terrain.wgsl (underwater_world/src/terrain.wgsl:26-59) evaluated per vertex
+ * into device buffers instead of a render target (no graphics API here):
+ * d_clip[v] = view_proj * (pos, 1) (4 floats), d_rgb[v] = fs_main's fogged
+ * colour at the vertex (3 floats), d_dist_light[v] = (distance to the sub,
+ * smoothstepped spotlight term) (2 floats); any of the three may be NULL.  The
+ * vertex count is d_totals[0] (a build's totals, clamped to vert_capacity) or,
+ * with d_totals NULL, `count`.  Asynchronous. */
+int uww_shade_vertices(uww_ctx* ctx, const uww_camera_uniform* cam, const uww_vert_color* d_verts,
+                       const uint64_t* d_totals, uint32_t count, uint32_t vert_capacity, float* d_clip, float* d_rgb,
+                       float* d_dist_light);
+
 /* ---- point queries ------------------------------------------------------------ */
 /* density(world xyz) for n points: perlin_util::iso_at (perlin_util.rs:24-29) with
  * (x,y,z) = world / CHUNK_SIZE as in boid.rs:132-137.  d_xyz: 3n floats; d_out: n. */

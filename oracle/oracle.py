@@ -59,6 +59,8 @@ def lib():
         L.oracle_schedule_chunks.argtypes = [C.POINTER(abi.Params), C.POINTER(abi.ScheduleParams), P, P, C.c_uint32,
                                              P, C.c_uint32, P, C.c_uint32, P]
         L.oracle_schedule_chunks.restype = C.c_int
+        L.oracle_shade_vertices.argtypes = [C.POINTER(abi.CameraUniform), P, C.c_uint32, P, P, P]
+        L.oracle_shade_vertices.restype = C.c_int
         _lib = L
     return _lib
 
@@ -277,3 +279,12 @@ def schedule_chunks(params: abi.Params, sp, known_descs=None, known_records=None
     if st:
         raise RuntimeError(f"oracle_schedule_chunks failed: {st}")
     return gen[:counts[0]], ren[:counts[1]]
+
+
+def shade_vertices(cam, verts: np.ndarray):
+    """terrain.wgsl at each vertex: (clip (V, 4), rgb (V, 3), dist_light (V, 2))."""
+    verts = np.ascontiguousarray(verts, dtype=abi.VERT_COLOR_DTYPE)
+    nv = verts.shape[0]
+    clip, rgb, dl = np.zeros((nv, 4), np.float32), np.zeros((nv, 3), np.float32), np.zeros((nv, 2), np.float32)
+    lib().oracle_shade_vertices(C.byref(cam), verts.ctypes.data, nv, clip.ctypes.data, rgb.ctypes.data, dl.ctypes.data)
+    return clip, rgb, dl

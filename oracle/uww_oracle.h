@@ -51,6 +51,8 @@ int    oracle_ray_query(const uww_params* p, const uww_chunk_desc* chunks, uint3
 int    oracle_schedule_chunks(const uww_params* p, const uww_schedule_params* sp, const uww_chunk_desc* known,
                               const uww_chunk_record* known_records, uint32_t n_known, uww_chunk_desc* gen_out,
                               uint32_t gen_cap, int32_t* render_out, uint32_t render_cap, uint32_t* counts);
+int    oracle_shade_vertices(const uww_camera_uniform* cam, const uww_vert_color* verts, uint32_t nv, float* clip,
+                             float* rgb, float* dist_light);
 double oracle_density64_full(const uww_params* p, const uint8_t* P, double wx, double wy, double wz,
                              double* grad);
 

@@ -253,3 +253,41 @@ int oracle_schedule_chunks(const uww_params* p, const uww_schedule_params* sp, c
     free(gens);
     return UWW_OK;
 }
+
+/* ---- terrain.wgsl:26-59 at each vertex ---------------------------------------- */
+static float smoothstep_c(float a, float b, float x)
+{
+    float t = (x - a) / (b - a);
+    t = t < 0.f ? 0.f : (t > 1.f ? 1.f : t);
+    return t * t * (3.f - 2.f * t);
+}
+static float clampf_c(float x, float lo, float hi) { return x < lo ? lo : (x > hi ? hi : x); }
+
+int oracle_shade_vertices(const uww_camera_uniform* cam, const uww_vert_color* verts, uint32_t nv, float* clip,
+                          float* rgb, float* dist_light)
+{
+    const float half_pi = 3.14159f / 2.0f;
+    for (uint32_t v = 0; v < nv; ++v) {
+        const float* p = verts[v].pos;
+        for (int i = 0; i < 4; ++i) {
+            float r = cam->view_proj[i] * p[0];
+            r = r + cam->view_proj[4 + i] * p[1];
+            r = r + cam->view_proj[8 + i] * p[2];
+            clip[4 * v + i] = r + cam->view_proj[12 + i];
+        }
+        const v3 dv = {p[0] - cam->sub_pos[0], p[1] - cam->sub_pos[1], p[2] - cam->sub_pos[2]};
+        const v3 f = {cam->sub_forward[0], cam->sub_forward[1], cam->sub_forward[2]};
+        const float dist = sqrtf(dot3(dv, dv));
+        const float cos_angle = dot3(dv, f) / (dist * sqrtf(dot3(f, f)));
+        const float angle = acosf(cos_angle);
+        const float light0 = cosf(angle * 3.0f) * (angle < half_pi ? 1.0f : 0.0f);
+        const float light = smoothstep_c(0.f, 1.f, light0);
+        const float min_dist_value = smoothstep_c(0.f, 20.f, clampf_c(dist, 0.f, 20.f));
+        const float max_dist_value = smoothstep_c(0.f, 45.f, clampf_c(dist, 0.f, 45.f));
+        const float dark = clampf_c(1.0f - light, max_dist_value, min_dist_value);
+        for (int i = 0; i < 3; ++i) rgb[3 * v + i] = verts[v].color[i] * (1.0f - dark) + cam->fog_color[i] * dark;
+        dist_light[2 * v] = dist;
+        dist_light[2 * v + 1] = light;
+    }
+    return UWW_OK;
+}

@@ -75,6 +75,11 @@ class ScheduleParams(C.Structure):
                 ("min_z", C.c_int32), ("max_z", C.c_int32), ("cells", C.c_uint32)]
 
 
+class CameraUniform(C.Structure):
+    _fields_ = [("view_proj", C.c_float * 16), ("fog_color", C.c_float * 3), ("pad1", C.c_float),
+                ("sub_pos", C.c_float * 3), ("pad2", C.c_float), ("sub_forward", C.c_float * 3), ("pad3", C.c_float)]
+
+
 class Tuning(C.Structure):
     _fields_ = [("threads", C.c_int32), ("blocks_per_sm", C.c_int32), ("smem_cells", C.c_int32),
                 ("reserved", C.c_int32)]
@@ -137,6 +142,7 @@ _SIGS = {
     "uww_ray_query": (C.c_int, [P, C.POINTER(RayScene), P, C.c_uint32, P, C.c_uint32, C.c_int32, P]),
     "uww_schedule_chunks": (C.c_int, [P, C.POINTER(ScheduleParams), P, P, P, C.c_uint32, P, C.c_uint32, P,
                                       C.c_uint32, P]),
+    "uww_shade_vertices": (C.c_int, [P, C.POINTER(CameraUniform), P, P, C.c_uint32, C.c_uint32, P, P, P]),
     "uww_forward": (C.c_int, [P, P, C.c_uint32, C.c_uint32, C.POINTER(MeshOut), P]),
     "uww_backward": (C.c_int, [P, P, C.c_uint32, C.c_uint32, P, P, P, P, P, C.c_uint64]),
     "uww_height_loss": (C.c_int, [P, P, P, C.c_uint32, C.c_float, C.c_float, C.c_float, C.c_uint32, C.c_uint32,

@@ -21,7 +21,7 @@ CSRC = PKG / "csrc"
 OUT = PKG / "_build"
 LIB = OUT / "libuww_gb300.so"
 
-SOURCES = ["uww_build.cu", "uww_api.cu", "uww_noalloc.cu", "uww_adjoint.cu", "uww_tune.cu", "uww_sample.cu", "uww_query.cu", "uww_schedule.cu"]
+SOURCES = ["uww_build.cu", "uww_api.cu", "uww_noalloc.cu", "uww_adjoint.cu", "uww_tune.cu", "uww_sample.cu", "uww_query.cu", "uww_schedule.cu", "uww_shade.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
               "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
