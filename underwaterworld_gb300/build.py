@@ -75,6 +75,7 @@ def build(verbose: bool = False, force: bool = False, extra_flags=()) -> Path:
         if r.returncode:
             sys.stderr.write(r.stdout + r.stderr)
             raise RuntimeError("link of libuww_gb300.so failed")
+    build_host()
     return LIB
 
 
@@ -85,6 +86,38 @@ def build_oracle() -> Path:
         sys.stderr.write(r.stdout + r.stderr)
         raise RuntimeError("oracle build failed")
     return ROOT / "oracle" / "_build" / "liboracle.so"
+
+
+HOST = PKG / "host"
+HOST_LIB = OUT / "libuww_host.so"
+# the C++ chunk interface over the C ABI; -ffp-contract=off keeps Tri's f32
+# arithmetic in the reference's (unfused) order
+HOST_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-variable",
+              f"-I{ROOT / 'include'}", f"-I{CSRC}", f"-I{HOST}"]
+
+
+def build_host(force: bool = False) -> Path:
+    srcs = [HOST / "uww_chunk.cpp"]
+    deps = srcs + [HOST / "uww_chunk.hpp", ROOT / "include" / "uww.h", CSRC / "mc_tables.h", LIB]
+    if force or _stale(HOST_LIB, deps):
+        cmd = [shutil.which("g++") or "g++", *HOST_FLAGS, "-shared", "-o", str(HOST_LIB), *map(str, srcs),
+               f"-L{OUT}", "-luww_gb300", f"-Wl,-rpath,{OUT}"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode:
+            sys.stderr.write(r.stdout + r.stderr)
+            raise RuntimeError("build of libuww_host.so failed")
+    return HOST_LIB
+
+
+def build_host_program(src: Path, exe: Path) -> Path:
+    """Compile a C++ program against the host interface (tests)."""
+    build_host()
+    cmd = [shutil.which("g++") or "g++", *HOST_FLAGS, "-o", str(exe), str(src), f"-L{OUT}", "-luww_host",
+           "-luww_gb300", f"-Wl,-rpath,{OUT}"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode:
+        raise RuntimeError("compile failed:\n" + r.stdout + r.stderr)
+    return exe
 
 
 if __name__ == "__main__":
