@@ -137,6 +137,20 @@ def cpu_model():
     return "unknown"
 
 
+def rank_seeds(rank: int):
+    """The permutation seeds one rank cycles through: with N GPUs every rank
+    builds the full grid with its own seeds (weak scaling, no exchange)."""
+    return [(s + rank * N_SEEDS) % 1000 for s in range(N_SEEDS)]
+
+
+def config_dict(n: int, build: str) -> dict:
+    return {"workload": "uniform grid: 16x16x16 = 4096 chunks of 12^3 cells (13^3 f32 samples), "
+                        "4-oct fBm f=0.04 lac 2 pers 0.5, bias -0.03(z-128), iso 0; "
+                        "outputs VertColor + normals + u32 indices",
+            "chunks_per_step": n, "cells_per_step": n * 12 ** 3, "samples_per_step": n * 13 ** 3,
+            "build": build, "l2": "flushed (256 MiB write) before each timed step"}
+
+
 def workload(seed):
     from underwaterworld_gb300 import abi, workloads
     return workloads.uniform_grid(seed=seed, outputs=abi.UWW_OUT_COLOR | abi.UWW_OUT_NORMALS)
@@ -180,8 +194,8 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0, "steps": steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * len(descs) / value, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "uniform grid 16x16x16 chunks of 12^3 cells, 4-oct fBm f=0.04, bias -0.03(z-128), iso 0",
-                   "chunks_per_step": int(len(descs)), "threads": threads},
+        "config": {**config_dict(int(len(descs)), "CPU oracle, reference semantics (f64 noise, O(V) dedup search)"),
+                   "threads": threads, "l2": "n/a (CPU)"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"full 4096-chunk grid per step, {threads} threads, CPU: {cpu_model()}"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -382,8 +396,8 @@ def main():
     assert stream.cuda_stream != 0
 
     params, descs = [], None
-    for s in range(N_SEEDS):
-        p, d = workload((s + rank * N_SEEDS) % 1000)
+    for s in rank_seeds(rank):
+        p, d = workload(s)
         p.math_mode = abi.UWW_MATH_FAST
         params.append(p)
         descs = d
@@ -569,12 +583,8 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded chunk grid; seeds 0-9 cycle per step)",
-        "config": {"workload": "uniform grid: 16x16x16 = 4096 chunks of 12^3 cells (13^3 f32 samples), "
-                               "4-oct fBm f=0.04 lac 2 pers 0.5, bias -0.03(z-128), iso 0; "
-                               "outputs VertColor + normals + u32 indices",
-                   "chunks_per_step": n, "cells_per_step": n * 12 ** 3, "samples_per_step": samples,
-                   "build": "fast (FMA), persistent grid + device work queue + decoupled look-back",
-                   "l2": "flushed (256 MiB write) before each timed step",
+        "config": {**config_dict(n, "fast (FMA), persistent grid + device work queue + decoupled look-back, "
+                                    "then the per-vertex colour/normal pass"),
                    "mean_verts_per_step": mean_v, "mean_inds_per_step": mean_i},
         "mvoxels_per_s": value * 12 ** 3 / 1e6,
         "msamples_per_s": value * 13 ** 3 / 1e6,

@@ -1,0 +1,52 @@
+"""The multi-GPU form of the benchmark is weak scaling with no exchange: every
+rank builds the full grid with its own permutation seeds, and rank 0 reports
+the chunks of all ranks over the slowest rank's time.  This checks that host
+logic with two gloo ranks on the CPU (the oracle stands in for the GPU build)."""
+import os
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+import torch.distributed as dist
+import torch.multiprocessing as mp
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def _rank_main(rank, world, port, q):
+    sys.path.insert(0, str(ROOT))
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world))
+    import torch
+    import bench
+    from oracle import oracle as O
+    from underwaterworld_gb300 import abi
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    seeds = bench.rank_seeds(rank)
+    p, d = bench.workload(seeds[0])
+    sub = d[:32]
+    from underwaterworld_gb300.chunk import make_descs
+    b = O.build_chunks(p, make_descs(sub["pos"], sub["cells"]), precision=O.F32)
+    counts = torch.tensor([len(sub), int(b.totals[0])], dtype=torch.float64)
+    t = torch.tensor([0.5 + rank], dtype=torch.float64)          # this rank's time
+    dist.all_reduce(counts, op=dist.ReduceOp.SUM)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    q.put((rank, seeds, counts.tolist(), float(t.item()), int(b.totals[0])))
+    dist.destroy_process_group()
+
+
+def test_two_gloo_ranks_weak_scaling(built_lib, oracle):
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = 29500 + os.getpid() % 1000
+    procs = [ctx.Process(target=_rank_main, args=(r, 2, port, q)) for r in range(2)]
+    for pr in procs:
+        pr.start()
+    res = sorted(q.get(timeout=120) for _ in procs)
+    for pr in procs:
+        pr.join(timeout=60)
+        assert pr.exitcode == 0
+    (r0, s0, c0, t0, v0), (r1, s1, c1, t1, v1) = res
+    assert not set(s0) & set(s1), "ranks must use distinct seeds"
+    assert c0 == c1 == [64.0, float(v0 + v1)]   # chunks and vertices of both ranks
+    assert t0 == t1 == 1.5                      # the slowest rank's time
