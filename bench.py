@@ -370,6 +370,89 @@ def leg_terrain_fit(stream, steps=200):
             "rms_height_error_last": rmse1, "peak_device_bytes": int(free0 - min_free)}
 
 
+def leg_queries(stream, flush, steps):
+    """The callers around the build (§8f rows): point density queries
+    (perlin_util::iso_at for 1M points), boid wall rays (100k boids x 18 rays
+    against the reference grid's mesh), the scheduler feed (update_nearby), and
+    the terrain shading pass over the uniform grid's vertices."""
+    import torch
+    from underwaterworld_gb300 import abi, workloads
+    from underwaterworld_gb300.chunk import Context, DeviceArray
+    from underwaterworld_gb300.query import RayScene
+    from underwaterworld_gb300.schedule import Scheduler, schedule_params
+    res = {}
+    L = abi.lib()
+    dev = stream.device
+    # point queries on the uniform grid's density
+    p, d = workloads.uniform_grid(seed=0, outputs=abi.UWW_OUT_COLOR)
+    p.math_mode = abi.UWW_MATH_FAST
+    ctx = Context(p, stream=stream.cuda_stream)
+    npts = 1 << 20
+    g = torch.Generator(device="cpu").manual_seed(0)
+    xyz = (torch.rand(npts, 3, generator=g) * 256.0).to(dev)
+    dens = torch.empty(npts, device=dev)
+    run = lambda: abi.check(L.uww_density_at(ctx.h, C.c_void_p(xyz.data_ptr()), npts, C.c_void_p(dens.data_ptr())))
+    run()
+    t = statistics.median([timed(stream, run, flush) for _ in range(steps)])
+    res["density_at"] = {"points": npts, "us": t * 1e6, "mpoints_per_s": npts / t / 1e6}
+    ctx.close()
+    # boid wall rays against the reference grid (iso -0.1, exact build)
+    p, d = workloads.reference_grid(outputs=abi.UWW_OUT_CASES)
+    ctx = Context(p, stream=stream.cuda_stream)
+    sc = RayScene(ctx, d)
+    b = sc.batch()
+    nq, nr = 100_000, 18
+    rng = np.random.default_rng(0)
+    origins = (b.verts["pos"][rng.integers(0, len(b.verts), nq)] + rng.normal(0, 1.5, (nq, 3))).astype(np.float32)
+    dirs = rng.normal(size=(nq, nr, 3)).astype(np.float32)
+    dirs /= np.linalg.norm(dirs, axis=-1, keepdims=True)
+    d_o, d_d = ctx.upload(origins), ctx.upload(dirs.astype(np.float32))
+    d_t = DeviceArray(nq * nr * 4)
+    run = lambda: abi.check(L.uww_ray_query(ctx.h, C.byref(sc.scene), C.c_void_p(d_o.ptr), nq, C.c_void_p(d_d.ptr),
+                                            nr, 3, C.c_void_p(d_t.ptr)))
+    run()
+    t = statistics.median([timed(stream, run, flush) for _ in range(steps)])
+    res["ray_query"] = {"boids": nq, "rays_per_boid": nr, "us": t * 1e6, "mrays_per_s": nq * nr / t / 1e6}
+    # scheduler feed with the reference grid as the known chunks
+    size = 1 << int(2 * len(d) - 1).bit_length()
+    d_tab = DeviceArray(size * 4)
+    abi.check(L.uww_chunk_index(ctx.h, C.c_void_p(sc.d_desc.ptr), len(d), C.c_void_p(d_tab.ptr), size))
+    sch = Scheduler(ctx)
+    sp = schedule_params(np.array([3.0, -2.0, 1.0], np.float32), np.array([-3.0, -2.0, 2.0], np.float32),
+                         np.array([4.0, -2.0, 1.0], np.float32))
+    known = (sc.d_desc.ptr, sc.d_rec.ptr, d_tab.ptr, size)
+    run = lambda: sch.run(sp, known)
+    run()
+    t = statistics.median([timed(stream, run) for _ in range(steps)])
+    gen, ren, counts = sch.fetch()
+    res["schedule"] = {"us": t * 1e6, "candidates": 10 * 10 * 5, "generate": int(counts[0]), "render": int(counts[1])}
+    ctx.close()
+    # terrain shading over the uniform grid's mesh
+    p, d = workloads.uniform_grid(seed=0, outputs=abi.UWW_OUT_COLOR)
+    p.math_mode = abi.UWW_MATH_FAST
+    ctx = Context(p, stream=stream.cuda_stream)
+    vcap = 1 << 20
+    d_desc = ctx.upload(d)
+    bufs = [DeviceArray(vcap * 24), DeviceArray(4 << 22), DeviceArray(len(d) * 32), DeviceArray(32)]
+    out = abi.MeshOut(bufs[0].ptr, None, bufs[1].ptr, None, None, bufs[2].ptr, bufs[3].ptr, vcap, 1 << 22, 0, 0)
+    abi.check(L.uww_build_chunks(ctx.h, C.c_void_p(d_desc.ptr), len(d), 12, C.byref(out)))
+    ctx.sync()
+    nv = int(ctx.download(bufs[3], (4,), np.uint64)[0])
+    cam = abi.CameraUniform()
+    for i in range(16):
+        cam.view_proj[i] = 1.0 if i % 5 == 0 else 0.0
+    for i in range(3):
+        cam.sub_pos[i], cam.sub_forward[i], cam.fog_color[i] = 128.0, (1.0, 0.0, 0.0)[i], 0.1
+    d_clip, d_rgb = DeviceArray(vcap * 16), DeviceArray(vcap * 12)
+    run = lambda: abi.check(L.uww_shade_vertices(ctx.h, C.byref(cam), C.c_void_p(bufs[0].ptr), C.c_void_p(bufs[3].ptr),
+                                                 0, vcap, C.c_void_p(d_clip.ptr), C.c_void_p(d_rgb.ptr), None))
+    run()
+    t = statistics.median([timed(stream, run, flush) for _ in range(steps)])
+    res["shade"] = {"vertices": nv, "us": t * 1e6, "mverts_per_s": nv / t / 1e6}
+    ctx.close()
+    return res
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -544,6 +627,7 @@ def main():
         extra["frame_graph"] = leg_frame_graph(ctx, params[0], descs, max(5, min(args.steps, 50)), 3)
         extra["mixed_lod"] = leg_mixed_lod(stream, flush, max(10, min(args.steps, 200)), 3)
         extra["adjoint"] = leg_adjoint(stream, flush, max(5, min(args.steps, 50)), 3)
+        extra["queries"] = leg_queries(stream, flush, max(5, min(args.steps, 50)))
         if not args.no_fit:
             extra["terrain_fit"] = leg_terrain_fit(stream, args.fit_steps)
 
