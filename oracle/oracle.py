@@ -1,7 +1,7 @@
 """ctypes binding of the CPU oracle (oracle/_build/liboracle.so).
 
 TEST INFRASTRUCTURE ONLY: used by tests/, __graft_entry__.smoke() and the
-CPU-baseline leg of bench.py as the checker of libuww_gb300.so.  The product
+CPU-baseline leg of bench.py, to verify libuww_gb300.so against.  The product
 never imports this module.  See uww_oracle.c for what it restates and the
 parity status of each part.
 """

@@ -1,7 +1,7 @@
 /*
  * uww_oracle.c -- CPU oracle for the chunk-generation path.
  *
- * TEST INFRASTRUCTURE ONLY.  This file is the checker for the CUDA library:
+ * TEST INFRASTRUCTURE ONLY.  The CUDA library is verified against this file:
  * only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load it.
  * The product (libuww_gb300.so) never links, calls or falls back to it.
  *

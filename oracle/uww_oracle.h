@@ -1,7 +1,7 @@
 /*
  * uww_oracle.h -- CPU oracle of the chunk-generation path.
  * TEST INFRASTRUCTURE ONLY: used by tests/, __graft_entry__.smoke() and the
- * CPU-baseline leg of bench.py as the checker; never by the product library.
+ * CPU-baseline leg of bench.py, to verify and time against; never by the product library.
  */
 #ifndef UWW_ORACLE_H
 #define UWW_ORACLE_H
