@@ -261,3 +261,34 @@ def test_fast_build_other_workloads(ctx_factory, oracle, which):
     blank_ref = (ref.records["flags"] & abi.UWW_CHUNK_HAS_MESH) > 0
     blank_got = (got.records["flags"] & abi.UWW_CHUNK_HAS_MESH) > 0
     assert np.count_nonzero(blank_ref != blank_got) <= 1
+
+
+def test_host_build_into_page_locked_buffers(ctx_factory):
+    """uww_build_chunks_host with page-locked (device-addressable) buffers copies
+    with one kernel and one synchronisation; the result is the device build's."""
+    import ctypes as C
+    from underwaterworld_gb300.chunk import HostArray
+    p, d = workloads.uniform_grid(seed=4, outputs=abi.UWW_OUT_COLOR | abi.UWW_OUT_NORMALS | abi.UWW_OUT_CASES)
+    p.math_mode = abi.UWW_MATH_FAST
+    d = relayout(d[::5])
+    ctx = ctx_factory(p)
+    want = ctx.build_chunks_device(d, 1 << 20, 1 << 22)
+    n, nc = len(d), int((d["cells"].astype(np.int64) ** 3).sum())
+    vcap, icap = int(want.totals[0]) + 7, int(want.totals[1]) + 5   # odd sizes: unaligned tails
+    hv = HostArray((vcap,), abi.VERT_COLOR_DTYPE)
+    hn = HostArray((vcap, 3), np.float32)
+    hi = HostArray((icap,), np.uint32)
+    hr = HostArray((n,), abi.CHUNK_RECORD_DTYPE)
+    hc = HostArray((nc,), np.uint8)
+    tot = np.zeros(4, np.uint64)
+    hd = HostArray((n,), abi.CHUNK_DESC_DTYPE)
+    hd.array[:] = d
+    out = abi.MeshOut(hv.ptr, hn.ptr, hi.ptr, hc.ptr, None, hr.ptr, tot.ctypes.data, vcap, icap, nc, 0)
+    abi.check(abi.lib().uww_build_chunks_host(ctx.h, C.c_void_p(hd.ptr), n, C.byref(out)))
+    nv, ni = int(tot[0]), int(tot[1])
+    np.testing.assert_array_equal(tot[:3], want.totals[:3])
+    np.testing.assert_array_equal(hr.array, want.records)
+    np.testing.assert_array_equal(hv.array[:nv], want.verts)
+    np.testing.assert_array_equal(hn.array[:nv], want.normals)
+    np.testing.assert_array_equal(hi.array[:ni], want.inds)
+    np.testing.assert_array_equal(hc.array, want.cases)

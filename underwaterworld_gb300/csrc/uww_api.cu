@@ -237,6 +237,20 @@ int launch(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint32_t ma
     return cuda_status(launch_build(ctx->dev, a, queue, cfg.grid, cfg.threads, cfg.dyn_smem, ctx->stream), "build kernel launch");
 }
 
+// The device address of page-locked host memory, or NULL when `p` is not
+// host memory the device can address.
+void* device_view(void* p)
+{
+    if (!p) return nullptr;
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (at.type != cudaMemoryTypeHost || !at.devicePointer) return nullptr;
+    return at.devicePointer;
+}
+
 int check_out(const uww_mesh_out* out)
 {
     if (!out || !out->verts || !out->inds || !out->records) return UWW_ERR_INVALID_ARG;
@@ -525,6 +539,46 @@ int uww_build_chunks_host(uww_ctx* ctx, const uww_chunk_desc* h_chunks, uint32_t
     d_out.vert_capacity = h_out->vert_capacity;
     d_out.ind_capacity = h_out->ind_capacity;
     if ((st = launch(ctx, ctx->d_chunks, n, max_cells, &d_out, true))) return st;
+
+    // Page-locked host buffers the device can address: one copy kernel that
+    // reads the vertex and index counts on the device, then one
+    // synchronisation.  Otherwise the copies are sized on the host after a
+    // first synchronisation.
+    void* dv = device_view(h_out->verts);
+    void* dn = want_normals ? device_view(h_out->normals) : nullptr;
+    void* di = device_view(h_out->inds);
+    void* dr = device_view(h_out->records);
+    void* dc = want_cases ? device_view(h_out->cases) : nullptr;
+    void* ds = want_samples ? device_view(h_out->samples) : nullptr;
+    if (dv && di && dr && (!want_normals || dn) && (!want_cases || dc) && (!want_samples || ds)) {
+        CopyOut c;
+        std::memset(&c, 0, sizeof(c));
+        auto seg = [&](const void* src, void* dst, unsigned long long fixed, int idx, uint32_t eb, unsigned long long cap) {
+            CopySeg& g = c.seg[c.nseg++];
+            g.src = static_cast<const uint8_t*>(src);
+            g.dst = static_cast<uint8_t*>(dst);
+            g.fixed_bytes = fixed;
+            g.count_idx = idx;
+            g.elem_bytes = eb;
+            g.cap_elems = cap;
+        };
+        seg(ctx->d_records, dr, (unsigned long long)n * sizeof(uww_chunk_record), -1, 0, 0);
+        seg(ctx->d_verts, dv, 0, 0, sizeof(uww_vert_color), h_out->vert_capacity);
+        seg(ctx->d_inds, di, 0, 1, sizeof(uint32_t), h_out->ind_capacity);
+        if (want_normals) seg(ctx->d_normals, dn, 0, 0, 12, h_out->vert_capacity);
+        if (want_cases && case_bytes) seg(ctx->d_cases, dc, case_bytes, -1, 0, 0);
+        if (want_samples && sample_count) seg(ctx->d_samples, ds, sample_count * 4, -1, 0, 0);
+        if ((e = launch_copy_out(c, ctx->d_totals, ctx->num_sms * 2, s)) != cudaSuccess) return cuda_status(e);
+        if ((e = cudaMemcpyAsync(ctx->h_totals, ctx->d_totals, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+            return cuda_status(e);
+        if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_status(e);
+        if (h_out->totals) std::memcpy(h_out->totals, ctx->h_totals, 4 * sizeof(uint64_t));
+        if (ctx->h_totals[3] & kErrTimeout) return UWW_ERR_TIMEOUT;
+        if (ctx->h_totals[3] & (kErrBadChunk | kErrRange)) return UWW_ERR_INVALID_ARG;
+        if (ctx->h_totals[2]) return UWW_ERR_CAPACITY;
+        return UWW_OK;
+    }
+
     if ((e = cudaMemcpyAsync(h_out->records, ctx->d_records, (size_t)n * sizeof(uww_chunk_record), cudaMemcpyDeviceToHost, s)) != cudaSuccess)
         return cuda_status(e);
     if ((e = cudaMemcpyAsync(ctx->h_totals, ctx->d_totals, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s)) != cudaSuccess)

@@ -731,6 +731,33 @@ __global__ void __launch_bounds__(256) vertex_kernel(const DevParams p, uww_vert
         finish_vertex<O>(p, P, gp, verts, normals, v, want_color, want_normals);
 }
 
+// Copy of a build's outputs into host memory the device can address (page-
+// locked, mapped): one segment per blockIdx.y, its length fixed or read from
+// the build's totals on the device, so the host needs no synchronisation
+// between the build and the copies.
+__global__ void copy_out_kernel(const CopyOut c, const unsigned long long* __restrict__ totals)
+{
+    const CopySeg& g = c.seg[blockIdx.y];
+    unsigned long long bytes = g.fixed_bytes;
+    if (g.count_idx >= 0) bytes = min(totals[g.count_idx], g.cap_elems) * g.elem_bytes;
+    const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (size_t)gridDim.x * blockDim.x;
+    const uintptr_t al = (uintptr_t)g.src | (uintptr_t)g.dst;
+    if ((al & 15) == 0) {
+        // 16-byte words, then the remaining bytes
+        const uint4* s4 = reinterpret_cast<const uint4*>(g.src);
+        uint4* d4 = reinterpret_cast<uint4*>(g.dst);
+        const size_t n16 = bytes / 16;
+        for (size_t i = tid; i < n16; i += stride) d4[i] = __ldcs(s4 + i);
+        for (size_t i = n16 * 16 + tid; i < bytes; i += stride) g.dst[i] = g.src[i];
+    } else if (((al | (uintptr_t)bytes) & 3) == 0) {
+        const uint32_t* s1 = reinterpret_cast<const uint32_t*>(g.src);
+        uint32_t* d1 = reinterpret_cast<uint32_t*>(g.dst);
+        for (size_t i = tid; i < bytes / 4; i += stride) d1[i] = s1[i];
+    } else {
+        for (size_t i = tid; i < bytes; i += stride) g.dst[i] = g.src[i];
+    }
+}
+
 template <class O>
 __global__ void density_kernel(const DevParams p, const float* __restrict__ xyz, uint32_t n, float* __restrict__ out)
 {
@@ -827,6 +854,13 @@ cudaError_t launch_build(const DevParams& p, const BuildArgs& a, bool queue, int
 cudaError_t launch_fma_probe(int blocks, uint32_t iters, float* sink, cudaStream_t s)
 {
     fma_probe_kernel<<<blocks, 256, 0, s>>>(iters, 1.0f, sink);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_copy_out(const CopyOut& c, const unsigned long long* totals, int blocks_x, cudaStream_t s)
+{
+    if (c.nseg <= 0) return cudaSuccess;
+    copy_out_kernel<<<dim3((unsigned)blocks_x, (unsigned)c.nseg), 256, 0, s>>>(c, totals);
     return cudaGetLastError();
 }
 

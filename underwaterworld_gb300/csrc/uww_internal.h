@@ -92,6 +92,21 @@ struct BuildArgs {
     const uint32_t* n_dev;           // optional device chunk count; the launch builds min(*n_dev, n)
 };
 
+// Device -> mapped-host copy of a build's outputs (uww_build.cu).
+struct CopySeg {
+    const uint8_t* src;
+    uint8_t* dst;                    // device address of page-locked host memory
+    unsigned long long fixed_bytes;  // when count_idx < 0
+    int count_idx;                   // else bytes = min(totals[count_idx], cap_elems) * elem_bytes
+    uint32_t elem_bytes;
+    unsigned long long cap_elems;
+};
+struct CopyOut {
+    CopySeg seg[8];
+    int nseg;
+};
+cudaError_t launch_copy_out(const CopyOut& c, const unsigned long long* totals, int blocks_x, cudaStream_t s);
+
 // Host helpers shared by the entry points (uww_api.cu).
 int check_params(const uww_params* p);
 void dev_params_from(const uww_params* p, DevParams* d);
