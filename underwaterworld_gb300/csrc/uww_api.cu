@@ -158,9 +158,10 @@ int plan_launch(uww_ctx* ctx, uint32_t n, uint32_t max_cells, bool queue, Launch
     cfg->smem_buf = smem_cells > 0 ? chunk_layout((int)smem_cells).total : 0;
     cfg->ztable_offset = (size_t)slots * cfg->smem_buf;
     cfg->dyn_smem = cfg->ztable_offset + zt;
-    // compute threads: by default about one per (x, y) sample column of the
-    // largest chunk, rounded so the last round of columns fills its warps;
-    // the batched form adds one control warp
+    // compute threads: by default 192 for chunks of up to 12 cells (one per
+    // sample column of a 13^3 grid) and 256 above, which keeps two CTAs per SM
+    // (larger chunks loop over their columns); the batched form adds one
+    // control warp
     const int compute = ctx->threads > 0 ? ctx->threads : default_compute_threads(max_cells);
     cfg->threads = compute + (queue ? 32 : 0);
     cfg->scratch_slot = max_cells > smem_cells ? chunk_layout((int)max_cells).total : 0;
@@ -265,7 +266,7 @@ int check_params(const uww_params* p) { return validate_params(p); }
 void dev_params_from(const uww_params* p, DevParams* d) { make_dev_params(p, d); }
 int status_from_cuda(cudaError_t e, const char* where) { return cuda_status(e, where); }
 long long spin_limit_cycles() { return kSpinLimitCycles; }
-int default_compute_threads(uint32_t max_cells) { return max_cells <= 12 ? 192 : max_cells <= 24 ? 320 : 512; }
+int default_compute_threads(uint32_t max_cells) { return max_cells <= 12 ? 192 : 256; }
 int ensure_device_bytes(void** ptr, size_t* cap, size_t bytes) { return ensure_device(ptr, cap, bytes); }
 int launch_batched(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint32_t max_cells,
                    const uww_mesh_out* out, uint32_t* edge_ids, const uint32_t* n_dev)

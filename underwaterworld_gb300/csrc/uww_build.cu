@@ -357,7 +357,9 @@ __device__ void chunk_front(const DevParams& p, const BuildArgs& a, SmemTables& 
             }
         } else if constexpr (std::is_same<O, FastOps>::value) {
             const ZTable zt = ztable_at(dyn_smem + a.ztable_offset, S, p.octaves);
-            inside = sample_columns_fast(p, T.perm, T.gp, zt, rho, N, ox, oy, oz, ncomp);
+            // a chunk in a global scratch slot accumulates its columns in local memory
+            inside = (uint32_t)N <= a.smem_cells ? sample_columns_fast<false>(p, T.perm, T.gp, zt, rho, N, ox, oy, oz, ncomp)
+                                                 : sample_columns_fast<true>(p, T.perm, T.gp, zt, rho, N, ox, oy, oz, ncomp);
         } else {
             for (int idx = tid; idx < S3; idx += ncomp) {
                 const int x = idx / S2, r = idx - x * S2, y = r / S, z = r - y * S;

@@ -191,6 +191,10 @@ __device__ __forceinline__ ZTable ztable_at(uint8_t* base, int S, int octaves)
     return t;
 }
 
+// COLBUF: accumulate each column in a per-thread buffer (local memory, L1)
+// and write it to rho once, for rho in global memory where an accumulate per
+// sample and octave would be an L2 round trip each.
+template <bool COLBUF = false>
 __device__ __forceinline__ int sample_columns_fast(const DevParams& p, const uint8_t* __restrict__ P,
                                                    const float4* __restrict__ gp, const ZTable Z,
                                                    float* __restrict__ rho, int N, int ox, int oy, int oz,
@@ -230,7 +234,8 @@ __device__ __forceinline__ int sample_columns_fast(const DevParams& p, const uin
     int inside = 0;
     for (int col = threadIdx.x; col < SS; col += ncomp) {
         const int x = col / S, y = col - x * S;
-        float* out = rho + col * S;
+        float colbuf[COLBUF ? UWW_MAX_CELLS + 1 : 1];
+        float* out = COLBUF ? colbuf : rho + col * S;
         const float nx = column_coord((float)x, s, ox, p.offset[0], bf);
         const float ny = column_coord((float)y, s, oy, p.offset[1], bf);
         for (int k = 0; k < K; ++k) {
@@ -262,6 +267,10 @@ __device__ __forceinline__ int sample_columns_fast(const DevParams& p, const uin
                     if (last) inside |= !(r0 > iso);
                 }
             }
+        }
+        if (COLBUF) {
+            float* dst = rho + col * S;
+            for (int z = 0; z < S; ++z) dst[z] = colbuf[z];
         }
     }
     return inside;

@@ -160,7 +160,8 @@ __global__ void __launch_bounds__(THREADS, MINB) sample_kernel_fast(const DevPar
             uint8_t* zt = reinterpret_cast<uint8_t*>(stage) + stage_bytes(MAXS);
             const bool staged = S <= MAXS;
             float* rho = staged ? stage : dst;
-            sample_columns_fast(p, P, gp, ztable_at(zt, S, p.octaves), rho, N, ox, oy, oz, blockDim.x);
+            if (staged) sample_columns_fast<false>(p, P, gp, ztable_at(zt, S, p.octaves), rho, N, ox, oy, oz, blockDim.x);
+            else sample_columns_fast<true>(p, P, gp, ztable_at(zt, S, p.octaves), rho, N, ox, oy, oz, blockDim.x);
             if (staged) {
                 __syncthreads();
                 for (int i = threadIdx.x; i < (int)S3; i += blockDim.x) dst[i] = stage[i];
