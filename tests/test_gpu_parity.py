@@ -263,9 +263,14 @@ def test_fast_build_other_workloads(ctx_factory, oracle, which):
     assert np.count_nonzero(blank_ref != blank_got) <= 1
 
 
-def test_host_build_into_page_locked_buffers(ctx_factory):
-    """uww_build_chunks_host with page-locked (device-addressable) buffers copies
-    with one kernel and one synchronisation; the result is the device build's."""
+@pytest.mark.parametrize("shift", [0, 4, 8, 12, 1])
+def test_host_build_into_page_locked_buffers(ctx_factory, shift):
+    """uww_build_chunks_host with page-locked (device-addressable) buffers:
+    records, indices, vertices and normals are streamed to the host during
+    the build, cases by one copy kernel, with one synchronisation; the result
+    is the device build's.  `shift` moves every output buffer off a 16-byte
+    boundary by that many bytes (single-word stores; off a 4-byte boundary,
+    the sized-copy path)."""
     import ctypes as C
     from underwaterworld_gb300.chunk import HostArray
     p, d = workloads.uniform_grid(seed=4, outputs=abi.UWW_OUT_COLOR | abi.UWW_OUT_NORMALS | abi.UWW_OUT_CASES)
@@ -275,20 +280,83 @@ def test_host_build_into_page_locked_buffers(ctx_factory):
     want = ctx.build_chunks_device(d, 1 << 20, 1 << 22)
     n, nc = len(d), int((d["cells"].astype(np.int64) ** 3).sum())
     vcap, icap = int(want.totals[0]) + 7, int(want.totals[1]) + 5   # odd sizes: unaligned tails
-    hv = HostArray((vcap,), abi.VERT_COLOR_DTYPE)
-    hn = HostArray((vcap, 3), np.float32)
-    hi = HostArray((icap,), np.uint32)
-    hr = HostArray((n,), abi.CHUNK_RECORD_DTYPE)
-    hc = HostArray((nc,), np.uint8)
+    keep = []
+
+    def host(shape, dtype):
+        dtype = np.dtype(dtype)
+        nbytes = int(np.prod(shape)) * dtype.itemsize
+        h = HostArray((nbytes + 16,), np.uint8)
+        keep.append(h)
+        return h.ptr + shift, h.array[shift:shift + nbytes].view(dtype).reshape(shape)
+
+    pv, hv = host((vcap,), abi.VERT_COLOR_DTYPE)
+    pn, hn = host((vcap, 3), np.float32)
+    pi, hi = host((icap,), np.uint32)
+    pr, hr = host((n,), abi.CHUNK_RECORD_DTYPE)
+    pc, hc = host((nc,), np.uint8)
     tot = np.zeros(4, np.uint64)
     hd = HostArray((n,), abi.CHUNK_DESC_DTYPE)
     hd.array[:] = d
-    out = abi.MeshOut(hv.ptr, hn.ptr, hi.ptr, hc.ptr, None, hr.ptr, tot.ctypes.data, vcap, icap, nc, 0)
+    out = abi.MeshOut(pv, pn, pi, pc, None, pr, tot.ctypes.data, vcap, icap, nc, 0)
     abi.check(abi.lib().uww_build_chunks_host(ctx.h, C.c_void_p(hd.ptr), n, C.byref(out)))
     nv, ni = int(tot[0]), int(tot[1])
     np.testing.assert_array_equal(tot[:3], want.totals[:3])
-    np.testing.assert_array_equal(hr.array, want.records)
-    np.testing.assert_array_equal(hv.array[:nv], want.verts)
-    np.testing.assert_array_equal(hn.array[:nv], want.normals)
-    np.testing.assert_array_equal(hi.array[:ni], want.inds)
-    np.testing.assert_array_equal(hc.array, want.cases)
+    np.testing.assert_array_equal(hr, want.records)
+    np.testing.assert_array_equal(hv[:nv], want.verts)
+    np.testing.assert_array_equal(hn[:nv], want.normals)
+    np.testing.assert_array_equal(hi[:ni], want.inds)
+    np.testing.assert_array_equal(hc, want.cases)
+
+
+def test_host_build_streamed_positions_only(ctx_factory, oracle):
+    """Streamed host output with neither colours nor normals requested: pass 2
+    still runs to move the positions to the host; parity build bit-exact."""
+    import ctypes as C
+    from underwaterworld_gb300.chunk import HostArray
+    p, d = workloads.reference_grid(outputs=0)
+    ctx = ctx_factory(p)
+    ref = oracle.build_chunks(p, d)
+    vcap, icap = caps(ref)
+    n = len(d)
+    hv = HostArray((vcap,), abi.VERT_COLOR_DTYPE)
+    hi = HostArray((icap,), np.uint32)
+    hr = HostArray((n,), abi.CHUNK_RECORD_DTYPE)
+    hd = HostArray((n,), abi.CHUNK_DESC_DTYPE)
+    hd.array[:] = d
+    tot = np.zeros(4, np.uint64)
+    out = abi.MeshOut(hv.ptr, None, hi.ptr, None, None, hr.ptr, tot.ctypes.data, vcap, icap)
+    abi.check(abi.lib().uww_build_chunks_host(ctx.h, C.c_void_p(hd.ptr), n, C.byref(out)))
+    nv, ni = int(tot[0]), int(tot[1])
+    assert (nv, ni) == (int(ref.totals[0]), int(ref.totals[1]))
+    assert_records_equal(hr.array, ref.records)
+    np.testing.assert_array_equal(hi.array[:ni], ref.inds)
+    np.testing.assert_array_equal(hv.array[:nv]["pos"], ref.verts["pos"])
+    assert not hv.array[:nv]["color"].any()
+
+
+def test_misaligned_device_outputs_are_refused(ctx_factory):
+    """Device outputs off the alignment the kernels store with (8 bytes for
+    vertices and totals, 4 for the rest) and descriptors off a 4-byte
+    boundary are refused on the host, before any launch."""
+    import ctypes as C
+    import torch
+    p, d = workloads.reference_grid()
+    ctx = ctx_factory(p)
+    dev = torch.device("cuda")
+    n = len(d)
+    dd = torch.zeros(n * 32 + 16, dtype=torch.uint8, device=dev)
+    dd[:n * 32] = torch.from_numpy(d.view(np.uint8).copy()).to(dev)
+    bufs = {k: torch.zeros(1 << 20, dtype=torch.uint8, device=dev) for k in ("v", "n", "i", "r", "t")}
+    base = {k: b.data_ptr() for k, b in bufs.items()}
+    L = abi.lib()
+
+    def run(desc_ptr, **shift):
+        ptr = {k: base[k] + shift.get(k, 0) for k in base}
+        out = abi.MeshOut(ptr["v"], ptr["n"], ptr["i"], None, None, ptr["r"], ptr["t"], 1 << 14, 1 << 16)
+        return L.uww_build_chunks(ctx.h, C.c_void_p(desc_ptr), n, 12, C.byref(out))
+
+    for shift in ({"v": 4}, {"t": 4}, {"i": 2}, {"n": 1}, {"r": 2}):
+        assert run(dd.data_ptr(), **shift) == abi.UWW_ERR_INVALID_ARG, shift
+    assert run(dd.data_ptr() + 2) == abi.UWW_ERR_INVALID_ARG
+    assert run(dd.data_ptr()) == abi.UWW_OK
+    torch.cuda.synchronize()

@@ -180,9 +180,20 @@ int plan_launch(uww_ctx* ctx, uint32_t n, uint32_t max_cells, bool queue, Launch
     return UWW_OK;
 }
 
+// Device addresses of page-locked host buffers for the streamed host output
+// of a batched build (BuildArgs::host_*).
+struct HostOut {
+    uww_vert_color* verts;
+    float* normals;
+    uint32_t* inds;
+    uww_chunk_record* records;
+    unsigned long long* totals;
+};
+
 int launch(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint32_t max_cells, const uww_mesh_out* out,
            bool queue, const float* samples_in = nullptr, unsigned long long samples_in_count = 0,
-           uint32_t* edge_ids = nullptr, const uint32_t* n_dev = nullptr, bool prepare_only = false)
+           uint32_t* edge_ids = nullptr, const uint32_t* n_dev = nullptr, bool prepare_only = false,
+           const HostOut* host = nullptr)
 {
     LaunchCfg cfg;
     int st = plan_launch(ctx, n, max_cells, queue, &cfg);
@@ -219,6 +230,13 @@ int launch(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint32_t ma
     a.spin_limit_cycles = kSpinLimitCycles;
     a.edge_ids = edge_ids;
     a.n_dev = n_dev;
+    if (host && queue) {
+        a.host_verts = host->verts;
+        a.host_normals = host->normals;
+        a.host_inds = host->inds;
+        a.host_records = host->records;
+        a.host_totals = host->totals;
+    }
     if (queue) {
         // The look-back words, ticket counter and accumulators are zero when a
         // launch starts: zeroed once here on (re)allocation, and reset by the
@@ -252,10 +270,13 @@ void* device_view(void* p)
     return at.devicePointer;
 }
 
-int check_out(const uww_mesh_out* out)
+// device: the buffers are device memory the kernels write (alignment checked);
+// otherwise host buffers, reached by copies of any alignment
+int check_out(const uww_mesh_out* out, bool device = true)
 {
     if (!out || !out->verts || !out->inds || !out->records) return UWW_ERR_INVALID_ARG;
     if (out->vert_capacity > kLbVertMax) return UWW_ERR_INVALID_ARG;
+    if (device && !device_out_aligned(out)) return UWW_ERR_INVALID_ARG;
     return UWW_OK;
 }
 
@@ -464,7 +485,7 @@ int uww_build_chunks(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, u
         if (out->totals) return cuda_status(cudaMemsetAsync(out->totals, 0, 4 * sizeof(uint64_t), ctx->stream));
         return UWW_OK;
     }
-    if (!d_chunks) return UWW_ERR_INVALID_ARG;
+    if (!d_chunks || !aligned_to(d_chunks, 4)) return UWW_ERR_INVALID_ARG;
     return launch(ctx, d_chunks, n, max_cells, out, true);
 }
 
@@ -479,13 +500,13 @@ int uww_build_chunks_from_samples(uww_ctx* ctx, const uww_chunk_desc* d_chunks, 
         if (out->totals) return cuda_status(cudaMemsetAsync(out->totals, 0, 4 * sizeof(uint64_t), ctx->stream));
         return UWW_OK;
     }
-    if (!d_chunks || !d_samples) return UWW_ERR_INVALID_ARG;
+    if (!d_chunks || !d_samples || !aligned_to(d_chunks, 4) || !aligned_to(d_samples, 4)) return UWW_ERR_INVALID_ARG;
     return launch(ctx, d_chunks, n, max_cells, out, true, d_samples, sample_count);
 }
 
 int uww_build_chunk_plain(uww_ctx* ctx, const uww_chunk_desc* d_chunk, uint32_t cells, const uww_mesh_out* out)
 {
-    if (!ctx || !d_chunk) return UWW_ERR_INVALID_ARG;
+    if (!ctx || !d_chunk || !aligned_to(d_chunk, 4)) return UWW_ERR_INVALID_ARG;
     int st = check_out(out);
     if (st) return st;
     if (!out->totals) return UWW_ERR_INVALID_ARG;
@@ -496,7 +517,7 @@ int uww_build_chunk_plain(uww_ctx* ctx, const uww_chunk_desc* d_chunk, uint32_t 
 int uww_build_chunks_host(uww_ctx* ctx, const uww_chunk_desc* h_chunks, uint32_t n, const uww_mesh_out* h_out)
 {
     if (!ctx) return UWW_ERR_INVALID_ARG;
-    int st = check_out(h_out);
+    int st = check_out(h_out, false);
     if (st) return st;
     if (n && !h_chunks) return UWW_ERR_INVALID_ARG;
     const bool want_cases = (ctx->params.outputs & UWW_OUT_CASES) && h_out->cases;
@@ -539,38 +560,45 @@ int uww_build_chunks_host(uww_ctx* ctx, const uww_chunk_desc* h_chunks, uint32_t
     d_out.totals = reinterpret_cast<uint64_t*>(ctx->d_totals);
     d_out.vert_capacity = h_out->vert_capacity;
     d_out.ind_capacity = h_out->ind_capacity;
-    if ((st = launch(ctx, ctx->d_chunks, n, max_cells, &d_out, true))) return st;
 
-    // Page-locked host buffers the device can address: one copy kernel that
-    // reads the vertex and index counts on the device, then one
-    // synchronisation.  Otherwise the copies are sized on the host after a
-    // first synchronisation.
+    // Page-locked host buffers the device can address: the build streams
+    // records, indices, vertices and normals into them as chunks finish (the
+    // transfer overlaps the build), a copy kernel adds cases and samples, and
+    // the host synchronises once.  Otherwise the copies are sized on the host
+    // after a first synchronisation.
     void* dv = device_view(h_out->verts);
     void* dn = want_normals ? device_view(h_out->normals) : nullptr;
     void* di = device_view(h_out->inds);
     void* dr = device_view(h_out->records);
     void* dc = want_cases ? device_view(h_out->cases) : nullptr;
     void* ds = want_samples ? device_view(h_out->samples) : nullptr;
-    if (dv && di && dr && (!want_normals || dn) && (!want_cases || dc) && (!want_samples || ds)) {
+    // (the streamed words are 4-byte stores: host buffers off a 4-byte boundary take the copy path)
+    const bool words_ok = aligned_to(dv, 4) && aligned_to(dn, 4) && aligned_to(di, 4) && aligned_to(dr, 4);
+    if (dv && di && dr && words_ok && (!want_normals || dn) && (!want_cases || dc) && (!want_samples || ds)) {
+        HostOut ho;
+        ho.verts = static_cast<uww_vert_color*>(dv);
+        ho.normals = static_cast<float*>(dn);
+        ho.inds = static_cast<uint32_t*>(di);
+        ho.records = static_cast<uww_chunk_record*>(dr);
+        ho.totals = static_cast<unsigned long long*>(device_view(ctx->h_totals));
+        if ((st = launch(ctx, ctx->d_chunks, n, max_cells, &d_out, true, nullptr, 0, nullptr, nullptr, false, &ho)))
+            return st;
         CopyOut c;
         std::memset(&c, 0, sizeof(c));
-        auto seg = [&](const void* src, void* dst, unsigned long long fixed, int idx, uint32_t eb, unsigned long long cap) {
+        auto seg = [&](const void* src, void* dst, unsigned long long fixed) {
             CopySeg& g = c.seg[c.nseg++];
             g.src = static_cast<const uint8_t*>(src);
             g.dst = static_cast<uint8_t*>(dst);
             g.fixed_bytes = fixed;
-            g.count_idx = idx;
-            g.elem_bytes = eb;
-            g.cap_elems = cap;
+            g.count_idx = -1;
+            g.elem_bytes = 0;
+            g.cap_elems = 0;
         };
-        seg(ctx->d_records, dr, (unsigned long long)n * sizeof(uww_chunk_record), -1, 0, 0);
-        seg(ctx->d_verts, dv, 0, 0, sizeof(uww_vert_color), h_out->vert_capacity);
-        seg(ctx->d_inds, di, 0, 1, sizeof(uint32_t), h_out->ind_capacity);
-        if (want_normals) seg(ctx->d_normals, dn, 0, 0, 12, h_out->vert_capacity);
-        if (want_cases && case_bytes) seg(ctx->d_cases, dc, case_bytes, -1, 0, 0);
-        if (want_samples && sample_count) seg(ctx->d_samples, ds, sample_count * 4, -1, 0, 0);
+        if (want_cases && case_bytes) seg(ctx->d_cases, dc, case_bytes);
+        if (want_samples && sample_count) seg(ctx->d_samples, ds, sample_count * 4);
         if ((e = launch_copy_out(c, ctx->d_totals, ctx->num_sms * 2, s)) != cudaSuccess) return cuda_status(e);
-        if ((e = cudaMemcpyAsync(ctx->h_totals, ctx->d_totals, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+        if (!ho.totals &&
+            (e = cudaMemcpyAsync(ctx->h_totals, ctx->d_totals, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s)) != cudaSuccess)
             return cuda_status(e);
         if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_status(e);
         if (h_out->totals) std::memcpy(h_out->totals, ctx->h_totals, 4 * sizeof(uint64_t));
@@ -580,6 +608,7 @@ int uww_build_chunks_host(uww_ctx* ctx, const uww_chunk_desc* h_chunks, uint32_t
         return UWW_OK;
     }
 
+    if ((st = launch(ctx, ctx->d_chunks, n, max_cells, &d_out, true))) return st;
     if ((e = cudaMemcpyAsync(h_out->records, ctx->d_records, (size_t)n * sizeof(uww_chunk_record), cudaMemcpyDeviceToHost, s)) != cudaSuccess)
         return cuda_status(e);
     if ((e = cudaMemcpyAsync(ctx->h_totals, ctx->d_totals, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s)) != cudaSuccess)

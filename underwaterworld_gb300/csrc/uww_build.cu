@@ -258,6 +258,7 @@ __device__ __forceinline__ void chunk_record(const BuildArgs& a, SmemTables& T, 
     rec.num_active_cells = nA;
     rec.reserved[0] = rec.reserved[1] = 0;
     a.records[ci.ticket] = rec;
+    if (a.host_records) a.host_records[ci.ticket] = rec;
     if (!queue || ci.ticket == T.n - 1) {
         a.totals[0] = ev + nV;
         a.totals[1] = ei + nI;
@@ -457,31 +458,64 @@ __device__ void chunk_front(const DevParams& p, const BuildArgs& a, SmemTables& 
 // colour slot 0, the owner's corner b (the value ramp's input, chunk.rs:215);
 // write its colour and unit normal.
 template <class O>
-__device__ __forceinline__ void finish_vertex(const DevParams& p, const uint8_t* P, const float4* gp,
-                                              uww_vert_color* verts, float* normals, uint32_t v, bool want_color,
-                                              bool want_normals)
+__device__ __forceinline__ void vertex_outputs(const DevParams& p, const uint8_t* P, const float4* gp,
+                                               const uww_vert_color* verts, uint32_t v, bool want_color,
+                                               bool want_normals, float2 out[3], float g[3])
 {
-    float2* v2 = reinterpret_cast<float2*>(verts + v);
+    const float2* v2 = reinterpret_cast<const float2*>(verts + v);
     const float2 p01 = v2[0], p2c = v2[1];
     const int cb = (int)p2c.y;
+    out[0] = p01;
     if (want_color) {
         float col[3];
         vertex_color<O>(p, p2c.x, cb, col);
-        v2[1] = make_float2(p2c.x, col[0]);
-        v2[2] = make_float2(col[1], col[2]);
+        out[1] = make_float2(p2c.x, col[0]);
+        out[2] = make_float2(col[1], col[2]);
     } else {
-        v2[1] = make_float2(p2c.x, 0.f);
+        out[1] = make_float2(p2c.x, 0.f);
+        out[2] = make_float2(0.f, 0.f);
     }
     if (want_normals) {
-        float g[3];
         if constexpr (std::is_same<O, FastOps>::value)
             density_grad_fast(p, P, gp, p01.x, p01.y, p2c.x, g);
         else
             density<O, true>(p, P, p01.x, p01.y, p2c.x, g);
         safe_normalize<O>(g);
+    }
+}
+
+template <class O>
+__device__ __forceinline__ void finish_vertex(const DevParams& p, const uint8_t* P, const float4* gp,
+                                              uww_vert_color* verts, float* normals, uint32_t v, bool want_color,
+                                              bool want_normals)
+{
+    float2 out[3];
+    float g[3];
+    vertex_outputs<O>(p, P, gp, verts, v, want_color, want_normals, out, g);
+    float2* v2 = reinterpret_cast<float2*>(verts + v);
+    v2[1] = out[1];
+    v2[2] = out[2];
+    if (want_normals) {
         float* nn = normals + 3 * (size_t)v;
         nn[0] = g[0]; nn[1] = g[1]; nn[2] = g[2];
     }
+}
+
+// Copy n 32-bit words, by threads tid, tid + nt, ...: 16-byte words where
+// dst and src sit at the same offset from a 16-byte boundary, single words
+// otherwise.  Used for output bound for page-locked host memory, where wide
+// stores make the fewest transfers.
+__device__ __forceinline__ void copy_words(uint32_t* dst, const uint32_t* src, uint32_t n, int tid, int nt)
+{
+    uint32_t head = n;
+    if ((((uintptr_t)dst ^ (uintptr_t)src) & 15) == 0)
+        head = min(n, (uint32_t)((16 - ((uintptr_t)src & 15)) & 15) / 4);
+    for (uint32_t i = tid; i < head; i += nt) dst[i] = src[i];
+    const uint32_t n4 = (n - head) / 4;
+    const uint4* s4 = reinterpret_cast<const uint4*>(src + head);
+    uint4* d4 = reinterpret_cast<uint4*>(dst + head);
+    for (uint32_t i = tid; i < n4; i += nt) d4[i] = s4[i];
+    for (uint32_t i = head + 4 * n4 + tid; i < n; i += nt) dst[i] = src[i];
 }
 
 // Emission of a chunk from workspace `buf`, given its offsets.  Every compute
@@ -564,12 +598,26 @@ __device__ void chunk_emit(const DevParams& p, const BuildArgs& a, SmemTables& T
             }
         }
     }
-    // pass 2 (colour and normal per vertex): inline for one chunk per launch;
-    // the batched form runs it as vertex_kernel over the whole batch
-    if (!QUEUE && (want_color || want_normals)) {
+    // pass 2 (colour and normal per vertex): inline for one chunk per launch
+    // and for streamed host output; otherwise the batched form runs it as
+    // vertex_kernel over the whole batch
+    const bool stream_host = QUEUE && a.host_verts != nullptr;
+    if ((!QUEUE || stream_host) && (want_color || want_normals)) {
         bar_sync(kBarCompute, ncomp);
         for (uint32_t vid = tid; vid < nV; vid += ncomp)
             finish_vertex<O>(p, T.perm, T.gp, a.verts, a.normals, voff + vid, want_color, want_normals);
+    }
+    // streamed host output: the finished chunk, just written by this CTA,
+    // goes on to host memory in 16-byte words while later chunks build
+    if (stream_host) {
+        bar_sync(kBarCompute, ncomp);
+        const uint32_t nI = (uint32_t)((ci.total >> kIndShift) & kField22);
+        copy_words(a.host_inds + ioff, a.inds + ioff, nI, tid, ncomp);
+        copy_words(reinterpret_cast<uint32_t*>(a.host_verts + voff), reinterpret_cast<const uint32_t*>(a.verts + voff),
+                   6 * nV, tid, ncomp);
+        if (want_normals && a.host_normals)
+            copy_words(reinterpret_cast<uint32_t*>(a.host_normals + 3 * (size_t)voff),
+                       reinterpret_cast<const uint32_t*>(a.normals + 3 * (size_t)voff), 3 * nV, tid, ncomp);
     }
 }
 
@@ -697,10 +745,19 @@ __global__ void __launch_bounds__(MAXT, MINB) build_kernel(const DevParams p, co
         for (uint32_t i = tid; i < T.n; i += nthr) a.lookback[i] = 0ull;
         if (tid == 0) {
             if (T.n == 0) { a.totals[0] = 0ull; a.totals[1] = 0ull; }
-            a.totals[2] = atomicExch(&a.acc[0], 0ull);
-            a.totals[3] = atomicExch(&a.acc[1], 0ull);
+            const unsigned long long t2 = atomicExch(&a.acc[0], 0ull), t3 = atomicExch(&a.acc[1], 0ull);
+            a.totals[2] = t2;
+            a.totals[3] = t3;
             atomicExch(&a.acc[2], 0ull);
             atomicExch(a.work_counter, 0u);
+            if (a.host_totals) {
+                // totals[0..1] came from the CTA that recorded the last ticket,
+                // published before its count of finished CTAs
+                a.host_totals[0] = __ldcg(&a.totals[0]);
+                a.host_totals[1] = __ldcg(&a.totals[1]);
+                a.host_totals[2] = t2;
+                a.host_totals[3] = t3;
+            }
         }
     }
 }
@@ -841,7 +898,8 @@ cudaError_t launch_build(const DevParams& p, const BuildArgs& a, bool queue, int
     const bool exact = p.math_mode == UWW_MATH_EXACT;
     kernel_for(exact, queue, threads > 224)<<<grid, threads, dyn_smem, s>>>(p, a);
     cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess || !queue || !(p.outputs & (UWW_OUT_COLOR | UWW_OUT_NORMALS))) return e;
+    // streamed host output finishes its vertices inside the build kernel
+    if (e != cudaSuccess || !queue || a.host_verts || !(p.outputs & (UWW_OUT_COLOR | UWW_OUT_NORMALS))) return e;
     // the batched form's pass 2, over the whole batch
     int dev = 0, sms = 0;
     e = cudaGetDevice(&dev);

@@ -90,6 +90,16 @@ struct BuildArgs {
     long long spin_limit_cycles;     // bound on every device-side wait
     uint32_t* edge_ids;              // optional, per output vertex: (first corner sample << 3) | direction
     const uint32_t* n_dev;           // optional device chunk count; the launch builds min(*n_dev, n)
+    // Optional streamed host output (batched form): device addresses of
+    // page-locked host memory.  Pass 2 then runs inside the build kernel, and
+    // each chunk's record, indices, vertices and normals go there as soon as
+    // the chunk is finished (`verts`, `normals` and `inds` still receive the
+    // output), so the transfer to the host overlaps the build.
+    uint32_t* host_inds;
+    uww_chunk_record* host_records;
+    uww_vert_color* host_verts;
+    float* host_normals;
+    unsigned long long* host_totals;  // optional copy of the four totals, by the last CTA (queue mode)
 };
 
 // Device -> mapped-host copy of a build's outputs (uww_build.cu).
@@ -135,6 +145,17 @@ int prepare_batched(uww_ctx* ctx, uint32_t n, uint32_t max_cells, const uww_mesh
 int plan_batched(uww_ctx* ctx, uint32_t n, uint32_t max_cells, int* threads, int* grid, size_t* dyn_smem);
 // (re)allocate *ptr to at least `bytes` of device memory (contents not kept)
 int ensure_device_bytes(void** ptr, size_t* cap, size_t bytes);
+// The build writes vertex positions and the totals with 8-byte stores and
+// everything else (descriptors read) with 4-byte words: device buffers that
+// are not aligned to match are refused with UWW_ERR_INVALID_ARG before any
+// launch, instead of faulting in the kernel.
+inline bool aligned_to(const void* p, uintptr_t a) { return ((uintptr_t)p & (a - 1)) == 0; }
+inline bool device_out_aligned(const uww_mesh_out* o)
+{
+    return aligned_to(o->verts, 8) && aligned_to(o->normals, 4) && aligned_to(o->inds, 4) &&
+           aligned_to(o->records, 4) && aligned_to(o->totals, 8) && aligned_to(o->samples, 4);
+}
+
 template <class T>
 int ensure_device_of(T** ptr, size_t* cap, size_t bytes)
 {

@@ -97,6 +97,7 @@ extern "C" int uww_build_chunks_noalloc(const uww_params* params, void* stream, 
     if (st) return st;
     if (!out || !out->verts || !out->inds || !out->records) return UWW_ERR_INVALID_ARG;
     if (out->vert_capacity > kLbVertMax) return UWW_ERR_INVALID_ARG;
+    if (!device_out_aligned(out)) return UWW_ERR_INVALID_ARG;
     if (max_cells < 1 || max_cells > UWW_MAX_CELLS) return UWW_ERR_INVALID_ARG;
     if (n > kNoAllocMaxChunks) return UWW_ERR_INVALID_ARG;  // beyond the fixed scratch
     cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -104,7 +105,7 @@ extern "C" int uww_build_chunks_noalloc(const uww_params* params, void* stream, 
         if (out->totals) return status_from_cuda(cudaMemsetAsync(out->totals, 0, 4 * sizeof(uint64_t), s), "cudaMemsetAsync");
         return UWW_OK;
     }
-    if (!d_chunks) return UWW_ERR_INVALID_ARG;
+    if (!d_chunks || !aligned_to(d_chunks, 4)) return UWW_ERR_INVALID_ARG;
 
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
