@@ -86,6 +86,7 @@ struct SmemTables {
     uint8_t owner[2][8][12];      // UWW_EDGE_OWNER
     uint8_t corners[12][2];
     uint16_t owned[2][64];        // [oriented?][boundary flags] -> owned edge mask
+    uint16_t first_ref[256];      // per case: row positions that are their edge's first reference
     unsigned long long warp_sums[32];
     unsigned long long chunk_total;
     ChunkInfo ci[2];              // the chunks in flight (front / back)
@@ -542,26 +543,38 @@ __device__ void chunk_emit(const DevParams& p, const BuildArgs& a, SmemTables& T
     {
         const float s = __fdiv_rn((float)p.chunk_size, (float)N);
         const float iso = p.iso_level;
-        for (uint32_t ai = tid; ai < nA; ai += ncomp) {
+        // one thread per triangle of the chunk's index stream, so a dense
+        // chunk's emission is spread over the CTA like a sparse one's; a
+        // triangle's cell is the last active cell whose first index position
+        // is at or before it
+        const uint32_t nT = (uint32_t)((ci.total >> kIndShift) & kField22) / 3u;
+        for (uint32_t t = tid; t < nT; t += ncomp) {
+            const uint32_t g = 3u * t;
+            uint32_t ai = 0, len = nA;
+            while (len > 1) {
+                const uint32_t h = len >> 1;
+                if (W.get_ibase(ai + h) <= g) ai += h;
+                len -= h;
+            }
             const int c = W.get_active(ai);
             const int x = c / (N * N), y = (c / N) % N, z = c % N;
             const int cs = cases[c];
             const int8_t* row = T.tri[cs];
             const unsigned own_mask = T.owned[oriented][boundary_flags(x, y, z, N)];
+            const unsigned fr = T.first_ref[cs];
             const uint32_t vb = W.get_vbase(c);
-            const uint32_t ib = W.get_ibase(ai);
-            unsigned seen = 0;
+            const int j0 = (int)(g - W.get_ibase(ai));
             const uint16_t* before = UWW_EDGE_BEFORE[cs];
-            const int nidx = 3 * T.ntri[cs];
-            for (int i = 0; i < nidx; ++i) {
+#pragma unroll
+            for (int m = 0; m < 3; ++m) {
+                const int i = j0 + m;
                 const int e = row[i];
                 const unsigned bit = 1u << e;
                 uint32_t id;
                 if (own_mask & bit) {
                     // the cell numbers its owned edges' vertices in first-reference order
                     id = vb + __popc(own_mask & __ldg(before + e));
-                    if (!(seen & bit)) {
-                        seen |= bit;
+                    if ((fr >> i) & 1u) {
                         const int ca = T.corners[e][0], cb = T.corners[e][1];
                         const int ax = x + ((0x66 >> ca) & 1), ay = y + (ca >> 2), az = z + ((0xcc >> ca) & 1);
                         const int bx = x + ((0x66 >> cb) & 1), by = y + (cb >> 2), bz = z + ((0xcc >> cb) & 1);
@@ -569,10 +582,10 @@ __device__ void chunk_emit(const DevParams& p, const BuildArgs& a, SmemTables& T
                         const float ibv = rho[(bx * S + by) * S + bz];
                         const float sax = O::mul((float)ax, s), say = O::mul((float)ay, s), saz = O::mul((float)az, s);
                         const float sbx = O::mul((float)bx, s), sby = O::mul((float)by, s), sbz = O::mul((float)bz, s);
-                        const float t = O::div(O::sub(iso, ia), O::sub(ibv, ia));
-                        const float mx = O::add(sax, O::mul(t, O::sub(sbx, sax)));
-                        const float my = O::add(say, O::mul(t, O::sub(sby, say)));
-                        const float mz = O::add(saz, O::mul(t, O::sub(sbz, saz)));
+                        const float tt = O::div(O::sub(iso, ia), O::sub(ibv, ia));
+                        const float mx = O::add(sax, O::mul(tt, O::sub(sbx, sax)));
+                        const float my = O::add(say, O::mul(tt, O::sub(sby, say)));
+                        const float mz = O::add(saz, O::mul(tt, O::sub(sbz, saz)));
                         if (a.edge_ids) {
                             // direction of corner b from corner a: +x -x +y -y +z -z
                             const int dir = bx != ax ? (bx < ax) : by != ay ? 2 + (by < ay) : 4 + (bz < az);
@@ -594,7 +607,7 @@ __device__ void chunk_emit(const DevParams& p, const BuildArgs& a, SmemTables& T
                     const unsigned oown = T.owned[oriented][boundary_flags(qx, qy, qz, N)];
                     id = W.get_vbase(oc) + __popc(oown & __ldg(&UWW_EDGE_BEFORE[cases[oc]][oe]));
                 }
-                a.inds[ioff + ib + i] = id;
+                a.inds[ioff + g + m] = id;
             }
         }
     }
@@ -663,6 +676,15 @@ __global__ void __launch_bounds__(MAXT, MINB) build_kernel(const DevParams p, co
     for (int i = tid; i < 2 * 8 * 12; i += nthr) (&T.owner[0][0][0])[i] = __ldg(&UWW_EDGE_OWNER[0][0][0] + i);
     for (int i = tid; i < 24; i += nthr) (&T.corners[0][0])[i] = __ldg(&UWW_EDGE_CORNERS[0][0] + i);
     __syncthreads();
+    for (int cs = tid; cs < 256; cs += nthr) {
+        unsigned seen = 0, fr = 0;
+        for (int i = 0; i < 15 && T.tri[cs][i] >= 0; ++i) {
+            const unsigned bit = 1u << T.tri[cs][i];
+            if (!(seen & bit)) fr |= 1u << i;
+            seen |= bit;
+        }
+        T.first_ref[cs] = (uint16_t)fr;
+    }
     for (int i = tid; i < 256; i += nthr) {
         float gx, gy, gz;
         grad_vec(T.perm[i], gx, gy, gz);
