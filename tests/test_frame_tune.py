@@ -60,6 +60,29 @@ def test_frame_graph_matches_direct_builds(ctx_factory):
     fb.close()
 
 
+def test_frame_graph_recaptures_after_work_buffers_grow(ctx_factory):
+    """A larger build on the same context reallocates the look-back words and
+    the global scratch the captured graph refers to; the next frame launch
+    recaptures the graph instead of using the freed buffers."""
+    p, d = workloads.uniform_grid(seed=3, outputs=OUT)
+    p.math_mode = abi.UWW_MATH_FAST
+    ctx = ctx_factory(p)
+    vcap, icap = 1 << 20, 1 << 22
+    fb = FrameBuilder(ctx, 512, 12, vcap, icap)
+    sel = d[:512]
+    rec0, tot0 = fb.build(sel)
+    # 8192 chunks (more look-back words) and 24-cell chunks (global scratch)
+    big = make_descs(np.concatenate([d["pos"], d["pos"] + np.array([0, 0, 16], np.int32)]), 12)
+    direct_build(ctx, big, 1 << 21, 1 << 23)
+    direct_build(ctx, make_descs(d["pos"][:64], 24), 1 << 21, 1 << 23)
+    rec, tot = fb.build(sel)
+    np.testing.assert_array_equal(rec, rec0)
+    np.testing.assert_array_equal(tot[:3], tot0[:3])
+    want = direct_build(ctx, sel, vcap, icap)
+    np.testing.assert_array_equal(rec, want.records)
+    fb.close()
+
+
 def test_frame_graph_rejects_a_count_above_its_maximum(ctx_factory):
     p, d = workloads.uniform_grid(seed=0)
     ctx = ctx_factory(p)

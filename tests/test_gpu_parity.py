@@ -360,3 +360,31 @@ def test_misaligned_device_outputs_are_refused(ctx_factory):
     assert run(dd.data_ptr() + 2) == abi.UWW_ERR_INVALID_ARG
     assert run(dd.data_ptr()) == abi.UWW_OK
     torch.cuda.synchronize()
+
+
+def test_surface_layer_bit_exact(ctx_factory, oracle):
+    """A layer of 1024 chunks on the surface, nearly all meshed: the batched
+    build's look-back, emission and vertex pass under a dense work queue."""
+    p = workloads.fbm_params(5, 4, 0.04, -0.03, 128.0, 0.0, ALL)
+    g = np.arange(32)
+    pos = np.stack(np.meshgrid(g, g, [8], indexing="ij"), -1).reshape(-1, 3)
+    d = make_descs(pos, 12)
+    ref = oracle.build_chunks(p, d)
+    meshed = int((ref.records["flags"] & abi.UWW_CHUNK_HAS_MESH).astype(bool).sum())
+    assert meshed > 900, meshed
+    got = ctx_factory(p).build_chunks_device(d, *caps(ref))
+    assert_batches_equal(got, ref)
+
+
+def test_dense_meshes_bit_exact(ctx_factory, oracle):
+    """Dense meshes (high frequency, no depth bias): thousands of triangles
+    per chunk, emitted a triangle per thread over many rounds."""
+    p = workloads.fbm_params(6, 2, 0.3, 0.0, 0.0, 0.0, ALL)
+    g = np.arange(8)
+    pos = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)
+    d = make_descs(pos, 12)
+    ref = oracle.build_chunks(p, d)
+    tris = ref.records["num_inds"].astype(np.int64) // 3
+    assert tris.min() > 3000, tris.min()
+    got = ctx_factory(p).build_chunks_device(d, *caps(ref))
+    assert_batches_equal(got, ref)

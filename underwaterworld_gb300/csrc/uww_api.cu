@@ -198,8 +198,16 @@ int launch(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint32_t ma
     LaunchCfg cfg;
     int st = plan_launch(ctx, n, max_cells, queue, &cfg);
     if (st) return st;
+    // the work buffers a captured frame graph refers to: a reallocation
+    // moves the context's generation on, and such a frame recaptures itself
+    auto grow = [ctx](auto** ptr, size_t* cap, size_t bytes) {
+        const void* old = *ptr;
+        const int r = ensure_device(ptr, cap, bytes);
+        if (*ptr != old) ++ctx->work_gen;
+        return r;
+    };
     if (cfg.scratch_slot) {
-        st = ensure_device(&ctx->d_scratch, &ctx->scratch_cap, cfg.scratch_slot * cfg.slots * (size_t)cfg.grid);
+        st = grow(&ctx->d_scratch, &ctx->scratch_cap, cfg.scratch_slot * cfg.slots * (size_t)cfg.grid);
         if (st) return st;
     }
     if (prepare_only && !queue) return UWW_OK;
@@ -242,8 +250,7 @@ int launch(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint32_t ma
         // launch starts: zeroed once here on (re)allocation, and reset by the
         // last CTA of every launch.  So a batched build is one kernel launch.
         if (!ctx->d_lookback || ctx->lookback_cap < (size_t)n * sizeof(unsigned long long)) {
-            st = ensure_device(&ctx->d_lookback, &ctx->lookback_cap,
-                               std::max<size_t>((size_t)n, 4096) * sizeof(unsigned long long));
+            st = grow(&ctx->d_lookback, &ctx->lookback_cap, std::max<size_t>((size_t)n, 4096) * sizeof(unsigned long long));
             if (st) return st;
             cudaError_t e = cudaMemsetAsync(ctx->d_lookback, 0, ctx->lookback_cap, ctx->stream);
             if (e != cudaSuccess) return cuda_status(e, "cudaMemsetAsync");

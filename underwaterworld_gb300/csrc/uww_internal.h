@@ -189,6 +189,7 @@ struct uww_ctx {
     unsigned long long* d_totals = nullptr;
     uint8_t* d_scratch = nullptr;
     size_t scratch_cap = 0;
+    uint64_t work_gen = 0;  // moves on whenever d_scratch or d_lookback is reallocated
 
     // buffers of the host-buffer path
     uww_chunk_desc* d_chunks = nullptr;

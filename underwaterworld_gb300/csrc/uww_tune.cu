@@ -33,6 +33,7 @@ struct uww_frame {
     uint32_t* d_count = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
+    uint64_t gen = 0;  // the context's work-buffer generation the graph was captured with
 };
 
 namespace {
@@ -66,6 +67,32 @@ int capture_frame(uww_frame* f, cudaGraph_t* out)
         return status_from_cuda(ce != cudaSuccess ? ce : e, "frame capture");
     }
     *out = g;
+    f->gen = ctx->work_gen;
+    return UWW_OK;
+}
+
+// Capture the frame again and update the executable graph with it
+// (re-instantiated when the launch shape changed).
+int recapture_frame(uww_frame* f)
+{
+    cudaGraph_t g = nullptr;
+    int st = capture_frame(f, &g);
+    if (st) return st;
+    cudaGraphExecUpdateResultInfo info;
+    cudaError_t e = cudaGraphExecUpdate(f->exec, g, &info);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        cudaGraphExec_t x = nullptr;
+        e = cudaGraphInstantiate(&x, g, 0);
+        if (e != cudaSuccess) {
+            cudaGraphDestroy(g);
+            return status_from_cuda(e, "cudaGraphInstantiate");
+        }
+        cudaGraphExecDestroy(f->exec);
+        f->exec = x;
+    }
+    cudaGraphDestroy(f->graph);
+    f->graph = g;
     return UWW_OK;
 }
 
@@ -168,6 +195,11 @@ int uww_frame_launch(uww_frame* f)
 {
     if (!f || !f->exec) return UWW_ERR_INVALID_ARG;
     if (*f->h_count > f->max_chunks) return UWW_ERR_INVALID_ARG;
+    // another build on the context reallocated a work buffer the graph uses
+    if (f->gen != f->ctx->work_gen) {
+        const int st = recapture_frame(f);
+        if (st) return st;
+    }
     return status_from_cuda(cudaGraphLaunch(f->exec, f->ctx->stream), "cudaGraphLaunch");
 }
 
@@ -176,26 +208,7 @@ int uww_frame_set_params(uww_frame* f, const uww_params* p)
     if (!f) return UWW_ERR_INVALID_ARG;
     int st = uww_ctx_set_params(f->ctx, p);
     if (st) return st;
-    cudaGraph_t g = nullptr;
-    st = capture_frame(f, &g);
-    if (st) return st;
-    cudaGraphExecUpdateResultInfo info;
-    cudaError_t e = cudaGraphExecUpdate(f->exec, g, &info);
-    if (e != cudaSuccess) {
-        // the new launch shape differs (another kernel or block size): re-instantiate
-        cudaGetLastError();
-        cudaGraphExec_t x = nullptr;
-        e = cudaGraphInstantiate(&x, g, 0);
-        if (e != cudaSuccess) {
-            cudaGraphDestroy(g);
-            return status_from_cuda(e, "cudaGraphInstantiate");
-        }
-        cudaGraphExecDestroy(f->exec);
-        f->exec = x;
-    }
-    cudaGraphDestroy(f->graph);
-    f->graph = g;
-    return UWW_OK;
+    return recapture_frame(f);
 }
 
 int uww_frame_destroy(uww_frame* f)
