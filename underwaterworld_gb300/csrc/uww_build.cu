@@ -345,8 +345,8 @@ __device__ void chunk_front(const DevParams& p, const BuildArgs& a, SmemTables& 
     uint8_t* cases = W.cases;
     const int ox = d.pos[0] * p.chunk_size, oy = d.pos[1] * p.chunk_size, oz = d.pos[2] * p.chunk_size;
 
-    // ---- density grid (build_iso) + early blank vote ----
-    int inside = 0;
+    // ---- density grid (build_iso) + early blank and solid votes ----
+    int inside = 0, outside = 0;
     if (!bad) {
         const float s = __fdiv_rn((float)p.chunk_size, (float)N);  // SIZE_SCALE
         const int S2 = S * S, S3 = S2 * S;
@@ -356,12 +356,15 @@ __device__ void chunk_front(const DevParams& p, const BuildArgs& a, SmemTables& 
                 const float v = src[idx];
                 rho[idx] = v;
                 inside |= !(v > p.iso_level);
+                outside |= !(v < p.iso_level);
             }
         } else if constexpr (std::is_same<O, FastOps>::value) {
             const ZTable zt = ztable_at(dyn_smem + a.ztable_offset, S, p.octaves);
             // a chunk in a global scratch slot accumulates its columns in local memory
-            inside = (uint32_t)N <= a.smem_cells ? sample_columns_fast<false>(p, T.perm, T.gp, zt, rho, N, ox, oy, oz, ncomp)
-                                                 : sample_columns_fast<true>(p, T.perm, T.gp, zt, rho, N, ox, oy, oz, ncomp);
+            const int io = (uint32_t)N <= a.smem_cells ? sample_columns_fast<false>(p, T.perm, T.gp, zt, rho, N, ox, oy, oz, ncomp)
+                                                       : sample_columns_fast<true>(p, T.perm, T.gp, zt, rho, N, ox, oy, oz, ncomp);
+            inside = io & 1;
+            outside = io >> 1;
         } else {
             for (int idx = tid; idx < S3; idx += ncomp) {
                 const int x = idx / S2, r = idx - x * S2, y = r / S, z = r - y * S;
@@ -371,10 +374,14 @@ __device__ void chunk_front(const DevParams& p, const BuildArgs& a, SmemTables& 
                 const float v = density<O, false>(p, T.perm, wx, wy, wz, nullptr);
                 rho[idx] = v;
                 inside |= !(v > p.iso_level);
+                outside |= !(v < p.iso_level);
             }
         }
     }
     const int any_inside = bar_or(kBarCompute, ncomp, inside);
+    // every sample below the iso level: every case is 255, no cell is
+    // crossed, nothing to classify
+    const int solid = bar_and(kBarCompute, ncomp, !outside);
     // tell the control warp the noise is done: it now resolves the previous
     // chunk's look-back while this chunk is classified
     if (QUEUE) bar_arrive(kBarNoiseDone, nall);
@@ -384,10 +391,10 @@ __device__ void chunk_front(const DevParams& p, const BuildArgs& a, SmemTables& 
     }
 
     unsigned long long total = 0ull;
-    if (bad || !any_inside) {
+    if (bad || !any_inside || solid) {
         if (QUEUE && tid == 0) lookback_publish(a, ticket, 0ull);
         if (!bad && cases_ok)
-            for (int c = tid; c < NC; c += ncomp) a.cases[(size_t)d.cell_offset + c] = 0;
+            for (int c = tid; c < NC; c += ncomp) a.cases[(size_t)d.cell_offset + c] = solid ? 255 : 0;
     } else {
         // ---- classify + count, contiguous runs of cells per thread ----
         const int R = (NC + ncomp - 1) / ncomp;

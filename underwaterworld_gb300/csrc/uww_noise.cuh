@@ -43,6 +43,20 @@ __device__ __forceinline__ int bar_or(int id, int count, int pred)
     return r;
 }
 
+__device__ __forceinline__ int bar_and(int id, int count, int pred)
+{
+    int r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.s32 p, %1, 0;\n\t"
+        "bar.red.and.pred q, %2, %3, p;\n\t"
+        "selp.s32 %0, 1, 0, q;\n\t}"
+        : "=r"(r)
+        : "r"(pred), "r"(id), "r"(count)
+        : "memory");
+    return r;
+}
+
 // ---------------------------------------------------------------------------
 // Fast-build density grid, one compute thread per (x, y) column of samples.
 //
@@ -191,6 +205,9 @@ __device__ __forceinline__ ZTable ztable_at(uint8_t* base, int S, int octaves)
     return t;
 }
 
+// Returns bit 0: a sample of this thread's columns is not above the iso
+// level (the early blank vote); bit 1: one is not below it (its corner bit in
+// a cell's case stays clear).
 // COLBUF: accumulate each column in a per-thread buffer (local memory, L1)
 // and write it to rho once, for rho in global memory where an accumulate per
 // sample and octave would be an L2 round trip each.
@@ -231,7 +248,7 @@ __device__ __forceinline__ int sample_columns_fast(const DevParams& p, const uin
     }
     bar_sync(kBarCompute, ncomp);
 
-    int inside = 0;
+    int inside = 0, outside = 0;
     for (int col = threadIdx.x; col < SS; col += ncomp) {
         const int x = col / S, y = col - x * S;
         float colbuf[COLBUF ? UWW_MAX_CELLS + 1 : 1];
@@ -264,7 +281,10 @@ __device__ __forceinline__ int sample_columns_fast(const DevParams& p, const uin
                 for (int z = zb; z < ze; ++z) {
                     const float r0 = __fadd_rn(run_value(q, dzc[z]), first ? Z.bias[z] : out[z]);
                     out[z] = r0;
-                    if (last) inside |= !(r0 > iso);
+                    if (last) {
+                        inside |= !(r0 > iso);
+                        outside |= !(r0 < iso);  // a case bit stays clear
+                    }
                 }
             }
         }
@@ -273,7 +293,7 @@ __device__ __forceinline__ int sample_columns_fast(const DevParams& p, const uin
             for (int z = 0; z < S; ++z) dst[z] = colbuf[z];
         }
     }
-    return inside;
+    return inside | (outside << 1);
 }
 
 
