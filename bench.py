@@ -156,6 +156,29 @@ def workload(seed):
     return workloads.uniform_grid(seed=seed, outputs=abi.UWW_OUT_COLOR | abi.UWW_OUT_NORMALS)
 
 
+def bias_decided(params, descs) -> int:
+    """How many chunks the build decides from the depth bias alone (without
+    their noise): a float32 restatement of the kernel's test (fBm bound
+    3/2 * |norm| * sum|amp|, margin 1e-3 (1 + B + |bias|)), used to count the
+    noise flops the build actually performs."""
+    f32 = np.float32
+    amps = np.array([params.amplitude * params.persistence ** k for k in range(params.octaves)], np.float64)
+    scale = f32(1.1547005383792515)
+    norm = scale / f32(amps.sum()) if params.normalize else scale
+    B = f32(1.5) * abs(norm) * f32(np.abs(amps).sum())
+    cells = descs["cells"].astype(np.int64)
+    oz = descs["pos"][:, 2].astype(np.int64) * 16
+    s = (f32(16) / cells.astype(f32)).astype(f32)
+    if params.bias_mode != 2:  # linear only here (the workloads measured use it)
+        return 0
+    b0 = f32(params.bias_a) * (oz.astype(f32) - f32(params.bias_b))
+    b1 = f32(params.bias_a) * ((cells.astype(f32) * s + oz.astype(f32)).astype(f32) - f32(params.bias_b))
+    lo, hi = np.minimum(b0, b1), np.maximum(b0, b1)
+    m = f32(1e-3) * (f32(1) + B + np.maximum(np.abs(lo), np.abs(hi)))
+    iso = f32(params.iso_level)
+    return int(((lo - B - m > iso) | (hi + B + m < iso)).sum())
+
+
 def cpu_reference(descs, seeds, threads, budget_s=20.0):
     """The reference algorithm on the host: oracle in f64 reference semantics with
     the O(V) dedup search and colours (no normals, like the reference)."""
@@ -647,7 +670,10 @@ def main():
         pk.append(fl.value / (e0.elapsed_time(e1) * 1e-3))
     fp32_peak = max(pk) / 1e12
 
-    samples = n * 13 ** 3
+    # the noise flops the build performs: chunks decided by the depth bias
+    # alone evaluate none
+    decided = bias_decided(params[0], descs)
+    samples = (n - decided) * 13 ** 3
     mean_v, mean_i = verts_sum / args.steps, inds_sum / args.steps
     oct_ = params[0].octaves
     flops = samples * (oct_ * FLOPS_PER_OCTAVE + FLOPS_PER_SAMPLE_EXTRA) + \
@@ -669,7 +695,8 @@ def main():
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded chunk grid; seeds 0-9 cycle per step)",
         "config": {**config_dict(n, "fast (FMA), persistent grid + device work queue + decoupled look-back, "
                                     "then the per-vertex colour/normal pass"),
-                   "mean_verts_per_step": mean_v, "mean_inds_per_step": mean_i},
+                   "mean_verts_per_step": mean_v, "mean_inds_per_step": mean_i,
+                   "chunks_decided_by_depth_bias": decided},
         "mvoxels_per_s": value * 12 ** 3 / 1e6,
         "msamples_per_s": value * 13 ** 3 / 1e6,
         "gpu_launches": args.steps * (2 if params[0].outputs & (abi.UWW_OUT_COLOR | abi.UWW_OUT_NORMALS) else 1),

@@ -388,3 +388,33 @@ def test_dense_meshes_bit_exact(ctx_factory, oracle):
     assert tris.min() > 3000, tris.min()
     got = ctx_factory(p).build_chunks_device(d, *caps(ref))
     assert_batches_equal(got, ref)
+
+
+@pytest.mark.parametrize("bias", ["terraced", "linear"])
+def test_depth_bias_bound_decides_far_chunks(ctx_factory, oracle, bias):
+    """Chunks far above or below the surface are decided by the depth bias
+    and the fBm bound without their noise: a tall column of chunks crossing
+    the cut-off on both sides, bit-exact against the oracle (records, cases,
+    mesh), and the samples output (which disables the shortcut) unchanged."""
+    if bias == "terraced":
+        p = abi.reference_params()
+        p.outputs = ALL
+        zs = np.arange(-12, 13)
+    else:
+        p = workloads.fbm_params(7, 4, 0.04, -0.03, 128.0, 0.0, ALL)
+        zs = np.arange(0, 16)
+    g = np.arange(2)
+    pos = np.stack(np.meshgrid(g, g, zs, indexing="ij"), -1).reshape(-1, 3)
+    d = make_descs(pos, 12)
+    ref = oracle.build_chunks(p, d)
+    flags = ref.records["flags"]
+    assert (flags & abi.UWW_CHUNK_EARLY_BLANK).any() and (flags & abi.UWW_CHUNK_HAS_MESH).any()
+    got = ctx_factory(p).build_chunks_device(d, *caps(ref))
+    assert_batches_equal(got, ref)
+    assert (got.cases.reshape(len(d), -1) == 255).all(axis=1).any()  # solid chunks
+    q = p.copy()
+    q.outputs = ALL | abi.UWW_OUT_SAMPLES
+    with_samples = ctx_factory(q).build_chunks_device(d, *caps(ref))
+    assert_batches_equal(with_samples, ref)
+    want = np.concatenate([oracle.sample_grid(q, d[i]) for i in range(len(d))])
+    np.testing.assert_array_equal(with_samples.samples, want)

@@ -77,6 +77,8 @@ struct Offsets {
     uint32_t pad;
 };
 
+constexpr int kMaxPending = 64;
+
 struct SmemTables {
     float4 gp[256];               // gradient vector of P[i] (fast build: the last hash lookup)
     int8_t tri[256][16];
@@ -96,6 +98,8 @@ struct SmemTables {
     uint32_t errflags;            // UWW_ERRFLAG_* raised by this CTA
     uint32_t last;                // this CTA is the last of the launch to finish
     uint32_t n;                   // chunks in this launch (min of the device count and BuildArgs::n)
+    uint32_t npend;               // tickets the control warp decided from the depth bias, records pending
+    uint32_t pend[kMaxPending];   // their tickets | kind << 30 (1 blank, 2 solid)
 };
 
 __device__ __forceinline__ int boundary_flags(int x, int y, int z, int N)
@@ -346,8 +350,12 @@ __device__ void chunk_front(const DevParams& p, const BuildArgs& a, SmemTables& 
     const int ox = d.pos[0] * p.chunk_size, oy = d.pos[1] * p.chunk_size, oz = d.pos[2] * p.chunk_size;
 
     // ---- density grid (build_iso) + early blank and solid votes ----
-    int inside = 0, outside = 0;
-    if (!bad) {
+    // A chunk whose depth bias keeps every sample above (below) the iso level
+    // by more than the fBm can reach is blank (solid) without its noise --
+    // unless its samples are read or written.
+    const int decided = (!bad && !a.samples_in && !a.samples_out) ? bias_decides(p, N, oz) : 0;
+    int inside = decided == 2, outside = decided == 1;
+    if (!bad && !decided) {
         const float s = __fdiv_rn((float)p.chunk_size, (float)N);  // SIZE_SCALE
         const int S2 = S * S, S3 = S2 * S;
         if (a.samples_in) {
@@ -654,6 +662,73 @@ __device__ __forceinline__ void take_ticket(const BuildArgs& a, uint32_t n, Tick
     __syncwarp();
 }
 
+// The record of a chunk the depth bias decided (no cells crossed): empty,
+// early blank when every sample is above the iso level; by lane 0.
+__device__ __forceinline__ void decided_record(const BuildArgs& a, SmemTables& T, uint32_t ticket, int kind,
+                                               unsigned long long ex)
+{
+    ChunkInfo ci;
+    ci.ticket = ticket;
+    ci.ox = ci.oy = ci.oz = 0;
+    ci.N = 0;
+    ci.flags = kind == 1 ? UWW_CHUNK_EARLY_BLANK : 0u;
+    ci.classified = 0;
+    ci.pad = 0;
+    ci.total = 0ull;
+    Offsets off;
+    chunk_record(a, T, ci, ex, off, true);
+}
+
+// Control warp: take tickets until one needs the compute warps.  A chunk the
+// depth bias decides (when neither its samples nor its cases are wanted) is
+// settled here: its empty aggregate is published at once, so no successor
+// waits on it, and its record -- which needs its prefix -- is written when the
+// control warp has no other work (kMaxPending at a time; beyond that at once).
+__device__ void take_work_ticket(const DevParams& p, const BuildArgs& a, SmemTables& T, Ticket& tk, bool decide)
+{
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        take_ticket(a, T.n, tk);
+        const uint32_t t = tk.ticket;
+        if (!decide || t >= T.n) return;
+        const uww_chunk_desc d = tk.desc;
+        if (d.cells < 1 || d.cells > a.max_cells || d.cells > UWW_MAX_CELLS) return;
+        const int kind = bias_decides(p, (int)d.cells, d.pos[2] * p.chunk_size);
+        if (kind == 0) return;
+        if (t == 0) {
+            if (lane == 0) {
+                lookback_publish(a, 0u, 0ull);  // ticket 0: its inclusive prefix
+                decided_record(a, T, 0u, kind, 0ull);
+            }
+        } else if (T.npend < kMaxPending) {
+            if (lane == 0) {
+                lookback_publish(a, t, 0ull);
+                T.pend[T.npend] = t | ((uint32_t)kind << 30);
+                T.npend = T.npend + 1;
+            }
+        } else {
+            if (lane == 0) lookback_publish(a, t, 0ull);
+            __syncwarp();
+            const unsigned long long ex = lookback_warp(a, t, 0ull, &T.errflags);
+            if (lane == 0) decided_record(a, T, t, kind, ex);
+        }
+        __syncwarp();
+    }
+}
+
+// Control warp, after its last ticket: the pending records, in ticket order.
+__device__ void settle_pending(const BuildArgs& a, SmemTables& T)
+{
+    const int lane = threadIdx.x & 31;
+    for (uint32_t k = 0; k < T.npend; ++k) {
+        const uint32_t t = T.pend[k] & 0x3fffffffu;
+        const int kind = (int)(T.pend[k] >> 30);
+        const unsigned long long ex = lookback_warp(a, t, 0ull, &T.errflags);
+        if (lane == 0) decided_record(a, T, t, kind, ex);
+        __syncwarp();
+    }
+}
+
 // MAXT/MINB: the launch bounds of an instantiation.  Chunks of up to 16 cells
 // per edge run with <= 224 threads (192 compute + the control warp) and at
 // least 4 CTAs per SM (<= 72
@@ -701,6 +776,7 @@ __global__ void __launch_bounds__(MAXT, MINB) build_kernel(const DevParams p, co
         T.errflags = 0;
         T.overflow = 0;
         T.n = a.n_dev ? min(*a.n_dev, a.n) : a.n;
+        T.npend = 0;
     }
     __syncthreads();
 
@@ -720,7 +796,8 @@ __global__ void __launch_bounds__(MAXT, MINB) build_kernel(const DevParams p, co
 
     if (tid >= ncomp) {
         // ---- control warp ----
-        take_ticket(a, T.n, T.tk[0]);
+        const bool decide = !a.samples_in && !a.samples_out && !((p.outputs & UWW_OUT_CASES) && a.cases);
+        take_work_ticket(p, a, T, T.tk[0], decide);
         for (int i = 0;; ++i) {
             bar_sync(kBarTicket, nthr);  // ticket i staged; chunk i-1's counts visible
             const bool valid = T.tk[i & 1].ticket < T.n;
@@ -739,8 +816,9 @@ __global__ void __launch_bounds__(MAXT, MINB) build_kernel(const DevParams p, co
             // that follow it in the queue do not wait on a late aggregate
             if (!valid) break;
             if (i > 0) bar_sync(kBarEmitDone, nthr);
-            take_ticket(a, T.n, T.tk[(i + 1) & 1]);
+            take_work_ticket(p, a, T, T.tk[(i + 1) & 1], decide);
         }
+        settle_pending(a, T);
     } else {
         // ---- compute warps ----
         for (int i = 0;; ++i) {

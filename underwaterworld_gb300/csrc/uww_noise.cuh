@@ -120,6 +120,48 @@ __device__ __forceinline__ float z_bias(const DevParams& p, int z, float s, int 
     return 0.f;
 }
 
+// A bound on |fBm|: each octave's Perlin value is the trilinear blend, with
+// weights from the fade curve, of g . d over the cube's corners, where every
+// gradient g has two components of +-1 and one 0 and d is the offset from the
+// corner.  So |g . d| <= |dx| + |dy| + |dz|, and along each axis the blend of
+// |d| is (1 - f(u)) u + f(u) (1 - u) <= 1/2 (at u = 1/2): |value| <= 3/2
+// before the output scale.  The fBm sums the octaves with weights
+// amp_k * norm.
+__device__ __forceinline__ float fbm_bound(const DevParams& p)
+{
+    float sa = 0.f;
+    for (int k = 0; k < p.octaves; ++k) sa += fabsf(p.amp[k]);
+    return 1.5f * fabsf(fbm_norm(p)) * sa;
+}
+
+// Whether the depth bias alone decides every sample of a chunk with N cells
+// per edge at z offset oz: 1 when every sample is above the iso level (an
+// early blank chunk), 2 when every sample is below it (every case 255), 0
+// otherwise.  The margin covers f32 rounding and, for the terraced bias, a
+// step of the staircase (the parity and fast builds may round the depth to
+// either side of a step).
+__device__ __forceinline__ int bias_decides(const DevParams& p, int N, int oz)
+{
+    const float s = __fdiv_rn((float)p.chunk_size, (float)N);
+    float lo = 3.0e38f, hi = -3.0e38f;
+    bool ok = true;
+    // the linear bias is monotonic in z: its ends suffice
+    const int step = p.bias_mode == UWW_BIAS_TERRACED ? 1 : N;
+    for (int z = 0; z <= N; z += step) {
+        const float b = z_bias(p, z, s, oz);
+        ok = ok && fabsf(b) < 1.0e30f;  // false for NaN too
+        lo = fminf(lo, b);
+        hi = fmaxf(hi, b);
+    }
+    const float B = fbm_bound(p), iso = p.iso_level;
+    if (!ok || !(B < 1.0e30f) || !(fabsf(iso) < 1.0e30f)) return 0;
+    float m = 1.0e-3f * (1.f + B + fmaxf(fabsf(lo), fabsf(hi)));
+    if (p.bias_mode == UWW_BIAS_TERRACED) m += fabsf(p.bias_c);
+    if (lo - B - m > iso) return 1;
+    if (hi + B + m < iso) return 2;
+    return 0;
+}
+
 // noise coordinate of a column: (i s + o + offset) f
 __device__ __forceinline__ float column_coord(float i, float s, int o, float off, float f)
 {
