@@ -142,22 +142,45 @@ __device__ __forceinline__ float tri_hit(V3 a, V3 b, V3 c, V3 n, V3 o, V3 d, flo
 
 constexpr int kQueryWarps = 4;
 constexpr int kMaxRays = 32;
+constexpr int kTriBuf = 160;  // triangles staged per warp: 32 cells x at most 5
 
 // One warp per query point: the chunks around it (boid.rs:176-207), in each
-// the cells within `range` of the point (chunk.rs:315-342), every triangle of
-// those cells against every ray; the nearest hit per ray.
+// the cells within `range` of the point (chunk.rs:315-342).  The warp stages
+// the triangles of 32 cells at a time in shared memory (Tri::new's vertices
+// and normal, one lane per cell, placed by a warp prefix sum), then tests
+// every (triangle, ray) pair with all 32 lanes; the nearest hit per ray is an
+// atomic minimum on the float's bits.  The minimum does not depend on the
+// order, so the result is the oracle's exactly.
 __global__ void __launch_bounds__(kQueryWarps * 32) ray_query_kernel(const uww_ray_scene sc, int chunk_size,
                                                                      const float* __restrict__ origins, uint32_t nq,
                                                                      const float* __restrict__ dirs, uint32_t nrays,
                                                                      int range, float* __restrict__ out)
 {
     __shared__ int best[kQueryWarps][kMaxRays];  // bit patterns of non-negative floats order like ints
+    __shared__ float rdir[kQueryWarps][kMaxRays * 3];
+    __shared__ float4 tri[kQueryWarps][kTriBuf * 3];  // (a, n.x), (b, n.y), (c, n.z)
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const float cs = (float)chunk_size, rf = (float)range;
+    const int R = (int)nrays;
     for (uint32_t q = blockIdx.x * kQueryWarps + warp; q < nq; q += gridDim.x * kQueryWarps) {
-        for (uint32_t k = lane; k < nrays; k += 32) best[warp][k] = 0x7f800000;  // +inf
+        for (int k = lane; k < R; k += 32) best[warp][k] = 0x7f800000;  // +inf
+        for (int k = lane; k < 3 * R; k += 32) rdir[warp][k] = dirs[3 * (size_t)q * R + k];
         __syncwarp();
         const V3 o = {origins[3 * (size_t)q], origins[3 * (size_t)q + 1], origins[3 * (size_t)q + 2]};
+        int nbuf = 0;  // warp-uniform
+        // every (staged triangle, ray) pair, all lanes
+        auto flush = [&]() {
+            const int pairs = nbuf * R;
+            for (int pi = lane; pi < pairs; pi += 32) {
+                const int t = pi / R, k = pi - t * R;
+                const float4 A = tri[warp][3 * t], B = tri[warp][3 * t + 1], Cc = tri[warp][3 * t + 2];
+                const V3 dir = {rdir[warp][3 * k], rdir[warp][3 * k + 1], rdir[warp][3 * k + 2]};
+                const float th = tri_hit({A.x, A.y, A.z}, {B.x, B.y, B.z}, {Cc.x, Cc.y, Cc.z}, {A.w, B.w, Cc.w}, o, dir, rf);
+                if (th >= 0.f) atomicMin(&best[warp][k], __float_as_int(th));
+            }
+            __syncwarp();
+            nbuf = 0;
+        };
         // chunk window, world units (boid.rs:176-182)
         const int sx = (int)floorf(__fdiv_rn(__fsub_rn(o.x, rf), cs)), ex = (int)floorf(__fdiv_rn(__fadd_rn(o.x, rf), cs));
         const int sy = (int)floorf(__fdiv_rn(__fsub_rn(o.y, rf), cs)), ey = (int)floorf(__fdiv_rn(__fadd_rn(o.y, rf), cs));
@@ -183,15 +206,31 @@ __global__ void __launch_bounds__(kQueryWarps * 32) ray_query_kernel(const uww_r
                     if (x0 > x1 || y0 > y1 || z0 > z1) continue;
                     const int wy = y1 - y0 + 1, wz = z1 - z0 + 1;
                     const int cells = (x1 - x0 + 1) * wy * wz;
-                    for (int w = lane; w < cells; w += 32) {
-                        const int x = x0 + w / (wy * wz), y = y0 + (w / wz) % wy, z = z0 + w % wz;
-                        const uint32_t cell = d.cell_offset + (uint32_t)((x * N + y) * N + z);
-                        const int nt = __ldg(&UWW_CASE_NTRI[sc.cases[cell]]);
-                        if (!nt) continue;
-                        const uint32_t fl = sc.cell_first[cell];
-                        // a scene assembled from different builds is skipped, not read out of range
-                        if ((unsigned long long)fl + 3ull * nt > r.num_inds) continue;
-                        const uint32_t f = r.ind_offset + fl;
+                    for (int w0 = 0; w0 < cells; w0 += 32) {
+                        const int w = w0 + lane;
+                        int nt = 0;
+                        uint32_t f = 0;
+                        if (w < cells) {
+                            const int x = x0 + w / (wy * wz), y = y0 + (w / wz) % wy, z = z0 + w % wz;
+                            const uint32_t cell = d.cell_offset + (uint32_t)((x * N + y) * N + z);
+                            nt = __ldg(&UWW_CASE_NTRI[sc.cases[cell]]);
+                            if (nt) {
+                                const uint32_t fl = sc.cell_first[cell];
+                                // a scene assembled from different builds is skipped, not read out of range
+                                if ((unsigned long long)fl + 3ull * nt > r.num_inds) nt = 0;
+                                f = r.ind_offset + fl;
+                            }
+                        }
+                        int incl = nt;
+#pragma unroll
+                        for (int sh = 1; sh < 32; sh <<= 1) {
+                            const int v = __shfl_up_sync(0xffffffffu, incl, sh);
+                            if (lane >= sh) incl += v;
+                        }
+                        const int total = __shfl_sync(0xffffffffu, incl, 31);
+                        if (total == 0) continue;
+                        if (nbuf + total > kTriBuf) flush();
+                        const int base = nbuf + incl - nt;
                         for (int j = 0; j < nt; ++j) {
                             V3 vv[3];
                             bool ok = true;
@@ -202,24 +241,27 @@ __global__ void __launch_bounds__(kQueryWarps * 32) ray_query_kernel(const uww_r
                                 const uww_vert_color vc = sc.verts[r.vert_offset + min(id, r.num_verts - 1u)];
                                 vv[m] = {vc.pos[0], vc.pos[1], vc.pos[2]};
                             }
-                            if (!ok) continue;
-                            // Tri::new (util.rs:12-21): normal = safe_normalize((b - a) x (c - a))
-                            V3 nn = vcross(vsub(vv[1], vv[0]), vsub(vv[2], vv[0]));
-                            const float mag = __fsqrt_rn(vdot(nn, nn));
-                            if (mag != 0.f) nn = {__fdiv_rn(nn.x, mag), __fdiv_rn(nn.y, mag), __fdiv_rn(nn.z, mag)};
-                            for (uint32_t k = 0; k < nrays; ++k) {
-                                const size_t di = 3 * ((size_t)q * nrays + k);
-                                const V3 dir = {dirs[di], dirs[di + 1], dirs[di + 2]};
-                                const float t = tri_hit(vv[0], vv[1], vv[2], nn, o, dir, rf);
-                                if (t >= 0.f) atomicMin(&best[warp][k], __float_as_int(t));
+                            // Tri::new (util.rs:12-21): normal = safe_normalize((b - a) x (c - a));
+                            // a triangle with an index out of range gets a zero normal, which no ray hits
+                            V3 nn = {0.f, 0.f, 0.f};
+                            if (ok) {
+                                nn = vcross(vsub(vv[1], vv[0]), vsub(vv[2], vv[0]));
+                                const float mag = __fsqrt_rn(vdot(nn, nn));
+                                if (mag != 0.f) nn = {__fdiv_rn(nn.x, mag), __fdiv_rn(nn.y, mag), __fdiv_rn(nn.z, mag)};
                             }
+                            float4* T = &tri[warp][3 * (base + j)];
+                            T[0] = make_float4(vv[0].x, vv[0].y, vv[0].z, nn.x);
+                            T[1] = make_float4(vv[1].x, vv[1].y, vv[1].z, nn.y);
+                            T[2] = make_float4(vv[2].x, vv[2].y, vv[2].z, nn.z);
                         }
+                        nbuf += total;
+                        __syncwarp();
                     }
                 }
-        __syncwarp();
-        for (uint32_t k = lane; k < nrays; k += 32) {
-            const int b = best[warp][k];
-            out[(size_t)q * nrays + k] = b == 0x7f800000 ? -1.f : __int_as_float(b);
+        if (nbuf) flush();
+        for (int k = lane; k < R; k += 32) {
+            const int bb = best[warp][k];
+            out[(size_t)q * R + k] = bb == 0x7f800000 ? -1.f : __int_as_float(bb);
         }
         __syncwarp();
     }
