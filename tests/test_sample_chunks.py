@@ -72,3 +72,24 @@ def test_bad_descriptors_are_flagged_and_skipped(ctx_factory):
     abi.check(L.uww_sample_chunks(ctx.h, C.c_void_p(d_desc2.ptr), 1, 12, C.c_void_p(buf.ptr), 13 ** 3))
     abi.check(L.uww_sample_status(ctx.h, C.byref(flags)))
     assert flags.value & abi.UWW_ERRFLAG_RANGE
+
+
+def test_global_scratch_classification_matches_sampled_build(ctx_factory):
+    """Chunks above the shared-memory cut keep their samples in global scratch
+    and are classified from per-column inside masks; the same chunks built
+    from their sampled densities (classified from the samples) give the same
+    mesh, cases and records bit for bit."""
+    from helpers import assert_batches_equal
+    p = workloads.fbm_params(4, 6, 0.03, 0.02, 0.0, 0.0,
+                             abi.UWW_OUT_COLOR | abi.UWW_OUT_NORMALS | abi.UWW_OUT_CASES)
+    p.math_mode = abi.UWW_MATH_FAST
+    cells = np.array([24, 48, 12, 40, 64, 5, 24, 48, 33, 63])
+    pos = np.stack([np.arange(len(cells)) - 5, np.zeros(len(cells)), np.arange(len(cells)) % 2 - 1], 1)
+    d = make_descs(pos, cells)
+    ctx = ctx_factory(p)
+    samples = ctx.sample_chunks(d)
+    a = ctx.build_chunks_device(d, 1 << 21, 1 << 23)
+    b = ctx.build_chunks_device(d, 1 << 21, 1 << 23, samples_in=samples)
+    assert a.status == abi.UWW_OK and b.status == abi.UWW_OK
+    assert (a.records["flags"] & abi.UWW_CHUNK_HAS_MESH).sum() >= 6
+    assert_batches_equal(a, b)

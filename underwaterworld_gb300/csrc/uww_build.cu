@@ -102,6 +102,16 @@ struct SmemTables {
     uint32_t pend[kMaxPending];   // their tickets | kind << 30 (1 blank, 2 solid)
 };
 
+// A cell's case from its four corner columns' inside masks (bit z: sample
+// below the iso level), corner order of chunk.rs:144-153.
+__device__ __forceinline__ int mask_case(unsigned long long m00, unsigned long long m10, unsigned long long m01,
+                                         unsigned long long m11, int z)
+{
+    const unsigned long long z0 = m00 >> z, z1 = m10 >> z, z2 = m01 >> z, z3 = m11 >> z;
+    return (int)((z0 & 1) | ((z1 & 1) << 1) | (((z1 >> 1) & 1) << 2) | (((z0 >> 1) & 1) << 3) | ((z2 & 1) << 4) |
+                 ((z3 & 1) << 5) | (((z3 >> 1) & 1) << 6) | (((z2 >> 1) & 1) << 7));
+}
+
 __device__ __forceinline__ int boundary_flags(int x, int y, int z, int N)
 {
     return (x == 0) | ((y == 0) << 1) | ((z == 0) << 2) | ((x == N - 1) << 3) | ((y == N - 1) << 4) |
@@ -348,6 +358,13 @@ __device__ void chunk_front(const DevParams& p, const BuildArgs& a, SmemTables& 
     float* rho = W.rho;
     uint8_t* cases = W.cases;
     const int ox = d.pos[0] * p.chunk_size, oy = d.pos[1] * p.chunk_size, oz = d.pos[2] * p.chunk_size;
+    // a chunk in global scratch leaves the shared workspace `buf` free: its
+    // columns' inside bits go there (fast build, up to 64 samples a column)
+    unsigned long long* masks =
+        (std::is_same<O, FastOps>::value && (uint32_t)N > a.smem_cells && S <= 64 && !a.samples_in &&
+         (size_t)S * S * sizeof(unsigned long long) <= a.smem_buf_bytes)
+            ? reinterpret_cast<unsigned long long*>(dyn_smem + (size_t)buf * a.smem_buf_bytes)
+            : nullptr;
 
     // ---- density grid (build_iso) + early blank and solid votes ----
     // A chunk whose depth bias keeps every sample above (below) the iso level
@@ -369,8 +386,9 @@ __device__ void chunk_front(const DevParams& p, const BuildArgs& a, SmemTables& 
         } else if constexpr (std::is_same<O, FastOps>::value) {
             const ZTable zt = ztable_at(dyn_smem + a.ztable_offset, S, p.octaves);
             // a chunk in a global scratch slot accumulates its columns in local memory
-            const int io = (uint32_t)N <= a.smem_cells ? sample_columns_fast<false>(p, T.perm, T.gp, zt, rho, N, ox, oy, oz, ncomp)
-                                                       : sample_columns_fast<true>(p, T.perm, T.gp, zt, rho, N, ox, oy, oz, ncomp);
+            const int io = (uint32_t)N <= a.smem_cells
+                               ? sample_columns_fast<false>(p, T.perm, T.gp, zt, rho, N, ox, oy, oz, ncomp)
+                               : sample_columns_fast<true>(p, T.perm, T.gp, zt, rho, N, ox, oy, oz, ncomp, masks);
             inside = io & 1;
             outside = io >> 1;
         } else {
@@ -415,15 +433,28 @@ __device__ void chunk_front(const DevParams& p, const BuildArgs& a, SmemTables& 
             // the z+1 face of a cell is the z face of the next cell in the
             // run: carry its 4 inside bits (corners 3,2,7,6 -> 0,1,4,5)
             int lo = -1;
+            unsigned long long m00 = 0, m10 = 0, m01 = 0, m11 = 0;
+            int mcol = -1;
             for (int c = c0; c < c1; ++c) {
-                const int b = (x * S + y) * S + z;
-                if (lo < 0)
-                    lo = (rho[b] < iso) | ((rho[b + SS] < iso) << 1) | ((rho[b + S] < iso) << 4) |
-                         ((rho[b + SS + S] < iso) << 5);
-                const int c3 = rho[b + 1] < iso, c2 = rho[b + SS + 1] < iso;
-                const int c7 = rho[b + S + 1] < iso, c6 = rho[b + SS + S + 1] < iso;
-                const int cs = lo | (c2 << 2) | (c3 << 3) | (c6 << 6) | (c7 << 7);
-                lo = (z + 1 < N) ? (c3 | (c2 << 1) | (c7 << 4) | (c6 << 5)) : -1;
+                int cs;
+                if (masks) {
+                    // corner bits from the columns' masks (corner order of chunk.rs:144-153)
+                    const int col = x * S + y;
+                    if (col != mcol) {
+                        m00 = masks[col]; m10 = masks[col + S]; m01 = masks[col + 1]; m11 = masks[col + S + 1];
+                        mcol = col;
+                    }
+                    cs = mask_case(m00, m10, m01, m11, z);
+                } else {
+                    const int b = (x * S + y) * S + z;
+                    if (lo < 0)
+                        lo = (rho[b] < iso) | ((rho[b + SS] < iso) << 1) | ((rho[b + S] < iso) << 4) |
+                             ((rho[b + SS + S] < iso) << 5);
+                    const int c3 = rho[b + 1] < iso, c2 = rho[b + SS + 1] < iso;
+                    const int c7 = rho[b + S + 1] < iso, c6 = rho[b + SS + S + 1] < iso;
+                    cs = lo | (c2 << 2) | (c3 << 3) | (c6 << 6) | (c7 << 7);
+                    lo = (z + 1 < N) ? (c3 | (c2 << 1) | (c7 << 4) | (c6 << 5)) : -1;
+                }
                 cases[c] = (uint8_t)cs;
                 const int nt = T.ntri[cs];
                 if (nt) {
@@ -441,11 +472,27 @@ __device__ void chunk_front(const DevParams& p, const BuildArgs& a, SmemTables& 
             // second pass over the same runs: each cell's first vertex id and
             // the active-cell list with its first index position
             int x = c0 / (N * N), y = (c0 / N) % N, z = c0 % N;
+            unsigned long long m00 = 0, m10 = 0, m01 = 0, m11 = 0;
+            int mcol = -1;
             for (int c = c0; c < c1; ++c) {
-                const int cs = cases[c];
-                W.set_vbase(c, (uint32_t)(run & kField22));
+                int cs;
+                if (masks) {
+                    // the case again from the masks (no read of the global cases); only
+                    // active cells need a first vertex id: every owner cell of a crossed
+                    // edge is active
+                    const int col = x * S + y;
+                    if (col != mcol) {
+                        m00 = masks[col]; m10 = masks[col + S]; m01 = masks[col + 1]; m11 = masks[col + S + 1];
+                        mcol = col;
+                    }
+                    cs = mask_case(m00, m10, m01, m11, z);
+                } else {
+                    cs = cases[c];
+                    W.set_vbase(c, (uint32_t)(run & kField22));
+                }
                 const int nt = T.ntri[cs];
                 if (nt) {
+                    if (masks) W.set_vbase(c, (uint32_t)(run & kField22));
                     const uint32_t ar = (uint32_t)(run >> kActShift);
                     W.set_active(ar, c);
                     W.set_ibase(ar, (uint32_t)((run >> kIndShift) & kField22));

@@ -253,11 +253,14 @@ __device__ __forceinline__ ZTable ztable_at(uint8_t* base, int S, int octaves)
 // COLBUF: accumulate each column in a per-thread buffer (local memory, L1)
 // and write it to rho once, for rho in global memory where an accumulate per
 // sample and octave would be an L2 round trip each.
+// masks (optional, COLBUF, at most 64 samples per column): per column the
+// bits z with sample < iso level -- the columns' corner bits of every cell
+// case, so the classification of a chunk in global scratch reads no samples.
 template <bool COLBUF = false>
 __device__ __forceinline__ int sample_columns_fast(const DevParams& p, const uint8_t* __restrict__ P,
                                                    const float4* __restrict__ gp, const ZTable Z,
                                                    float* __restrict__ rho, int N, int ox, int oy, int oz,
-                                                   int ncomp)
+                                                   int ncomp, unsigned long long* masks = nullptr)
 {
     const int S = N + 1, SS = S * S, K = p.octaves;
     const float s = __fdiv_rn((float)p.chunk_size, (float)N);
@@ -332,7 +335,12 @@ __device__ __forceinline__ int sample_columns_fast(const DevParams& p, const uin
         }
         if (COLBUF) {
             float* dst = rho + col * S;
-            for (int z = 0; z < S; ++z) dst[z] = colbuf[z];
+            unsigned long long m = 0ull;
+            for (int z = 0; z < S; ++z) {
+                dst[z] = colbuf[z];
+                m |= (unsigned long long)(colbuf[z] < iso) << (z & 63);
+            }
+            if (masks) masks[col] = m;
         }
     }
     return inside | (outside << 1);
