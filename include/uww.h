@@ -119,7 +119,11 @@ typedef struct uww_vert_color {
 
 /* Output buffers of a build.  Device pointers for uww_build_chunks*, host
  * pointers for uww_build_chunks_host.  verts/inds/records are required; the
- * others may be NULL (then that output is skipped even if requested). */
+ * others may be NULL (then that output is skipped even if requested).  Device
+ * buffers must be aligned as the kernels store to them -- verts and totals to
+ * 8 bytes, normals, inds, records and samples to 4 -- and device descriptors
+ * to 4 bytes; anything else is refused with UWW_ERR_INVALID_ARG before a
+ * launch.  Host buffers may have any alignment. */
 typedef struct uww_mesh_out {
     uww_vert_color*   verts;      /* vert_capacity entries                              */
     float*            normals;    /* 3 * vert_capacity floats, or NULL                  */
@@ -209,6 +213,10 @@ int uww_build_chunk_plain(uww_ctx* ctx, const uww_chunk_desc* d_chunk, uint32_t 
 
 /* Host-buffer form of uww_build_chunks: copies the descriptors in, builds,
  * copies records, vertices, normals, indices and cases out, synchronises.
+ * With page-locked output buffers (uww_host_alloc, or any memory the device
+ * can address) at 4-byte alignment, the build streams each finished chunk to
+ * them while later chunks build, and the host synchronises once; other host
+ * buffers are filled by sized copies after the build.
  * Returns UWW_ERR_CAPACITY (records still valid) when a capacity is too small. */
 int uww_build_chunks_host(uww_ctx* ctx, const uww_chunk_desc* h_chunks, uint32_t n,
                           const uww_mesh_out* h_out);
