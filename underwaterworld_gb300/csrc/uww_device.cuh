@@ -311,6 +311,17 @@ __device__ __forceinline__ void density_grad_fast(const DevParams& p, const uint
 template <class O>
 __device__ __forceinline__ void safe_normalize(float g[3])
 {
+    if constexpr (std::is_same<O, FastOps>::value) {
+        // fast build: one reciprocal square root instead of a square root and three divisions
+        const float d = fmaf(g[0], g[0], fmaf(g[1], g[1], g[2] * g[2]));
+        if (d != 0.f) {
+            const float r = rsqrtf(d);
+            g[0] *= r;
+            g[1] *= r;
+            g[2] *= r;
+        }
+        return;
+    }
     const float mag = __fsqrt_rn(O::add(O::add(O::mul(g[0], g[0]), O::mul(g[1], g[1])), O::mul(g[2], g[2])));
     if (mag != 0.f) {
         g[0] = __fdiv_rn(g[0], mag);
@@ -323,15 +334,16 @@ __device__ __forceinline__ void safe_normalize(float g[3])
 template <class O>
 __device__ __forceinline__ void vertex_color(const DevParams& p, float world_z, int corner_b, float out[3])
 {
-    const float ratio = __fdiv_rn(world_z, (float)p.chunk_size);
-    const float mix = __fdiv_rn(O::sub(ratio, p.color_min_z), O::sub(p.color_max_z, p.color_min_z));
-    const float vi = __fdiv_rn((float)(corner_b % 3), 9.0f);
+    // divisions: IEEE in the parity build, the approximate quotient in the fast build
+    const float ratio = O::div(world_z, (float)p.chunk_size);
+    const float mix = O::div(O::sub(ratio, p.color_min_z), O::sub(p.color_max_z, p.color_min_z));
+    const float vi = O::div((float)(corner_b % 3), 9.0f);
     const float hue0 = O::add(-150.0f, O::mul(210.0f, mix));  // MIN_HUE + (MAX_HUE - MIN_HUE) * mix
     const float value = O::add(0.4f, vi);                      // BASE_VALUE + value_intensity
     const float r0 = fmodf(hue0, 360.0f);
     const float hue = r0 < 0.f ? O::add(r0, 360.0f) : r0;      // rem_euclid
     const float c = O::mul(value, 0.6f);                       // SATURATION
-    const float h = __fdiv_rn(hue, 60.0f);
+    const float h = O::div(hue, 60.0f);
     const float x = O::mul(c, O::sub(1.0f, fabsf(O::sub(fmodf(h, 2.0f), 1.0f))));
     const float m = O::sub(value, c);
     float r, gg, b;
@@ -345,7 +357,7 @@ __device__ __forceinline__ void vertex_color(const DevParams& p, float world_z, 
 #pragma unroll
     for (int i = 0; i < 3; ++i)
     {
-        const float base = __fdiv_rn(O::add(__fdiv_rn(rgb[i], 255.0f), 0.055f), 1.055f);
+        const float base = O::div(O::add(O::div(rgb[i], 255.0f), 0.055f), 1.055f);
         // parity build: powf; fast build: the hardware exp2/log2 pair (base > 0)
         out[i] = std::is_same<O, FastOps>::value ? __powf(base, 2.4f) : powf(base, 2.4f);
     }
