@@ -233,7 +233,7 @@ struct AdjointArgs {
     const float* pos_grad;           // [vert][3]
     float* sample_grad;              // optional, zeroed by the host
     unsigned long long sample_capacity;
-    float* part;                     // [n][KMAX + 5] per-chunk partials
+    float* part;                     // [grid][KMAX + 5] per-CTA partials
     unsigned int* counter;           // zero at launch; the last CTA resets it
     float* theta_grad;               // [octaves + 5]
     uint32_t n;
@@ -262,10 +262,14 @@ __device__ __forceinline__ void block_sum(float (&v)[NV], float (*red)[NV])
         }
 }
 
-// One CTA per chunk: every vertex of the chunk recomputes the density and its
-// theta derivatives at its two corners, forms dL/drho_A, dL/drho_B and
-// dL/diso, and accumulates dL/dtheta; the last CTA to finish reduces the
-// per-chunk partials in chunk order.
+// Vertex-parallel over the batch: thread t of CTA b takes vertices
+// b T + t, b T + t + G T, ... (T threads, G CTAs: a fixed assignment, so the
+// sums below are deterministic), finds each vertex's chunk by binary search
+// over the records' vertex offsets, recomputes the density and its theta
+// derivatives at the edge's two corners, forms dL/drho_A, dL/drho_B and
+// dL/diso, and accumulates dL/dtheta.  Per-CTA partials; the last CTA to
+// finish reduces them in CTA order.  (One CTA per chunk left the densest
+// chunks' CTAs as the tail of the launch.)
 template <class O, int KMAX>
 __global__ void __launch_bounds__(kBwdThreads) backward_kernel(const DevParams p, const AdjointArgs a)
 {
@@ -281,12 +285,22 @@ __global__ void __launch_bounds__(kBwdThreads) backward_kernel(const DevParams p
     for (int j = 0; j < NV; ++j) acc[j] = 0.f;
     float bad = 0.f;
 
-    const uint32_t c = blockIdx.x;
-    const uww_chunk_record r = a.records[c];
-    const uww_chunk_desc d = a.chunks[c];
-    const bool use = (r.flags & UWW_CHUNK_HAS_MESH) && !(r.flags & UWW_CHUNK_OVERFLOW) && d.cells >= 1 &&
-                     d.cells <= a.max_cells;
-    if (use) {
+    // the batch's vertices: the last chunk's inclusive prefix
+    const uww_chunk_record rl = a.records[a.n - 1];
+    const uint32_t V = rl.vert_offset + rl.num_verts;
+    for (uint32_t gid = blockIdx.x * kBwdThreads + threadIdx.x; gid < V; gid += gridDim.x * kBwdThreads) {
+        // its chunk: the last one whose first vertex is at or before it
+        uint32_t c = 0, len = a.n;
+        while (len > 1) {
+            const uint32_t h = len >> 1;
+            if (__ldg(&a.records[c + h].vert_offset) <= gid) c += h;
+            len -= h;
+        }
+        const uww_chunk_record r = a.records[c];
+        const uww_chunk_desc d = a.chunks[c];
+        const bool use = (r.flags & UWW_CHUNK_HAS_MESH) && !(r.flags & UWW_CHUNK_OVERFLOW) && d.cells >= 1 &&
+                         d.cells <= a.max_cells && gid - r.vert_offset < r.num_verts;
+        if (!use) continue;
         const int N = (int)d.cells, S = N + 1;
         const uint32_t S3 = (uint32_t)S * S * S;
         const float s = __fdiv_rn((float)p.chunk_size, (float)N);
@@ -294,8 +308,7 @@ __global__ void __launch_bounds__(kBwdThreads) backward_kernel(const DevParams p
                     oz = (float)(d.pos[2] * p.chunk_size);
         const float iso = p.iso_level;
         const bool sg = a.sample_grad && (unsigned long long)d.sample_offset + S3 <= a.sample_capacity;
-        for (uint32_t v = threadIdx.x; v < r.num_verts; v += kBwdThreads) {
-            const uint32_t gid = r.vert_offset + v;
+        {
             const uint32_t e = a.edge_ids[gid];
             const uint32_t sa = e >> 3, dir = e & 7u;
             const int xa = (int)(sa / (uint32_t)(S * S)), ya = (int)((sa / (uint32_t)S) % (uint32_t)S),
@@ -342,19 +355,19 @@ __global__ void __launch_bounds__(kBwdThreads) backward_kernel(const DevParams p
     block_sum<NV>(acc, red);
     if (threadIdx.x == 0) {
 #pragma unroll
-        for (int j = 0; j < NV; ++j) a.part[(size_t)c * NV + j] = acc[j];
+        for (int j = 0; j < NV; ++j) a.part[(size_t)blockIdx.x * NV + j] = acc[j];
         __threadfence();
         last = atomicAdd(a.counter, 1u) == gridDim.x - 1;
     }
     __syncthreads();
     if (!last) return;
     __threadfence();
-    // final reduction: thread i sums chunks i, i + 256, ... in order, then the
-    // block sum combines the threads in a fixed order
+    // final reduction: thread i sums the partials of CTAs i, i + 256, ... in
+    // order, then the block sum combines the threads in a fixed order
     float tot[NV];
 #pragma unroll
     for (int j = 0; j < NV; ++j) tot[j] = 0.f;
-    for (uint32_t k = threadIdx.x; k < a.n; k += kBwdThreads)
+    for (uint32_t k = threadIdx.x; k < gridDim.x; k += kBwdThreads)
 #pragma unroll
         for (int j = 0; j < NV; ++j) tot[j] += __ldcg(a.part + (size_t)k * NV + j);
     __syncthreads();
@@ -434,18 +447,40 @@ __global__ void height_grad(const HeightArgs h)
 }
 
 template <class O, int KMAX>
-cudaError_t launch_backward_t(const DevParams& p, const AdjointArgs& a, cudaStream_t s)
+cudaError_t launch_backward_t(const DevParams& p, const AdjointArgs& a, int grid, cudaStream_t s)
 {
-    backward_kernel<O, KMAX><<<a.n, kBwdThreads, 0, s>>>(p, a);
+    backward_kernel<O, KMAX><<<grid, kBwdThreads, 0, s>>>(p, a);
     return cudaGetLastError();
 }
 
-template <class O>
-cudaError_t launch_backward_o(const DevParams& p, const AdjointArgs& a, cudaStream_t s)
+// CTAs of the backward: every resident one (the assignment of vertices to
+// threads depends only on this number)
+template <class O, int KMAX>
+int backward_grid_t(int sms)
 {
-    if (p.octaves <= 4) return launch_backward_t<O, 4>(p, a, s);
-    if (p.octaves <= 8) return launch_backward_t<O, 8>(p, a, s);
-    return launch_backward_t<O, 16>(p, a, s);
+    int occ = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, backward_kernel<O, KMAX>, kBwdThreads, 0) != cudaSuccess ||
+        occ < 1) {
+        cudaGetLastError();
+        occ = 1;
+    }
+    return occ * sms;
+}
+
+template <class O>
+int backward_grid_o(const DevParams& p, int sms)
+{
+    if (p.octaves <= 4) return backward_grid_t<O, 4>(sms);
+    if (p.octaves <= 8) return backward_grid_t<O, 8>(sms);
+    return backward_grid_t<O, 16>(sms);
+}
+
+template <class O>
+cudaError_t launch_backward_o(const DevParams& p, const AdjointArgs& a, int grid, cudaStream_t s)
+{
+    if (p.octaves <= 4) return launch_backward_t<O, 4>(p, a, grid, s);
+    if (p.octaves <= 8) return launch_backward_t<O, 8>(p, a, grid, s);
+    return launch_backward_t<O, 16>(p, a, grid, s);
 }
 
 int kmax_for(int octaves) { return octaves <= 4 ? 4 : octaves <= 8 ? 8 : 16; }
@@ -490,7 +525,9 @@ int uww_backward(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint3
         return status_from_cuda(cudaMemsetAsync(d_theta_grad, 0, (size_t)(K + 5) * sizeof(float), s), "cudaMemsetAsync");
     if (!d_chunks || !d_records || !d_edge_ids || !d_pos_grad) return UWW_ERR_INVALID_ARG;
     const int NV = kmax_for(K) + 5;
-    int st = ensure_device_of(&ctx->d_adj_part, &ctx->adj_part_cap, (size_t)n * NV * sizeof(float));
+    const bool exact = ctx->dev.math_mode == UWW_MATH_EXACT;
+    const int grid = exact ? backward_grid_o<ExactOps>(ctx->dev, ctx->num_sms) : backward_grid_o<FastOps>(ctx->dev, ctx->num_sms);
+    int st = ensure_device_of(&ctx->d_adj_part, &ctx->adj_part_cap, (size_t)grid * NV * sizeof(float));
     if (st) return st;
     if (!ctx->d_adj_counter) {
         cudaError_t e = cudaMalloc((void**)&ctx->d_adj_counter, sizeof(unsigned int));
@@ -514,8 +551,8 @@ int uww_backward(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint3
     a.theta_grad = d_theta_grad;
     a.n = n;
     a.max_cells = max_cells;
-    const cudaError_t e = ctx->dev.math_mode == UWW_MATH_EXACT ? launch_backward_o<ExactOps>(ctx->dev, a, s)
-                                                               : launch_backward_o<FastOps>(ctx->dev, a, s);
+    const cudaError_t e = exact ? launch_backward_o<ExactOps>(ctx->dev, a, grid, s)
+                                : launch_backward_o<FastOps>(ctx->dev, a, grid, s);
     return status_from_cuda(e, "backward kernel launch");
 }
 

@@ -148,7 +148,10 @@ int plan_launch(uww_ctx* ctx, uint32_t n, uint32_t max_cells, bool queue, Launch
     // The batched form pipelines two chunks per CTA, so it holds two workspaces.
     const uint32_t slots = queue ? 2u : 1u;
     const size_t cap = ctx->smem_dyn_max;
-    uint32_t smem_cells = ctx->smem_cells > 0 ? (uint32_t)ctx->smem_cells : max_cells;
+    // by default chunks up to 16 cells work in shared memory; a batch with
+    // larger ones keeps 12 there (small workspaces, more CTAs per SM) and the
+    // rest in global scratch
+    uint32_t smem_cells = ctx->smem_cells > 0 ? (uint32_t)ctx->smem_cells : (max_cells > 16 ? 12u : max_cells);
     smem_cells = std::min(smem_cells, max_cells);
     // the fast build also keeps per-chunk z tables (sized for the largest chunk)
     const size_t zt = ctx->dev.math_mode == UWW_MATH_FAST ? ztable_bytes((int)max_cells + 1, ctx->dev.octaves) : 0;
@@ -159,8 +162,9 @@ int plan_launch(uww_ctx* ctx, uint32_t n, uint32_t max_cells, bool queue, Launch
     cfg->ztable_offset = (size_t)slots * cfg->smem_buf;
     cfg->dyn_smem = cfg->ztable_offset + zt;
     // compute threads: by default 192 for chunks of up to 12 cells (one per
-    // sample column of a 13^3 grid) and 256 above, which keeps two CTAs per SM
-    // (larger chunks loop over their columns); the batched form adds one
+    // sample column of a 13^3 grid), 256 up to 16 cells (two CTAs per SM) and
+    // 512 above (one CTA per SM: a 25^2-column chunk in global scratch is
+    // latency-bound, 1.7x faster than with 256); the batched form adds one
     // control warp
     const int compute = ctx->threads > 0 ? ctx->threads : default_compute_threads(max_cells);
     cfg->threads = compute + (queue ? 32 : 0);
@@ -294,7 +298,7 @@ int check_params(const uww_params* p) { return validate_params(p); }
 void dev_params_from(const uww_params* p, DevParams* d) { make_dev_params(p, d); }
 int status_from_cuda(cudaError_t e, const char* where) { return cuda_status(e, where); }
 long long spin_limit_cycles() { return kSpinLimitCycles; }
-int default_compute_threads(uint32_t max_cells) { return max_cells <= 12 ? 192 : 256; }
+int default_compute_threads(uint32_t max_cells) { return max_cells <= 12 ? 192 : max_cells <= 16 ? 256 : 512; }
 int ensure_device_bytes(void** ptr, size_t* cap, size_t bytes) { return ensure_device(ptr, cap, bytes); }
 int launch_batched(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint32_t max_cells,
                    const uww_mesh_out* out, uint32_t* edge_ids, const uint32_t* n_dev)
