@@ -252,6 +252,8 @@ __device__ __forceinline__ void density_grad_fast(const DevParams& p, const uint
     const float bf = p.base_freq;
     const float nx = (wx + p.offset[0]) * bf, ny = (wy + p.offset[1]) * bf, nz = (wz + p.offset[2]) * bf;
     float gx = 0.f, gy = 0.f, gz = 0.f, msum = 0.f;
+    // unrolled so that independent octaves overlap their table-lookup chains
+#pragma unroll 4
     for (int k = 0; k < p.octaves; ++k) {
         const float m = p.mult[k], am = p.amp[k];
         msum += am;
