@@ -195,6 +195,8 @@ __device__ __forceinline__ float fbm(const DevParams& p, const uint8_t* P, float
 {
     float total = 0.f, maxv = 0.f;
     float gt0 = 0.f, gt1 = 0.f, gt2 = 0.f;
+    // unrolled so that independent octaves overlap their table-lookup chains
+#pragma unroll 4
     for (int k = 0; k < p.octaves; ++k) {
         const float m = p.mult[k], am = p.amp[k];
         float gk[3];
