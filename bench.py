@@ -70,6 +70,8 @@ def parse():
     ap.add_argument("--bps", type=int, default=0, help="resident CTAs per SM (0: tuned/automatic)")
     ap.add_argument("--no-fit", action="store_true", help="skip the terrain-fitting leg")
     ap.add_argument("--fit-steps", type=int, default=200, help="Adam steps of the terrain-fitting leg")
+    ap.add_argument("--leg", default="", choices=["", "mixed_lod", "adjoint", "queries", "terrain_fit"],
+                    help="with --quick: also run this one leg (profiling runs)")
     return ap.parse_args()
 
 
@@ -646,6 +648,15 @@ def main():
                         "h2d_bytes_per_step": h2d // k, "d2h_bytes_per_step": d2h // k}
 
     extra["noise_stage"] = leg_noise_stage(ctx, stream, flush, params[0], descs, max(10, min(args.steps, 200)), 3)
+    if args.quick and args.leg:
+        if args.leg == "mixed_lod":
+            extra["mixed_lod"] = leg_mixed_lod(stream, flush, max(5, min(args.steps, 200)), 3)
+        elif args.leg == "adjoint":
+            extra["adjoint"] = leg_adjoint(stream, flush, max(5, min(args.steps, 50)), 3)
+        elif args.leg == "queries":
+            extra["queries"] = leg_queries(stream, flush, max(5, min(args.steps, 50)))
+        else:
+            extra["terrain_fit"] = leg_terrain_fit(stream, args.fit_steps)
     if not args.quick:
         extra["frame_graph"] = leg_frame_graph(ctx, params[0], descs, max(5, min(args.steps, 50)), 3)
         extra["mixed_lod"] = leg_mixed_lod(stream, flush, max(10, min(args.steps, 200)), 3)
