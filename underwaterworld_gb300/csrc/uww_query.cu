@@ -169,14 +169,22 @@ __global__ void __launch_bounds__(kQueryWarps * 32) ray_query_kernel(const uww_r
         const V3 o = {origins[3 * (size_t)q], origins[3 * (size_t)q + 1], origins[3 * (size_t)q + 2]};
         int nbuf = 0;  // warp-uniform
         // every (staged triangle, ray) pair, all lanes
+        // pair pi = t R + k; lanes step by 32 pairs: t by 32 / R, k by 32 % R
+        const int dq = 32 / R, dr = 32 - dq * R;
         auto flush = [&]() {
             const int pairs = nbuf * R;
+            int t = lane / R, k = lane - (lane / R) * R;
             for (int pi = lane; pi < pairs; pi += 32) {
-                const int t = pi / R, k = pi - t * R;
                 const float4 A = tri[warp][3 * t], B = tri[warp][3 * t + 1], Cc = tri[warp][3 * t + 2];
                 const V3 dir = {rdir[warp][3 * k], rdir[warp][3 * k + 1], rdir[warp][3 * k + 2]};
                 const float th = tri_hit({A.x, A.y, A.z}, {B.x, B.y, B.z}, {Cc.x, Cc.y, Cc.z}, {A.w, B.w, Cc.w}, o, dir, rf);
                 if (th >= 0.f) atomicMin(&best[warp][k], __float_as_int(th));
+                t += dq;
+                k += dr;
+                if (k >= R) {
+                    k -= R;
+                    ++t;
+                }
             }
             __syncwarp();
             nbuf = 0;
