@@ -418,3 +418,23 @@ def test_depth_bias_bound_decides_far_chunks(ctx_factory, oracle, bias):
     assert_batches_equal(with_samples, ref)
     want = np.concatenate([oracle.sample_grid(q, d[i]) for i in range(len(d))])
     np.testing.assert_array_equal(with_samples.samples, want)
+
+
+def test_long_runs_of_bias_decided_chunks(ctx_factory, oracle):
+    """A tall column of chunks, nearly all far above or below the surface:
+    control warps run through long runs of depth-bias-decided tickets, more
+    than a CTA keeps pending (their records then resolved at once).  Records,
+    mesh and totals equal the oracle's."""
+    p = abi.reference_params()
+    p.outputs = abi.UWW_OUT_COLOR
+    g = np.arange(2)
+    pos = np.stack(np.meshgrid(g, g, np.arange(-1500, 1500), indexing="ij"), -1).reshape(-1, 3)
+    d = make_descs(pos, 12)
+    ref = oracle.build_chunks(p, d)
+    assert (ref.records["flags"] & abi.UWW_CHUNK_HAS_MESH).sum() > 0
+    ctx = ctx_factory(p)
+    ctx.set_tuning(threads=192, blocks_per_sm=1)  # 152 CTAs: ~79 tickets each, most decided
+    got = ctx.build_chunks_device(d, *caps(ref))
+    assert got.status == abi.UWW_OK
+    assert_batches_equal(got, ref)
+    np.testing.assert_array_equal(got.totals[:3], ref.totals[:3])
