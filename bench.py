@@ -8,7 +8,10 @@ vertices, unit normals and u32 indices per chunk plus per-chunk records.
 
   value    chunks/s of the batched persistent build (fast build, FMA on),
            inputs resident in HBM, CUDA events on the context stream, L2
-           flushed (256 MiB write) before every timed step.
+           flushed (256 MiB write) before every timed step.  The outputs are
+           every chunk's; the build skips the noise of the chunks its depth
+           bias and the fBm bound decide (the roofline counts only the noise
+           it evaluates).
   e2e      chunks/s through uww_build_chunks_host with pinned host buffers:
            descriptor upload, build, record/vertex/normal/index download.
   plain    chunks/s of the plain form: one launch per chunk (the drop-in of
@@ -705,6 +708,7 @@ def main():
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded chunk grid; seeds 0-9 cycle per step)",
         "config": {**config_dict(n, "fast (FMA), persistent grid + device work queue + decoupled look-back, "
+                                    "chunks the depth bias decides settled without their noise, "
                                     "then the per-vertex colour/normal pass"),
                    "mean_verts_per_step": mean_v, "mean_inds_per_step": mean_i,
                    "chunks_decided_by_depth_bias": decided},
