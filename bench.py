@@ -164,13 +164,13 @@ def workload(seed):
 def bias_decided(params, descs) -> int:
     """How many chunks the build decides from the depth bias alone (without
     their noise): a float32 restatement of the kernel's test (fBm bound
-    3/2 * |norm| * sum|amp|, margin 1e-3 (1 + B + |bias|)), used to count the
+    1.11 * |norm| * sum|amp|, margin 1e-3 (1 + B + |bias|)), used to count the
     noise flops the build actually performs."""
     f32 = np.float32
     amps = np.array([params.amplitude * params.persistence ** k for k in range(params.octaves)], np.float64)
     scale = f32(1.1547005383792515)
     norm = scale / f32(amps.sum()) if params.normalize else scale
-    B = f32(1.5) * abs(norm) * f32(np.abs(amps).sum())
+    B = f32(1.11) * abs(norm) * f32(np.abs(amps).sum())
     cells = descs["cells"].astype(np.int64)
     oz = descs["pos"][:, 2].astype(np.int64) * 16
     s = (f32(16) / cells.astype(f32)).astype(f32)

@@ -135,3 +135,35 @@ def test_oracle_range_checks_per_cell_outputs(oracle):
     sub = d[[0, 5, 9]]  # offsets still those of the full grid: beyond a 3-chunk buffer
     with pytest.raises(RuntimeError):
         oracle.build_chunks(p, sub)
+
+
+def test_perlin_bound_used_by_the_depth_bias_shortcut():
+    """The build decides a chunk from its depth bias when the bias keeps every
+    sample beyond the iso level by more than the fBm can reach, with
+    |Perlin| <= 1.11 before the 2/sqrt(3) output scale.  The bound: per corner
+    |g . d| <= S = |dx|+|dy|+|dz| - min(...) for gradients with two +-1
+    components, F = sum_c W_c S_c on a 201^3 grid, plus the Lipschitz margin
+    |grad F| <= 8.5 sqrt(3) times the largest distance to a grid point."""
+    def fade(t):
+        return t * t * t * (t * (t * 6 - 15) + 10)
+    n = 201
+    u = np.linspace(0.0, 1.0, n)
+    U, V, W = np.meshgrid(u, u, u, indexing="ij")
+    F = np.zeros_like(U)
+    for cx in (0, 1):
+        for cy in (0, 1):
+            for cz in (0, 1):
+                w = (fade(U) if cx else 1 - fade(U)) * (fade(V) if cy else 1 - fade(V)) * \
+                    (fade(W) if cz else 1 - fade(W))
+                dx, dy, dz = np.abs(U - cx), np.abs(V - cy), np.abs(W - cz)
+                F += w * (dx + dy + dz - np.minimum(np.minimum(dx, dy), dz))
+    h = 1.0 / (n - 1)
+    bound = F.max() + 8.5 * np.sqrt(3) * h * np.sqrt(3) / 2
+    assert F.max() < 1.037 and bound <= 1.11, (F.max(), bound)
+    # the oracle's Perlin (scaled by 2/sqrt(3)) stays inside the bound
+    from oracle import oracle as O
+    rng = np.random.default_rng(0)
+    xyz = rng.uniform(-300, 300, (200_000, 3))
+    for seed in (0, 1, 7):
+        v = O.perlin(seed, xyz)
+        assert np.abs(v).max() <= 1.0364 * 2 / np.sqrt(3) + 1e-9, np.abs(v).max()

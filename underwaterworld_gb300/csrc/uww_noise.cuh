@@ -120,18 +120,24 @@ __device__ __forceinline__ float z_bias(const DevParams& p, int z, float s, int 
     return 0.f;
 }
 
-// A bound on |fBm|: each octave's Perlin value is the trilinear blend, with
-// weights from the fade curve, of g . d over the cube's corners, where every
-// gradient g has two components of +-1 and one 0 and d is the offset from the
-// corner.  So |g . d| <= |dx| + |dy| + |dz|, and along each axis the blend of
-// |d| is (1 - f(u)) u + f(u) (1 - u) <= 1/2 (at u = 1/2): |value| <= 3/2
-// before the output scale.  The fBm sums the octaves with weights
-// amp_k * norm.
+// A bound on |fBm|.  Each octave's Perlin value is the trilinear blend, with
+// weights W_c from the fade curve, of g_c . d_c over the cube's corners c,
+// where every gradient g_c has two components of +-1 and one 0 and d_c is the
+// offset from the corner; so |g_c . d_c| <= S_c = |dx|+|dy|+|dz| - min(|dx|,
+// |dy|, |dz|) whatever the permutation, and |value| <= F = sum_c W_c S_c.  On
+// a 201^3 grid of the unit cube max F = 1.0364; |grad F| <= 8.5 sqrt(3)
+// (sum_c |dW_c/du| = 2 fade'(u) <= 3.75, S_c <= 2, |dS_c/du| <= 1), so
+// between grid points F exceeds the grid maximum by at most
+// 8.5 sqrt(3) * 0.005 sqrt(3) / 2 = 0.064: |value| <= 1.11 before the output
+// scale (test_oracle.py recomputes both).  The fBm sums the octaves with
+// weights amp_k * norm.
+constexpr float kPerlinBound = 1.11f;
+
 __device__ __forceinline__ float fbm_bound(const DevParams& p)
 {
     float sa = 0.f;
     for (int k = 0; k < p.octaves; ++k) sa += fabsf(p.amp[k]);
-    return 1.5f * fabsf(fbm_norm(p)) * sa;
+    return kPerlinBound * fabsf(fbm_norm(p)) * sa;
 }
 
 // Whether the depth bias alone decides every sample of a chunk with N cells
