@@ -65,6 +65,11 @@ def test_invalid_arguments_are_rejected_on_the_host(built_lib):
     bad = p.copy()
     bad.math_mode = 7
     assert L.uww_ctx_create(C.byref(bad), None, C.byref(h)) == abi.UWW_ERR_INVALID_ARG
+    for field, value in (("bias_a", float("inf")), ("bias_c", float("nan")), ("color_max_z", float("inf")),
+                         ("outputs", 16)):
+        bad = p.copy()
+        setattr(bad, field, value)
+        assert L.uww_ctx_create(C.byref(bad), None, C.byref(h)) == abi.UWW_ERR_INVALID_ARG, field
     assert L.uww_ctx_create(C.byref(p), None, None) == abi.UWW_ERR_INVALID_ARG
     assert L.uww_build_chunks(None, None, 0, 12, None) == abi.UWW_ERR_INVALID_ARG
     assert L.uww_perm_table(0, None) == abi.UWW_ERR_INVALID_ARG

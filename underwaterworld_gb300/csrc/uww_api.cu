@@ -78,6 +78,9 @@ int validate_params(const uww_params* p)
         return UWW_ERR_INVALID_ARG;
     if (!finite(p->iso_level) || !finite(p->offset[0]) || !finite(p->offset[1]) || !finite(p->offset[2]))
         return UWW_ERR_INVALID_ARG;
+    if (!finite(p->bias_a) || !finite(p->bias_b) || !finite(p->bias_c)) return UWW_ERR_INVALID_ARG;
+    if (!finite(p->color_min_z) || !finite(p->color_max_z)) return UWW_ERR_INVALID_ARG;
+    if (p->outputs & ~(UWW_OUT_COLOR | UWW_OUT_NORMALS | UWW_OUT_CASES | UWW_OUT_SAMPLES)) return UWW_ERR_INVALID_ARG;
     if (p->bias_mode < UWW_BIAS_NONE || p->bias_mode > UWW_BIAS_LINEAR) return UWW_ERR_INVALID_ARG;
     if (p->bias_mode == UWW_BIAS_TERRACED && (p->bias_b == 0.f || p->bias_c == 0.f)) return UWW_ERR_INVALID_ARG;
     if (p->math_mode != UWW_MATH_EXACT && p->math_mode != UWW_MATH_FAST) return UWW_ERR_INVALID_ARG;
@@ -409,7 +412,6 @@ int uww_ctx_create(const uww_params* p, void* stream, uww_ctx** out)
     ctx->smem_optin = (size_t)optin;
     if (e == cudaSuccess) {
         where = "cudaFuncSetAttribute(MaxDynamicSharedMemorySize)";
-        const size_t static_smem = build_static_smem_bytes();
         e = prepare_build_kernels(ctx->smem_optin, &ctx->smem_dyn_max);
     }
     if (e == cudaSuccess) {

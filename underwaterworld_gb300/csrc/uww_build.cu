@@ -1028,8 +1028,6 @@ size_t set_smem_attr(BuildFn fn, size_t optin)
 
 }  // namespace
 
-size_t build_static_smem_bytes() { return sizeof(SmemTables); }
-
 cudaError_t prepare_build_kernels(size_t optin, size_t* max_dyn_smem)
 {
     size_t m = ~size_t(0);

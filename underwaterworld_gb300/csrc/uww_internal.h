@@ -126,7 +126,6 @@ long long spin_limit_cycles();
 int default_compute_threads(uint32_t max_cells);
 
 // Launch helpers (uww_build.cu).
-size_t build_static_smem_bytes();
 cudaError_t launch_build(const DevParams& p, const BuildArgs& a, bool queue, int grid, int threads,
                          size_t dyn_smem, cudaStream_t s);
 cudaError_t build_occupancy(bool queue, bool exact, int threads, size_t dyn_smem, int* blocks_per_sm);
