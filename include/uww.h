@@ -167,9 +167,8 @@ int uww_layout_cells(uww_chunk_desc* desc, uint32_t n, uint64_t* total_cells, ui
 /* stream: a cudaStream_t, or NULL for a stream the context creates and owns.
  * create and set_params refuse, with UWW_ERR_INVALID_ARG, parameters with a
  * non-finite float, octaves outside 1..UWW_MAX_OCTAVES, chunk_size outside
- * 1..2^20, an unknown mode or
- * output bit, a terraced bias with bias_b or bias_c zero, or an empty colour
- * ramp (color_min_z == color_max_z). */
+ * 1..2^20, an unknown mode or output bit, a terraced bias with bias_b or
+ * bias_c zero, or an empty colour ramp (color_min_z == color_max_z). */
 int   uww_ctx_create(const uww_params* p, void* stream, uww_ctx** out);
 int   uww_ctx_destroy(uww_ctx* ctx);
 int   uww_ctx_set_params(uww_ctx* ctx, const uww_params* p);
