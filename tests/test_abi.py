@@ -73,3 +73,16 @@ def test_invalid_arguments_are_rejected_on_the_host(built_lib):
     assert L.uww_ctx_create(C.byref(p), None, None) == abi.UWW_ERR_INVALID_ARG
     assert L.uww_build_chunks(None, None, 0, 12, None) == abi.UWW_ERR_INVALID_ARG
     assert L.uww_perm_table(0, None) == abi.UWW_ERR_INVALID_ARG
+
+
+def test_totals_status_maps_every_error_flag():
+    """The Python mirror reads a device build's totals words as the C host path
+    does: timeout first, then a bad descriptor or an out-of-range per-cell or
+    per-sample write, then a capacity overflow."""
+    from underwaterworld_gb300.chunk import totals_status
+    t = lambda ovf, flags: np.array([10, 30, ovf, flags], np.uint64)
+    assert totals_status(t(0, 0)) == abi.UWW_OK
+    assert totals_status(t(3, 0)) == abi.UWW_ERR_CAPACITY
+    assert totals_status(t(0, abi.UWW_ERRFLAG_BAD)) == abi.UWW_ERR_INVALID_ARG
+    assert totals_status(t(0, abi.UWW_ERRFLAG_RANGE)) == abi.UWW_ERR_INVALID_ARG
+    assert totals_status(t(3, abi.UWW_ERRFLAG_RANGE | abi.UWW_ERRFLAG_TIMEOUT)) == abi.UWW_ERR_TIMEOUT

@@ -95,9 +95,10 @@ def total_samples(descs) -> int:
 
 def totals_status(totals) -> int:
     """Status of a finished device build from its totals words."""
-    if int(totals[3]) & 1:
+    flags = int(totals[3])
+    if flags & abi.UWW_ERRFLAG_TIMEOUT:
         return abi.UWW_ERR_TIMEOUT
-    if int(totals[3]) & 2:
+    if flags & (abi.UWW_ERRFLAG_BAD | abi.UWW_ERRFLAG_RANGE):
         return abi.UWW_ERR_INVALID_ARG
     if int(totals[2]):
         return abi.UWW_ERR_CAPACITY
