@@ -300,9 +300,6 @@ class Chunk:
     context's stream; the accessors follow chunk.rs:344-348.
     """
 
-    MAX_VERTS = 5 * 3 * INTERNAL_SIZE ** 3
-    MAX_INDS = 5 * 3 * INTERNAL_SIZE ** 3
-
     def __init__(self, pos, cells: int = INTERNAL_SIZE):
         self.pos = tuple(int(v) for v in pos)
         self.cells = int(cells)
@@ -319,8 +316,8 @@ class Chunk:
 
     def build_full(self, ctx: Context):
         d = make_descs([self.pos], self.cells)
-        n3 = self.cells ** 3
-        vcap = icap = 15 * n3
+        # at most 5 triangles per cell, and never more vertices than indices
+        vcap = icap = 15 * self.cells ** 3
         d_desc = ctx.upload(d)
         d_rec, d_tot = DeviceArray(32), DeviceArray(32)
         d_verts, d_inds = DeviceArray(vcap * 24), DeviceArray(icap * 4)
@@ -331,6 +328,9 @@ class Chunk:
         check(lib().uww_build_chunk_plain(ctx.h, C.c_void_p(d_desc.ptr), self.cells, C.byref(out)),
               "uww_build_chunk_plain")
         ctx.sync()
+        st = totals_status(ctx.download(d_tot, (4,), np.uint64))
+        if st:
+            raise abi.UWWError(st, "uww_build_chunk_plain")
         self._record = ctx.download(d_rec, (1,), abi.CHUNK_RECORD_DTYPE)[0]
         nv, ni = int(self._record["num_verts"]), int(self._record["num_inds"])
         self._verts = ctx.download(d_verts, (nv,), abi.VERT_COLOR_DTYPE)
