@@ -260,7 +260,10 @@ int uww_autotune(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint3
  * the device), and copy the records (if h_records) and totals (if h_totals,
  * page-locked) back.  The mesh stays in d_out's device buffers.  The graph is
  * captured once, on the context stream, with the context's parameters;
- * uww_frame_set_params recaptures it and updates the instantiated graph. */
+ * uww_frame_set_params recaptures it and updates the instantiated graph.
+ * The graph reads h_chunks and h_count and writes h_records and h_totals
+ * while it runs: fill the next frame's descriptors only after the previous
+ * launch has finished (uww_ctx_sync). */
 typedef struct uww_frame uww_frame;
 int uww_frame_create(uww_ctx* ctx, uint32_t max_chunks, uint32_t max_cells, const uww_chunk_desc* h_chunks,
                      const uint32_t* h_count, const uww_mesh_out* d_out, uww_chunk_record* h_records,

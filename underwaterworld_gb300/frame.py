@@ -43,9 +43,12 @@ class FrameBuilder:
         self.handle = h.value
 
     def submit(self, descs: np.ndarray):
-        """Stage this frame's descriptors and launch the graph (asynchronous)."""
+        """Stage this frame's descriptors and launch the graph (asynchronous).
+        The graph reads the staging buffer while it runs, so the previous
+        frame must have finished (``ctx.sync()``, as :meth:`build` does)."""
         n = descs.shape[0]
-        assert n <= self.max_chunks
+        if n > self.max_chunks:
+            raise ValueError(f"{n} chunks exceed the frame's maximum of {self.max_chunks}")
         self.h_desc.array[:n] = descs
         self.h_count.array[0] = n
         check(lib().uww_frame_launch(C.c_void_p(self.handle)), "uww_frame_launch")

@@ -16,7 +16,7 @@ import numpy as np
 
 from . import abi
 from .abi import check, lib
-from .chunk import Context, DeviceArray, total_cells
+from .chunk import Context, DeviceArray, total_cells, totals_status
 
 WALL_RANGE = 3  # boid.rs:15
 
@@ -45,9 +45,9 @@ class RayScene:
         check(L.uww_chunk_index(ctx.h, C.c_void_p(self.d_desc.ptr), n, C.c_void_p(self.d_table.ptr), self.table_size),
               "uww_chunk_index")
         ctx.sync()
-        tot = ctx.download(self.d_tot, (4,), np.uint64)
-        if int(tot[2]) or int(tot[3]):
-            raise abi.UWWError(abi.UWW_ERR_CAPACITY, "scene build")
+        st = totals_status(ctx.download(self.d_tot, (4,), np.uint64))
+        if st:
+            raise abi.UWWError(st, "scene build")
         self.scene = abi.RayScene(self.d_desc.ptr, self.d_rec.ptr, self.d_verts.ptr, self.d_inds.ptr, self.d_cases.ptr,
                                   self.d_first.ptr, self.d_table.ptr, n, self.table_size)
 
