@@ -44,6 +44,11 @@ int main(int argc, char** argv)
             std::fprintf(stderr, "plain and batched builds differ (%d)\n", mismatches);
             return 1;
         }
+        // an empty list builds nothing
+        if (!build_chunks(perlin, {}).empty()) {
+            std::fprintf(stderr, "an empty list gave chunks\n");
+            return 1;
+        }
 
         FILE* f = std::fopen(argv[1], "wb");
         if (!f) return 3;

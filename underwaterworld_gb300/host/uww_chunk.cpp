@@ -177,6 +177,7 @@ std::vector<Tri> Chunk::tris_around(const Vec3& p, int32_t range) const
 std::vector<Chunk> build_chunks(const Perlin& perlin, const std::vector<Pos>& positions, uint32_t cells)
 {
     const uint32_t n = (uint32_t)positions.size();
+    if (n == 0) return {};
     std::vector<uww_chunk_desc> desc(n);
     for (uint32_t i = 0; i < n; ++i) {
         std::memset(&desc[i], 0, sizeof(desc[i]));
