@@ -17,7 +17,7 @@ import numpy as np
 
 from . import abi
 from .abi import check, lib
-from .chunk import Context, DeviceArray, make_descs, total_cells, total_samples
+from .chunk import Context, DeviceArray, make_descs, total_cells, total_samples, totals_status
 
 
 def theta_from_params(p: abi.Params) -> np.ndarray:
@@ -87,7 +87,8 @@ class Adjoint:
     # -- transfers -------------------------------------------------------------------
     def set_pos_grad(self, g: np.ndarray):
         g = np.ascontiguousarray(g, dtype=np.float32)
-        assert g.size <= 3 * self.vcap
+        if g.size > 3 * self.vcap:
+            raise ValueError(f"{g.size} gradient entries exceed 3 x the vertex capacity {self.vcap}")
         check(lib().uww_memcpy(self.ctx.h, C.c_void_p(self.d_pos_grad.ptr), g.ctypes.data_as(C.c_void_p), g.nbytes,
                                abi.H2D), "pos_grad upload")
         self.ctx.sync()
@@ -97,8 +98,9 @@ class Adjoint:
 
     def fetch_forward(self) -> dict:
         tot = self.totals()
-        if int(tot[2]) or int(tot[3]):
-            raise abi.UWWError(abi.UWW_ERR_CAPACITY if not int(tot[3]) else abi.UWW_ERR_INVALID_ARG, "uww_forward")
+        st = totals_status(tot)
+        if st:
+            raise abi.UWWError(st, "uww_forward")
         nv = int(tot[0])
         return {"totals": tot,
                 "records": self.ctx.download(self.d_rec, (self.n,), abi.CHUNK_RECORD_DTYPE),
@@ -110,7 +112,8 @@ class Adjoint:
         return self.ctx.download(self.d_theta, (abi.theta_count(self.K),), np.float32)
 
     def sample_grad(self) -> np.ndarray:
-        assert self.d_sgrad is not None
+        if self.d_sgrad is None:
+            raise ValueError("built without sample_grad=True")
         return self.ctx.download(self.d_sgrad, (self.nsamp,), np.float32)
 
 
@@ -194,10 +197,11 @@ class TerrainFit:
     def step(self) -> tuple[float, np.ndarray]:
         for _ in range(8):
             loss, g, tot = self._evaluate()
-            if int(tot[3]):
-                raise abi.UWWError(abi.UWW_ERR_INVALID_ARG, "terrain fit forward")
-            if not int(tot[2]):
+            st = totals_status(tot)
+            if st == abi.UWW_OK:
                 break
+            if st != abi.UWW_ERR_CAPACITY:
+                raise abi.UWWError(st, "terrain fit forward")
             a = self.adj
             self.adj = Adjoint(self.ctx, self.descs, max(2 * a.vcap, int(tot[0]) + 1),
                                max(2 * a.icap, int(tot[1]) + 1))
