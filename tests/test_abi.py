@@ -86,3 +86,14 @@ def test_totals_status_maps_every_error_flag():
     assert totals_status(t(0, abi.UWW_ERRFLAG_BAD)) == abi.UWW_ERR_INVALID_ARG
     assert totals_status(t(0, abi.UWW_ERRFLAG_RANGE)) == abi.UWW_ERR_INVALID_ARG
     assert totals_status(t(3, abi.UWW_ERRFLAG_RANGE | abi.UWW_ERRFLAG_TIMEOUT)) == abi.UWW_ERR_TIMEOUT
+
+
+def test_rust_binding_declares_every_entry_point():
+    """The extern "C" block a Rust host adds declares every
+    function of include/uww.h, each once."""
+    import re
+    from pathlib import Path
+    text = (Path(__file__).resolve().parent.parent / "INTEGRATION.md").read_text()
+    bound = re.findall(r"pub fn (uww_\w+)\(", text)
+    assert sorted(bound) == sorted(set(bound))
+    assert set(bound) == set(abi.declared_functions()), set(bound) ^ set(abi.declared_functions())
