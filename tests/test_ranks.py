@@ -50,3 +50,28 @@ def test_two_gloo_ranks_weak_scaling(built_lib, oracle):
     assert not set(s0) & set(s1), "ranks must use distinct seeds"
     assert c0 == c1 == [64.0, float(v0 + v1)]   # chunks and vertices of both ranks
     assert t0 == t1 == 1.5                      # the slowest rank's time
+
+
+def test_reference_arm_runs_on_rank_zero_only(built_lib, oracle, monkeypatch, capsys):
+    """`bench.py --impl reference` under a 2-rank launch: rank 1 exits without
+    work or output; rank 0 times exactly --steps bounded steps on the host
+    cores and prints one JSON line for the launch's world size."""
+    import argparse
+    import json
+    sys.path.insert(0, str(ROOT))
+    import bench
+    monkeypatch.setattr(bench, "REF_BUDGET_S", 0.5)
+    args = argparse.Namespace(steps=7, warmup=3)
+    monkeypatch.setenv("WORLD_SIZE", "2")
+    monkeypatch.setenv("RANK", "1")
+    bench.run_reference(args)
+    assert capsys.readouterr().out == ""
+    monkeypatch.setenv("RANK", "0")
+    bench.run_reference(args)
+    lines = [l for l in capsys.readouterr().out.splitlines() if l.strip()]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["steps"] == 7 and d["warmup"] == 3 and d["n_gpus"] == 2
+    assert d["value"] > 0 and d["unit"] == bench.UNIT and d["metric"] == bench.METRIC
+    assert d["cpu_baseline"]["value"] == d["value"] and d["e2e"]["h2d_bytes_per_step"] == 0
+    assert 32 <= d["config"]["chunks_per_timed_step"] <= 4096
