@@ -20,7 +20,8 @@ vertices, unit normals and u32 indices per chunk plus per-chunk records.
 
 ``--impl reference`` times the reference algorithm on the host cores instead:
 the CPU oracle in reference semantics (f64 noise, O(V) linear dedup search,
-powf colours), with all host threads, on the same workload.
+powf colours), with all host threads, on the same workload: exactly --steps
+timed steps, each a bounded slice of the grid, about 30 s in all.
 """
 from __future__ import annotations
 
