@@ -163,11 +163,11 @@ def workload(seed):
     return workloads.uniform_grid(seed=seed, outputs=abi.UWW_OUT_COLOR | abi.UWW_OUT_NORMALS)
 
 
-def bias_decided(params, descs) -> int:
-    """How many chunks the build decides from the depth bias alone (without
-    their noise): a float32 restatement of the kernel's test (fBm bound
-    1.11 * |norm| * sum|amp|, margin 1e-3 (1 + B + |bias|)), used to count the
-    noise flops the build actually performs."""
+def bias_decided_mask(params, descs) -> np.ndarray:
+    """Which chunks the build decides from the depth bias alone (without their
+    noise): a float32 restatement of the kernel's test (fBm bound
+    1.11 * |norm| * sum|amp|, margin 1e-3 (1 + B + |bias|)), for the linear
+    bias of the measured workloads; all False for the other bias modes."""
     f32 = np.float32
     amps = np.array([params.amplitude * params.persistence ** k for k in range(params.octaves)], np.float64)
     scale = f32(1.1547005383792515)
@@ -176,14 +176,20 @@ def bias_decided(params, descs) -> int:
     cells = descs["cells"].astype(np.int64)
     oz = descs["pos"][:, 2].astype(np.int64) * 16
     s = (f32(16) / cells.astype(f32)).astype(f32)
-    if params.bias_mode != 2:  # linear only here (the workloads measured use it)
-        return 0
+    if params.bias_mode != 2:
+        return np.zeros(len(descs), bool)
     b0 = f32(params.bias_a) * (oz.astype(f32) - f32(params.bias_b))
     b1 = f32(params.bias_a) * ((cells.astype(f32) * s + oz.astype(f32)).astype(f32) - f32(params.bias_b))
     lo, hi = np.minimum(b0, b1), np.maximum(b0, b1)
     m = f32(1e-3) * (f32(1) + B + np.maximum(np.abs(lo), np.abs(hi)))
     iso = f32(params.iso_level)
-    return int(((lo - B - m > iso) | (hi + B + m < iso)).sum())
+    return (lo - B - m > iso) | (hi + B + m < iso)
+
+
+def bias_decided(params, descs) -> int:
+    """How many chunks the depth bias decides; used to count the noise flops
+    the build actually performs."""
+    return int(bias_decided_mask(params, descs).sum())
 
 
 def cpu_reference(descs, seeds, threads, budget_s=20.0):

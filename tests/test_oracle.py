@@ -167,3 +167,26 @@ def test_perlin_bound_used_by_the_depth_bias_shortcut():
     for seed in (0, 1, 7):
         v = O.perlin(seed, xyz)
         assert np.abs(v).max() <= 1.0364 * 2 / np.sqrt(3) + 1e-9, np.abs(v).max()
+
+
+def test_depth_bias_decided_chunks_have_no_mesh_in_the_oracle(oracle):
+    """The chunks bench.py counts as decided by the depth bias (its float32
+    restatement of the build's test, which sets the roofline's flop count) are,
+    in the oracle at both precisions, early blank (every sample above the iso
+    level) or solid (every case 255): none of them has a mesh."""
+    import bench
+    from underwaterworld_gb300 import abi
+    from underwaterworld_gb300.chunk import make_descs
+    p, d = bench.workload(3)
+    p.outputs = abi.UWW_OUT_CASES
+    mask = bench.bias_decided_mask(p, d)
+    assert mask.sum() == 2560
+    sub = d[mask][::8]
+    sub = make_descs(sub["pos"], sub["cells"])
+    for prec in (oracle.F32, oracle.F64):
+        b = oracle.build_chunks(p, sub, precision=prec)
+        assert (b.records["num_inds"] == 0).all()
+        blank = (b.records["flags"] & abi.UWW_CHUNK_EARLY_BLANK) != 0
+        solid = (b.cases.reshape(len(sub), -1) == 255).all(axis=1)
+        assert (blank | solid).all()
+        assert blank.any() and solid.any()
