@@ -97,3 +97,42 @@ def test_rust_binding_declares_every_entry_point():
     bound = re.findall(r"pub fn (uww_\w+)\(", text)
     assert sorted(bound) == sorted(set(bound))
     assert set(bound) == set(abi.declared_functions()), set(bound) ^ set(abi.declared_functions())
+
+
+def test_ctypes_mirrors_match_the_header_layouts(tmp_path):
+    """Every struct of include/uww.h has the same size and field offsets in the
+    Python mirror (compiled with gcc against the header)."""
+    import shutil
+    from pathlib import Path
+    import pytest
+    if not shutil.which("gcc"):
+        pytest.skip("gcc not available")
+    mirrors = {"uww_params": abi.Params, "uww_chunk_desc": abi.ChunkDesc, "uww_chunk_record": abi.ChunkRecord,
+               "uww_mesh_out": abi.MeshOut, "uww_ray_scene": abi.RayScene,
+               "uww_schedule_params": abi.ScheduleParams, "uww_camera_uniform": abi.CameraUniform,
+               "uww_tuning": abi.Tuning}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "uww.h"', "int main(void) {"]
+    for cname, cls in mirrors.items():
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for f in cls._fields_:
+            lines.append(f'printf("{cname} {f[0]} %zu\\n", offsetof({cname}, {f[0]}));')
+    lines.append('printf("uww_vert_color size %zu\\n", sizeof(uww_vert_color));')
+    for f in abi.VERT_COLOR_DTYPE.names:
+        lines.append(f'printf("uww_vert_color {f} %zu\\n", offsetof(uww_vert_color, {f}));')
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    inc = Path(__file__).resolve().parent.parent / "include"
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c11", f"-I{inc}", str(src), "-o", str(exe)], check=True)
+    got = {}
+    for line in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.splitlines():
+        s, f, v = line.split()
+        got[(s, f)] = int(v)
+    for cname, cls in mirrors.items():
+        assert got[(cname, "size")] == C.sizeof(cls), cname
+        for f in cls._fields_:
+            assert got[(cname, f[0])] == getattr(cls, f[0]).offset, (cname, f[0])
+    assert got[("uww_vert_color", "size")] == abi.VERT_COLOR_DTYPE.itemsize
+    for f in abi.VERT_COLOR_DTYPE.names:
+        assert got[("uww_vert_color", f)] == abi.VERT_COLOR_DTYPE.fields[f][1], f
