@@ -136,3 +136,31 @@ def test_ctypes_mirrors_match_the_header_layouts(tmp_path):
     assert got[("uww_vert_color", "size")] == abi.VERT_COLOR_DTYPE.itemsize
     for f in abi.VERT_COLOR_DTYPE.names:
         assert got[("uww_vert_color", f)] == abi.VERT_COLOR_DTYPE.fields[f][1], f
+
+
+def test_ctypes_signatures_match_the_header_prototypes():
+    """Each function's ctypes signature has the header prototype's argument
+    count, integer widths and return kind (int status, pointer, or void)."""
+    import re
+    text = re.sub(r"/\*.*?\*/", "", abi.HEADER.read_text(), flags=re.S)
+    protos = re.findall(r"^\s*((?:const )?\w+\s*\**)\s*(uww_\w+)\s*\(([^;]*)\)\s*;", text, flags=re.M)
+    assert {name for _, name, _ in protos} == set(abi.declared_functions())
+    widths = {"uint32_t": C.c_uint32, "int32_t": C.c_int32, "uint64_t": C.c_uint64, "int": C.c_int,
+              "size_t": C.c_size_t, "float": C.c_float, "double": C.c_double}
+    for ret, name, args in protos:
+        res, argtypes = abi._SIGS[name]
+        params = [] if " ".join(args.split()) in ("", "void") else [a.strip() for a in args.split(",")]
+        assert len(params) == len(argtypes), name
+        for decl, t in zip(params, argtypes):
+            base = decl.replace("const ", "").split()[0]
+            if "*" in decl or "[" in decl:
+                assert t in (C.c_void_p, C.c_char_p) or issubclass(t, C._Pointer), (name, decl)
+            else:
+                assert C.sizeof(t) == C.sizeof(widths[base]), (name, decl)
+        ret = ret.strip()
+        if "*" in ret:
+            assert res in (C.c_void_p, C.c_char_p), name
+        elif ret == "void":
+            assert res is None, name
+        else:
+            assert res is C.c_int, name
