@@ -220,8 +220,7 @@ def run_reference(args):
     Each step builds a bounded slice of the 4096-chunk grid, rotating through
     the grid and the seeds.  The slice is sized from an untimed calibration
     build (after the warm-up steps) so that the timed steps take about
-    REF_BUDGET_S.  Under torchrun,
-    rank 0 alone runs it."""
+    REF_BUDGET_S.  Under torchrun, rank 0 alone runs it."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
