@@ -87,7 +87,7 @@ def test_threads_do_not_change_results(oracle):
 
 
 def test_reference_grid_structure(oracle):
-    """Config 1 at the reference iso-level: blank chunks, u16-sized meshes, terraced surface."""
+    """The 5x5x5 reference grid at the reference iso-level: blank chunks, u16-sized meshes, terraced surface."""
     p, d = workloads.reference_grid(outputs=abi.UWW_OUT_COLOR | abi.UWW_OUT_CASES)
     b = oracle.build_chunks(p, d, precision=oracle.F64)
     r = b.records
