@@ -54,12 +54,15 @@ FLOPS_PER_OCTAVE_GRAD = 254    # Perlin value + analytic gradient + accumulate (
 FLOPS_PER_VERTEX_EXTRA = 60    # interpolation, colour ramp, normalisation
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one build_kernel
-# launch on this workload, from an ncu capture of this script's own step
-# (--steps 5 --warmup 3 --quick --no-cpu, mean of its 18 build launches:
-# 263.4 KB read + 3.7 KB written, caches flushed before each launch).
-# The outputs stay in L2 (write-back) when the kernel ends, so this is below
-# the algorithmic output bytes.
-NCU_DRAM_BYTES_PER_LAUNCH = 267_036
+# launch on this workload, from a single-kernel ncu capture of this script's
+# own step (-k regex:build_kernel -s 12 -c 1 of
+# `bench.py --steps 5 --warmup 3 --quick --no-cpu`, caches flushed before the
+# launch): 257.5 KB read + 4.1 KB written.  The outputs stay in L2
+# (write-back) when the kernel ends, so this is below the algorithmic output
+# bytes.
+NCU_DRAM_BYTES_PER_LAUNCH = 261_632
+NCU_TRAFFIC_SOURCE = ("ncu --set full -k regex:build_kernel -s 12 -c 1, python bench.py --steps 5 --warmup 3 "
+                      "--quick --no-cpu: dram__bytes_read.sum + dram__bytes_write.sum of that launch")
 
 
 def parse():
@@ -150,17 +153,17 @@ def rank_seeds(rank: int):
     return [(s + rank * N_SEEDS) % 1000 for s in range(N_SEEDS)]
 
 
-def config_dict(n: int, build: str) -> dict:
+def config_dict(n: int, l2: str = "flushed (256 MiB write) before each timed step") -> dict:
+    """The workload both arms run; identical between them but for the L2 note."""
     return {"workload": "uniform grid: 16x16x16 = 4096 chunks of 12^3 cells (13^3 f32 samples), "
                         "4-oct fBm f=0.04 lac 2 pers 0.5, bias -0.03(z-128), iso 0; "
                         "outputs VertColor + normals + u32 indices",
-            "chunks_per_step": n, "cells_per_step": n * 12 ** 3, "samples_per_step": n * 13 ** 3,
-            "build": build, "l2": "flushed (256 MiB write) before each timed step"}
+            "chunks_per_step": n, "cells_per_step": n * 12 ** 3, "samples_per_step": n * 13 ** 3, "l2": l2}
 
 
 def workload(seed):
-    from underwaterworld_gb300 import abi, workloads
-    return workloads.uniform_grid(seed=seed, outputs=abi.UWW_OUT_COLOR | abi.UWW_OUT_NORMALS)
+    from underwaterworld_gb300 import layout, workloads
+    return workloads.uniform_grid(seed=seed, outputs=layout.UWW_OUT_COLOR | layout.UWW_OUT_NORMALS)
 
 
 def bias_decided_mask(params, descs) -> np.ndarray:
@@ -194,14 +197,15 @@ def bias_decided(params, descs) -> int:
 
 def cpu_reference(descs, seeds, threads, budget_s=20.0):
     """The reference algorithm on the host: oracle in f64 reference semantics with
-    the O(V) dedup search and colours (no normals, like the reference)."""
+    the O(V) dedup search and colours (no normals, like the reference).  Whole
+    grids, one seed each, until budget_s has passed.  Loads no GPU library."""
     from oracle import oracle as O
-    from underwaterworld_gb300 import abi
+    from underwaterworld_gb300 import layout
     O.build()
     done, t0, i = 0, time.perf_counter(), 0
     while True:
         p, _ = workload(seeds[i % len(seeds)])
-        p.outputs = abi.UWW_OUT_COLOR
+        p.outputs = layout.UWW_OUT_COLOR
         O.build_chunks(p, descs, precision=O.F64, search=O.SEARCH_LINEAR, threads=threads)
         done += len(descs)
         i += 1
@@ -210,23 +214,27 @@ def cpu_reference(descs, seeds, threads, budget_s=20.0):
             return done / el, done, el
 
 
-REF_BUDGET_S = 30.0  # target length of the reference arm's timed steps
+REF_BUDGET_S = 150.0        # upper bound on the reference arm's timed steps
+REF_ONE_THREAD_S = 10.0     # the single-threaded figure beside it
 
 
 def run_reference(args):
     """The reference arm: the reference's algorithm (the CPU oracle in f64
     reference semantics, with its O(V) dedup search and colours) on every host
-    core, for this arm's workload and metric.  It times exactly --steps steps.
-    Each step builds a bounded slice of the 4096-chunk grid, rotating through
-    the grid and the seeds.  The slice is sized from an untimed calibration
-    build (after the warm-up steps) so that the timed steps take about
-    REF_BUDGET_S.  Under torchrun, rank 0 alone runs it."""
+    core, for this arm's workload and metric.  It times exactly --steps steps;
+    each step builds the whole 4096-chunk grid with the next seed, unless
+    --steps whole grids would take longer than REF_BUDGET_S (measured on the
+    warm-up steps), in which case each step builds a rotating slice of the
+    grid sized to fit.  The reference itself is single-threaded
+    (README.md:19), so a single-thread figure on whole grids is reported
+    beside it.  Under torchrun, rank 0 alone runs it.  Nothing here loads the
+    GPU library: the parameters and struct layouts come from
+    underwaterworld_gb300.layout."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
     from oracle import oracle as O
-    from underwaterworld_gb300 import abi
-    from underwaterworld_gb300.chunk import make_descs
+    from underwaterworld_gb300 import layout
     O.build()
     _, descs = workload(0)
     n = len(descs)
@@ -234,23 +242,26 @@ def run_reference(args):
     params = []
     for seed in range(N_SEEDS):
         p, _ = workload(seed)
-        p.outputs = abi.UWW_OUT_COLOR
+        p.outputs = layout.UWW_OUT_COLOR
         params.append(p)
 
-    def build(p, d):
-        O.build_chunks(p, d, precision=O.F64, search=O.SEARCH_LINEAR, threads=threads)
+    def build(p, d, th=threads):
+        O.build_chunks(p, d, precision=O.F64, search=O.SEARCH_LINEAR, threads=th)
 
     def step_slice(s, size):
+        if size >= n:
+            return descs
         idx = (s * size + np.arange(size)) % n
-        return make_descs(descs["pos"][idx], descs["cells"][idx])
+        return layout.make_descs(descs["pos"][idx], descs["cells"][idx])
 
-    for w in range(max(args.warmup, 1)):
-        build(params[w % N_SEEDS], step_slice(w, 256))
-    t0 = time.perf_counter()
-    build(params[0], step_slice(1, 512))
-    rate = 512 / (time.perf_counter() - t0)
     steps = max(1, args.steps)
-    per_step = int(min(n, max(32, rate * REF_BUDGET_S / steps)))
+    wt = []
+    for w in range(max(args.warmup, 1)):
+        t0 = time.perf_counter()
+        build(params[w % N_SEEDS], descs)
+        wt.append(time.perf_counter() - t0)
+    grid_s = min(wt)
+    per_step = n if steps * grid_s <= REF_BUDGET_S else int(max(32, n * REF_BUDGET_S / (steps * grid_s)))
     elapsed = 0.0
     for s in range(steps):
         d = step_slice(s, per_step)
@@ -258,17 +269,21 @@ def run_reference(args):
         build(params[s % N_SEEDS], d)
         elapsed += time.perf_counter() - t0
     value = steps * per_step / elapsed
+    one_v, one_n, one_el = cpu_reference(descs, list(range(N_SEEDS)), 1, budget_s=REF_ONE_THREAD_S)
+    cpu = cpu_model()
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {**config_dict(n, "CPU oracle, reference semantics (f64 noise, O(V) dedup search)"),
-                   "threads": threads, "l2": "n/a (CPU)", "device": "host CPU cores (no GPU used)",
-                   "chunks_per_timed_step": per_step},
+        "config": config_dict(n, l2="n/a (host CPU)"),
+        "build": "CPU oracle, reference semantics (f64 noise, O(V) dedup search)", "threads": threads, "device": f"host CPU cores, no GPU used ({cpu})",
+        "chunks_per_timed_step": per_step,
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{per_step} chunks per step (a rotating slice of the 4096-chunk grid, "
-                                   f"seeds cycling), {steps} steps in {elapsed:.1f} s, {threads} threads, "
-                                   f"CPU: {cpu_model()}"},
+                         "sample": f"{per_step} chunks per step ({'the whole 4096-chunk grid' if per_step >= n else 'a rotating slice of the 4096-chunk grid'}, "
+                                   f"seeds cycling), {steps} steps in {elapsed:.1f} s, {threads} threads, CPU: {cpu}"},
+        "single_thread": {"value": one_v, "unit": UNIT, "cores": 1,
+                          "sample": f"{one_n} chunks ({one_n // n} whole grids, seeds 0..) in {one_el:.1f} s, 1 thread "
+                                    f"(the reference is single-threaded)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -285,6 +300,137 @@ def timed(stream, fn, flush=None):
     e1.record(stream)
     e1.synchronize()
     return e0.elapsed_time(e1) * 1e-3
+
+
+CLOCK_WINDOW_S = 2.0   # nvidia-smi watches the timed build at least this long
+
+
+def probe_lib():
+    """The benchmark's measurement kernels (libuww_bench_probe.so)."""
+    from underwaterworld_gb300 import build as B
+    L = C.CDLL(str(B.build_probe()))
+    L.bench_probe_fma.argtypes = [C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p, C.POINTER(C.c_double)]
+    L.bench_probe_fma.restype = C.c_int
+    L.bench_probe_host_write.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_uint32, C.c_void_p]
+    L.bench_probe_host_write.restype = C.c_int
+    return L
+
+
+def leg_fp32_peak(stream, dev, sms, gpu_index, window_s=1.0):
+    """FP32 peak: the FMA probe (8 CTAs of 256 threads per SM, 8 independent
+    FMA chains per thread), timed launch by launch for about window_s with
+    nvidia-smi sampling the clocks; reported as measured (the fastest launch)
+    and as SMs x 128 lanes x 2 flops x the median SM clock under the probe."""
+    import torch
+    PL = probe_lib()
+    blocks = sms * 8
+    sink = torch.empty(blocks * 256, dtype=torch.float32, device=dev)
+    fl = C.c_double()
+    h = C.c_void_p(stream.cuda_stream)
+    for _ in range(3):
+        assert PL.bench_probe_fma(blocks, 4096, C.c_void_p(sink.data_ptr()), h, C.byref(fl)) == 0
+    torch.cuda.synchronize()
+    clk = ClockSampler(gpu_index)
+    clk.start()
+    rates, t0 = [], time.perf_counter()
+    while time.perf_counter() - t0 < window_s or len(rates) < 5:
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        PL.bench_probe_fma(blocks, 4096, C.c_void_p(sink.data_ptr()), h, C.byref(fl))
+        e1.record(stream)
+        e1.synchronize()
+        rates.append(fl.value / (e0.elapsed_time(e1) * 1e-3))
+    c = clk.stop()
+    mhz = c.get("sm_mhz")
+    return {"measured_tflops": max(rates) / 1e12, "median_tflops": statistics.median(rates) / 1e12,
+            "launches": len(rates), "sm_mhz_median": mhz, "clock_samples": c.get("samples"),
+            "reasons": c.get("reasons"), "sms": sms,
+            "clock_peak_tflops": sms * 128 * 2 * mhz * 1e6 / 1e12 if mhz else None,
+            "kernel": "bench_probe_fma (libuww_bench_probe.so)"}
+
+
+def leg_host_link(stream, dev, sms, nbytes, steps=20):
+    """Device-to-host bandwidth for one step's output size: a pinned
+    cudaMemcpyAsync (copy engine) and SM stores into the same pinned buffer
+    (how the streamed host output of the batched build moves)."""
+    import torch
+    PL = probe_lib()
+    nbytes = (nbytes + 15) // 16 * 16
+    d = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+    h = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    hs = C.c_void_p(stream.cuda_stream)
+
+    def ce():
+        h.copy_(d, non_blocking=True)
+
+    def sm():
+        assert PL.bench_probe_host_write(C.c_void_p(d.data_ptr()), C.c_void_p(h.data_ptr()), nbytes, sms * 4, hs) == 0
+
+    res = {"bytes": nbytes}
+    for name, fn in (("copy_engine_gbs", ce), ("sm_store_gbs", sm)):
+        for _ in range(3):
+            fn()
+        t = statistics.median([timed(stream, fn) for _ in range(steps)])
+        res[name] = nbytes / t / 1e9
+    return res
+
+
+def leg_no_shortcut(ctx, L, d_desc, n, out, out_t, params, flush, stream, steps, tuning):
+    """The batched build with the depth-bias shortcut off
+    (UWW_TUNE_NO_DEPTH_SHORTCUT): every chunk evaluates its noise, as every
+    chunk of the reference samples its grid before the blank check
+    (chunk.rs:131-133).  Same output; its per-chunk cost and FP32 roofline."""
+    from underwaterworld_gb300 import abi
+    ctx.set_tuning(*tuning, options=abi.UWW_TUNE_NO_DEPTH_SHORTCUT)
+    ts, vs = [], []
+    for i in range(steps + 3):
+        ctx.set_params(params[i % N_SEEDS])
+
+        def run():
+            abi.check(L.uww_build_chunks(ctx.h, C.c_void_p(d_desc.data_ptr()), n, 12, C.byref(out)), "build")
+
+        t = timed(stream, run, flush)
+        tot = out_t["totals"].cpu().numpy()
+        assert int(tot[2]) == 0 and int(tot[3]) == 0, tot
+        if i >= 3:
+            ts.append(t)
+            vs.append(int(tot[0]))
+    ctx.set_tuning(*tuning, options=0)
+    mean = statistics.mean(ts)
+    K = params[0].octaves
+    flops = n * 13 ** 3 * (K * FLOPS_PER_OCTAVE + FLOPS_PER_SAMPLE_EXTRA) + \
+        statistics.mean(vs) * (K * FLOPS_PER_OCTAVE_GRAD + FLOPS_PER_VERTEX_EXTRA)
+    return {"chunks_per_s": n / mean, "us_per_step": mean * 1e6, "steps": steps, "flops_per_step": flops,
+            "tflops": flops / mean / 1e12}
+
+
+def leg_fast_vs_f64(params, descs, seeds):
+    """Accuracy of the fast build (the one `value` times) against the F64
+    oracle -- the reference's f64 noise (perlin_util.rs:6-29) -- on the whole
+    grid for each seed, outside every timed region: flipped cells (case
+    indices that differ) and the vertex position error over the chunks with
+    identical index buffers."""
+    from oracle import oracle as O
+    from underwaterworld_gb300 import abi
+    from underwaterworld_gb300.chunk import Context
+    rows = []
+    for seed in seeds:
+        p = params[seed % len(params)].copy()
+        p.outputs = abi.UWW_OUT_CASES
+        p.math_mode = abi.UWW_MATH_FAST
+        ref_p = p.copy()
+        ref_p.math_mode = abi.UWW_MATH_EXACT
+        ref = O.build_chunks(ref_p, descs, precision=O.F64, threads=os.cpu_count() or 1)
+        with Context(p) as c:
+            got = c.build_chunks_device(descs, int(ref.totals[0]) + 4096, int(ref.totals[1]) + 16384)
+        assert got.status == abi.UWW_OK, got.status
+        rows.append(O.fast_vs_reference(got, ref))
+    return {"seeds": list(seeds), "cells": sum(r["cells"] for r in rows),
+            "flipped_cells": sum(r["flipped_cells"] for r in rows),
+            "max_vertex_err": max(r["max_vertex_err"] for r in rows),
+            "median_vertex_err": float(np.median([r["median_vertex_err"] for r in rows])),
+            "vertices_compared": sum(r["vertices_compared"] for r in rows),
+            "unit": "world units (a cell is 16/12)", "oracle": "F64 CPU oracle (reference semantics)"}
 
 
 def leg_noise_stage(ctx, stream, flush, params, descs, steps, warmup):
@@ -599,6 +745,7 @@ def main():
     # ---- timed batched steps ----
     clocks = ClockSampler(local)
     clocks.start()
+    t_window = time.perf_counter()
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
@@ -612,12 +759,28 @@ def main():
         e1.synchronize()
         times.append(e0.elapsed_time(e1) * 1e-3)
         tot = out_t["totals"].cpu().numpy()
+        # a step that overflowed or timed out is not counted as built
+        assert int(tot[2]) == 0 and int(tot[3]) == 0, ("timed step", i, tot)
         verts_sum += int(tot[0])
         inds_sum += int(tot[1])
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
+    # the timed steps of a short run end before nvidia-smi's first samples:
+    # keep running the same step, untimed, until the sampler has watched it
+    # for CLOCK_WINDOW_S
+    extra_steps = 0
+    while time.perf_counter() - t_window < CLOCK_WINDOW_S:
+        flush.zero_()
+        step(args.steps + extra_steps)
+        extra_steps += 1
+        if extra_steps % 16 == 0:
+            torch.cuda.synchronize()
+    torch.cuda.synchronize()
     clk = clocks.stop()
+    clk["window_s"] = round(time.perf_counter() - t_window, 2)
+    clk["note"] = (f"sampled every 100 ms over the {args.steps} timed steps and {extra_steps} more untimed steps "
+                   f"of the same build")
     t_total = sum(times)
     if world > 1:
         tt = torch.tensor([t_total], device=dev, dtype=torch.float64)
@@ -641,6 +804,8 @@ def main():
             e1.record(stream)
             e1.synchronize()
             ex_times.append(e0.elapsed_time(e1) * 1e-3)
+            tot = out_t["totals"].cpu().numpy()
+            assert int(tot[2]) == 0 and int(tot[3]) == 0, ("exact step", i, tot)
         extra["exact_chunks_per_s"] = n / statistics.mean(ex_times)
 
         # ---- plain: one launch per chunk, each into its own slot ----
@@ -703,7 +868,12 @@ def main():
             extra["queries"] = leg_queries(stream, flush, max(5, min(args.steps, 50)))
         else:
             extra["terrain_fit"] = leg_terrain_fit(stream, args.fit_steps)
+    tuning = (args.threads, args.bps)
     if not args.quick:
+        extra["no_depth_shortcut"] = leg_no_shortcut(ctx, L, d_desc, n, out, out_t, params, flush, stream,
+                                                     max(5, min(args.steps, 200)), tuning)
+        extra["host_link"] = leg_host_link(stream, dev, torch.cuda.get_device_properties(dev).multi_processor_count,
+                                           extra["e2e"]["d2h_bytes_per_step"])
         extra["frame_graph"] = leg_frame_graph(ctx, params[0], descs, max(5, min(args.steps, 50)), 3)
         extra["mixed_lod"] = leg_mixed_lod(stream, flush, max(10, min(args.steps, 200)), 3)
         extra["adjoint"] = leg_adjoint(stream, flush, max(5, min(args.steps, 50)), 3)
@@ -712,20 +882,10 @@ def main():
             extra["terrain_fit"] = leg_terrain_fit(stream, args.fit_steps)
 
     # ---- FP32 peak probe (roofline denominator) ----
-    sink = torch.empty(152 * 8 * 256, dtype=torch.float32, device=dev)
-    fl = C.c_double()
-    for _ in range(2):
-        L.uww_probe_fma(ctx.h, 152 * 8, 4096, C.c_void_p(sink.data_ptr()), C.byref(fl))
-    torch.cuda.synchronize()
-    pk = []
-    for _ in range(5):
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        L.uww_probe_fma(ctx.h, 152 * 8, 4096, C.c_void_p(sink.data_ptr()), C.byref(fl))
-        e1.record(stream)
-        e1.synchronize()
-        pk.append(fl.value / (e0.elapsed_time(e1) * 1e-3))
-    fp32_peak = max(pk) / 1e12
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    peak = leg_fp32_peak(stream, dev, sms, local)
+    fp32_peak = peak["measured_tflops"]
+    extra["fp32_peak"] = peak
 
     # the noise flops the build performs: chunks decided by the depth bias
     # alone evaluate none
@@ -750,19 +910,20 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded chunk grid; seeds 0-9 cycle per step)",
-        "config": {**config_dict(n, "fast (FMA), persistent grid + device work queue + decoupled look-back, "
-                                    "chunks the depth bias decides settled without their noise, "
-                                    "then the per-vertex colour/normal pass"),
-                   "mean_verts_per_step": mean_v, "mean_inds_per_step": mean_i,
-                   "chunks_decided_by_depth_bias": decided},
+        "config": config_dict(n),
+        "build": "fast (FMA), persistent grid + device work queue + decoupled look-back, chunks the depth bias "
+                 "decides settled without their noise, then the per-vertex colour/normal pass",
+        "mean_verts_per_step": mean_v, "mean_inds_per_step": mean_i, "chunks_decided_by_depth_bias": decided,
         "mvoxels_per_s": value * 12 ** 3 / 1e6,
         "msamples_per_s": value * 13 ** 3 / 1e6,
         "gpu_launches": args.steps * (2 if params[0].outputs & (abi.UWW_OUT_COLOR | abi.UWW_OUT_NORMALS) else 1),
         "clocks": clk,
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": achieved / fp32_peak, "traffic": NCU_DRAM_BYTES_PER_LAUNCH,
-                     "peak_source": "measured live: FMA probe kernel (uww_probe_fma), 152x8 CTAs "
-                                    "(no FP32 entry in the measured-peaks file)",
+                     "peak_source": f"measured live: FMA probe kernel, {sms}x8 CTAs, at a median "
+                                    f"{peak['sm_mhz_median']} MHz (SMs x 128 x 2 x clock = "
+                                    f"{peak['clock_peak_tflops']} TFLOP/s); the measured-peaks file has no FP32 entry",
+                     "traffic_source": NCU_TRAFFIC_SOURCE,
                      "flops_per_step": flops,
                      "emission": {"bound": "hbm", "achieved": out_bytes / (t_total / args.steps) / 1e9,
                                   "peak": hbm_peak, "unit": "GB/s",
@@ -783,6 +944,12 @@ def main():
     if "plain_chunks_per_s" in extra:
         line["batched_over_plain"] = value / world / extra["plain_chunks_per_s"]
 
+    nsc = extra.get("no_depth_shortcut")
+    if nsc:
+        nsc["frac_of_fp32_peak"] = nsc["tflops"] / fp32_peak
+    if rank == 0 and not args.quick:
+        # accuracy of the fast build against the f64 oracle, outside the timed region
+        line["fast_vs_f64"] = leg_fast_vs_f64(params, descs, range(N_SEEDS))
     if rank == 0 and not args.no_cpu and not args.quick:
         cv, cn, cel = cpu_reference(descs, list(range(N_SEEDS)), 1, budget_s=12.0)
         line["cpu_baseline"] = {"value": cv, "unit": UNIT, "cores": 1, "kind": "port",

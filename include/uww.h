@@ -25,7 +25,7 @@
 extern "C" {
 #endif
 
-#define UWW_ABI_VERSION 2
+#define UWW_ABI_VERSION 3
 
 /* ---- status codes --------------------------------------------------------- */
 #define UWW_OK               0
@@ -197,8 +197,12 @@ int uww_build_chunks(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n,
  * Every call shares that array and clears the part it uses first, so calls
  * that overlap on the GPU race: serialise them.  The first call on a device
  * looks up the array's address and sets kernel attributes; make it before any
- * stream capture.  Otherwise as uww_build_chunks, asynchronous on `stream`
- * (a cudaStream_t, NULL for the legacy default stream). */
+ * stream capture.  That set-up is kept for the life of the process, so a
+ * cudaDeviceReset() of the device afterwards is not supported.  out->totals
+ * is required (UWW_ERR_INVALID_ARG without it): its four words are the only
+ * report of a timed-out wait, a bad descriptor or an overflow.  Otherwise as
+ * uww_build_chunks, asynchronous on `stream` (a cudaStream_t, NULL for the
+ * legacy default stream). */
 int uww_build_chunks_noalloc(const uww_params* p, void* stream, const uww_chunk_desc* d_chunks, uint32_t n,
                              uint32_t max_cells, const uww_mesh_out* out);
 
@@ -232,8 +236,30 @@ typedef struct uww_tuning {
     int32_t blocks_per_sm;  /* resident CTAs per SM of the persistent grid                   */
     int32_t smem_cells;     /* chunks up to this many cells per edge work in shared memory;
                                larger ones use a global scratch slot per CTA                */
-    int32_t reserved;
-} uww_tuning;
+    int32_t spin_limit;     /* bound, in SM clock cycles, on each device-side wait of the
+                               batched build (the prefix-sum look-back); 0 = the default,
+                               4e9 cycles (about 2 s).  A wait that runs out raises
+                               UWW_ERRFLAG_TIMEOUT and the build finishes without it      */
+    uint32_t test_flags;    /* UWW_TEST_*: failure injection for tests; 0 in normal use      */
+    uint32_t options;       /* UWW_TUNE_*; 0 in normal use                                   */
+    int32_t reserved[2];
+} uww_tuning;               /* 32 bytes */
+
+/* uww_tuning.options.  NO_DEPTH_SHORTCUT: evaluate the noise of every chunk,
+ * also of the chunks whose depth bias alone decides every sample (the
+ * output does not change; for measuring the per-chunk cost of the full
+ * path). */
+#define UWW_TUNE_NO_DEPTH_SHORTCUT 1u
+
+/* Failure injection (uww_tuning.test_flags).  WITHHOLD_FIRST: the first chunk
+ * of every batched build never publishes its prefix, so the look-back waits
+ * of the chunks after it run out (after spin_limit cycles each): the build
+ * returns with UWW_ERRFLAG_TIMEOUT, every chunk after the first flagged
+ * UWW_CHUNK_OVERFLOW and nothing written outside the output capacities.  It
+ * lets a test check the timeout path without a fault or a hang. */
+#define UWW_TEST_WITHHOLD_FIRST 1u
+/* The autotuner sets threads, blocks_per_sm and smem_cells and keeps the
+ * context's spin_limit and test_flags. */
 int uww_ctx_set_tuning(uww_ctx* ctx, const uww_tuning* t);
 int uww_ctx_get_tuning(const uww_ctx* ctx, uww_tuning* t);
 
@@ -431,14 +457,6 @@ int uww_shade_vertices(uww_ctx* ctx, const uww_camera_uniform* cam, const uww_ve
 /* density(world xyz) for n points: perlin_util::iso_at (perlin_util.rs:24-29) with
  * (x,y,z) = world / CHUNK_SIZE as in boid.rs:132-137.  d_xyz: 3n floats; d_out: n. */
 int uww_density_at(uww_ctx* ctx, const float* d_xyz, uint32_t n, float* d_out);
-
-/* ---- diagnostics --------------------------------------------------------------- */
-/* FP32 roofline probe: launches `blocks` CTAs of 256 threads, each running
- * iters*128 independent FMAs, on the context stream; *flops receives the flop
- * count (2 per FMA) so that flops / elapsed time is the achievable FP32 rate.
- * d_sink: blocks*256 floats.  No counterpart in the reference (used to state
- * the FP32 peak the noise stage is measured against). */
-int uww_probe_fma(uww_ctx* ctx, uint32_t blocks, uint32_t iters, float* d_sink, double* flops);
 
 #ifdef __cplusplus
 }

@@ -13,8 +13,9 @@ from pathlib import Path
 
 import numpy as np
 
-from underwaterworld_gb300 import abi
-from underwaterworld_gb300.chunk import MeshBatch, total_cells, total_samples
+# struct layouts only: importing them never loads the GPU library
+from underwaterworld_gb300 import layout
+from underwaterworld_gb300.layout import MeshBatch, total_cells, total_samples
 
 HERE = Path(__file__).resolve().parent
 LIB_PATH = HERE / "_build" / "liboracle.so"
@@ -40,26 +41,26 @@ def lib():
         P = C.c_void_p
         L.oracle_perm.argtypes = [C.c_uint32, P]
         L.oracle_perm.restype = None
-        L.oracle_build_chunks.argtypes = [C.POINTER(abi.Params), C.c_int, C.c_int, P, C.c_uint32,
-                                          C.POINTER(abi.MeshOut), C.c_int, P, C.c_uint64]
+        L.oracle_build_chunks.argtypes = [C.POINTER(layout.Params), C.c_int, C.c_int, P, C.c_uint32,
+                                          C.POINTER(layout.MeshOut), C.c_int, P, C.c_uint64]
         L.oracle_build_chunks.restype = C.c_int
-        L.oracle_sample_grid.argtypes = [C.POINTER(abi.Params), C.c_int, P, P]
+        L.oracle_sample_grid.argtypes = [C.POINTER(layout.Params), C.c_int, P, P]
         L.oracle_sample_grid.restype = C.c_int
-        L.oracle_density_at.argtypes = [C.POINTER(abi.Params), C.c_int, P, C.c_uint32, P, P]
+        L.oracle_density_at.argtypes = [C.POINTER(layout.Params), C.c_int, P, C.c_uint32, P, P]
         L.oracle_density_at.restype = C.c_int
         L.oracle_perlin.argtypes = [C.c_uint32, C.c_int, P, C.c_uint32, P]
         L.oracle_perlin.restype = C.c_int
-        L.oracle_adjoint64.argtypes = [C.POINTER(abi.Params), P, P, C.c_uint32, P, P, P, P, P, P, P, P, P, P]
+        L.oracle_adjoint64.argtypes = [C.POINTER(layout.Params), P, P, C.c_uint32, P, P, P, P, P, P, P, P, P, P]
         L.oracle_adjoint64.restype = C.c_int
         L.oracle_cell_tri_offsets.argtypes = [P, C.c_uint32, P, P]
         L.oracle_cell_tri_offsets.restype = C.c_int
-        L.oracle_ray_query.argtypes = [C.POINTER(abi.Params), P, C.c_uint32, P, P, P, P, P, C.c_uint32, P,
+        L.oracle_ray_query.argtypes = [C.POINTER(layout.Params), P, C.c_uint32, P, P, P, P, P, C.c_uint32, P,
                                        C.c_uint32, C.c_int32, P]
         L.oracle_ray_query.restype = C.c_int
-        L.oracle_schedule_chunks.argtypes = [C.POINTER(abi.Params), C.POINTER(abi.ScheduleParams), P, P, C.c_uint32,
+        L.oracle_schedule_chunks.argtypes = [C.POINTER(layout.Params), C.POINTER(layout.ScheduleParams), P, P, C.c_uint32,
                                              P, C.c_uint32, P, C.c_uint32, P]
         L.oracle_schedule_chunks.restype = C.c_int
-        L.oracle_shade_vertices.argtypes = [C.POINTER(abi.CameraUniform), P, C.c_uint32, P, P, P]
+        L.oracle_shade_vertices.argtypes = [C.POINTER(layout.CameraUniform), P, C.c_uint32, P, P, P]
         L.oracle_shade_vertices.restype = C.c_int
         _lib = L
     return _lib
@@ -71,39 +72,39 @@ def perm(seed: int) -> bytes:
     return bytes(buf)
 
 
-def build_chunks(params: abi.Params, descs: np.ndarray, precision: int = F32, search: int = SEARCH_HASHED,
+def build_chunks(params: layout.Params, descs: np.ndarray, precision: int = F32, search: int = SEARCH_HASHED,
                  threads: int = 1, samples_in: np.ndarray | None = None, vert_capacity: int | None = None,
                  ind_capacity: int | None = None) -> MeshBatch:
-    descs = np.ascontiguousarray(descs, dtype=abi.CHUNK_DESC_DTYPE)
+    descs = np.ascontiguousarray(descs, dtype=layout.CHUNK_DESC_DTYPE)
     n = descs.shape[0]
     nc, ns = total_cells(descs), total_samples(descs)
     vcap = vert_capacity if vert_capacity is not None else 15 * nc
     icap = ind_capacity if ind_capacity is not None else 15 * nc
-    records = np.zeros(n, dtype=abi.CHUNK_RECORD_DTYPE)
-    verts = np.empty(vcap, dtype=abi.VERT_COLOR_DTYPE)
-    normals = np.empty((vcap, 3), dtype=np.float32) if params.outputs & abi.UWW_OUT_NORMALS else None
+    records = np.zeros(n, dtype=layout.CHUNK_RECORD_DTYPE)
+    verts = np.empty(vcap, dtype=layout.VERT_COLOR_DTYPE)
+    normals = np.empty((vcap, 3), dtype=np.float32) if params.outputs & layout.UWW_OUT_NORMALS else None
     inds = np.empty(icap, dtype=np.uint32)
-    cases = np.zeros(nc, dtype=np.uint8) if params.outputs & abi.UWW_OUT_CASES else None
-    samples = np.zeros(ns, dtype=np.float32) if params.outputs & abi.UWW_OUT_SAMPLES else None
+    cases = np.zeros(nc, dtype=np.uint8) if params.outputs & layout.UWW_OUT_CASES else None
+    samples = np.zeros(ns, dtype=np.float32) if params.outputs & layout.UWW_OUT_SAMPLES else None
     totals = np.zeros(4, dtype=np.uint64)
 
     def ptr(a):
         return a.ctypes.data if a is not None else None
 
-    out = abi.MeshOut(ptr(verts), ptr(normals), ptr(inds), ptr(cases), ptr(samples), ptr(records), ptr(totals),
+    out = layout.MeshOut(ptr(verts), ptr(normals), ptr(inds), ptr(cases), ptr(samples), ptr(records), ptr(totals),
                       vcap, icap, cases.size if cases is not None else 0, samples.size if samples is not None else 0)
     sin = np.ascontiguousarray(samples_in, dtype=np.float32) if samples_in is not None else None
     st = lib().oracle_build_chunks(C.byref(params), precision, search, descs.ctypes.data_as(C.c_void_p), n,
                                    C.byref(out), threads, ptr(sin), sin.size if sin is not None else 0)
-    if st not in (abi.UWW_OK, abi.UWW_ERR_CAPACITY):
+    if st not in (layout.UWW_OK, layout.UWW_ERR_CAPACITY):
         raise RuntimeError(f"oracle_build_chunks failed: {st}")
     nv, ni = min(int(totals[0]), vcap), min(int(totals[1]), icap)
     return MeshBatch(records, verts[:nv].copy(), normals[:nv].copy() if normals is not None else None,
                      inds[:ni].copy(), cases, totals, st, samples)
 
 
-def sample_grid(params: abi.Params, desc, precision: int = F32) -> np.ndarray:
-    d = np.ascontiguousarray(np.asarray(desc, dtype=abi.CHUNK_DESC_DTYPE).reshape(1))
+def sample_grid(params: layout.Params, desc, precision: int = F32) -> np.ndarray:
+    d = np.ascontiguousarray(np.asarray(desc, dtype=layout.CHUNK_DESC_DTYPE).reshape(1))
     S = int(d["cells"][0]) + 1
     out = np.zeros(S ** 3, dtype=np.float32)
     st = lib().oracle_sample_grid(C.byref(params), precision, d.ctypes.data_as(C.c_void_p),
@@ -113,7 +114,7 @@ def sample_grid(params: abi.Params, desc, precision: int = F32) -> np.ndarray:
     return out
 
 
-def density_at(params: abi.Params, xyz: np.ndarray, precision: int = F32, grad: bool = False):
+def density_at(params: layout.Params, xyz: np.ndarray, precision: int = F32, grad: bool = False):
     xyz = np.ascontiguousarray(xyz, dtype=np.float32).reshape(-1, 3)
     n = xyz.shape[0]
     out = np.zeros(n, dtype=np.float32)
@@ -134,7 +135,7 @@ def perlin(seed: int, xyz: np.ndarray, precision: int = F64) -> np.ndarray:
 
 
 # ---- topology-frozen adjoint (FP64 reference) ---------------------------------
-def theta_of(params: abi.Params) -> np.ndarray:
+def theta_of(params: layout.Params) -> np.ndarray:
     """theta = (effective per-octave amplitudes, base_freq, offset xyz, iso) in f64."""
     K = int(params.octaves)
     amps, a = [], np.float32(params.amplitude)
@@ -144,13 +145,13 @@ def theta_of(params: abi.Params) -> np.ndarray:
     return np.array(amps + [params.base_freq, *params.offset, params.iso_level], dtype=np.float64)
 
 
-def adjoint64(params: abi.Params, descs: np.ndarray, records: np.ndarray, edge_ids: np.ndarray,
+def adjoint64(params: layout.Params, descs: np.ndarray, records: np.ndarray, edge_ids: np.ndarray,
               pos_grad: np.ndarray, theta: np.ndarray | None = None, samples_in: np.ndarray | None = None,
               want_theta: bool = True, want_samples: bool = False, want_positions: bool = False,
               want_dmax: bool = False, want_pole: bool = False) -> dict:
     """FP64 loss sum_v pos_grad[v] . p_v over the given edges, and its gradients."""
-    descs = np.ascontiguousarray(descs, dtype=abi.CHUNK_DESC_DTYPE)
-    records = np.ascontiguousarray(records, dtype=abi.CHUNK_RECORD_DTYPE)
+    descs = np.ascontiguousarray(descs, dtype=layout.CHUNK_DESC_DTYPE)
+    records = np.ascontiguousarray(records, dtype=layout.CHUNK_RECORD_DTYPE)
     edge_ids = np.ascontiguousarray(edge_ids, dtype=np.uint32)
     pos_grad = np.ascontiguousarray(pos_grad, dtype=np.float32).reshape(-1, 3)
     K = int(params.octaves)
@@ -174,7 +175,7 @@ def adjoint64(params: abi.Params, descs: np.ndarray, records: np.ndarray, edge_i
     return {"loss": loss.value, "theta_grad": tg, "sample_grad": sg, "positions": pos, "dmax": dmax, "pole": pole}
 
 
-def fd_theta(params: abi.Params, descs, records, edge_ids, pos_grad, h: float = 1e-4, theta=None,
+def fd_theta(params: layout.Params, descs, records, edge_ids, pos_grad, h: float = 1e-4, theta=None,
              richardson: bool = False, pole_frac: float = 0.02) -> tuple:
     """FP64 central differences of the loss in theta.  The step of parameter i
     is h in units of its effect on the density: h / max|d rho/d theta_i| over
@@ -206,13 +207,13 @@ def fd_theta(params: abi.Params, descs, records, edge_ids, pos_grad, h: float = 
     return fd, steps
 
 
-def crossing_edges(params: abi.Params, descs: np.ndarray, samples: np.ndarray):
+def crossing_edges(params: layout.Params, descs: np.ndarray, samples: np.ndarray):
     """Every grid edge whose two samples lie on opposite sides of the iso-level
     (one vertex per edge), as records + edge ids in the forward's encoding:
     id = (sample index << 3) | dir, from the lower sample in direction +axis."""
-    descs = np.ascontiguousarray(descs, dtype=abi.CHUNK_DESC_DTYPE)
+    descs = np.ascontiguousarray(descs, dtype=layout.CHUNK_DESC_DTYPE)
     iso = np.float32(params.iso_level)
-    recs = np.zeros(descs.shape[0], dtype=abi.CHUNK_RECORD_DTYPE)
+    recs = np.zeros(descs.shape[0], dtype=layout.CHUNK_RECORD_DTYPE)
     ids, off = [], 0
     for i, d in enumerate(descs):
         S = int(d["cells"]) + 1
@@ -230,7 +231,7 @@ def crossing_edges(params: abi.Params, descs: np.ndarray, samples: np.ndarray):
         e = np.concatenate(mine).astype(np.uint32)
         recs[i]["num_verts"] = e.size
         recs[i]["vert_offset"] = off
-        recs[i]["flags"] = abi.UWW_CHUNK_HAS_MESH if e.size else 0
+        recs[i]["flags"] = layout.UWW_CHUNK_HAS_MESH if e.size else 0
         ids.append(e)
         off += e.size
     return recs, (np.concatenate(ids) if ids else np.zeros(0, np.uint32))
@@ -238,16 +239,16 @@ def crossing_edges(params: abi.Params, descs: np.ndarray, samples: np.ndarray):
 
 # ---- queries against built chunks ------------------------------------------------
 def cell_tri_offsets(descs: np.ndarray, cases: np.ndarray) -> np.ndarray:
-    descs = np.ascontiguousarray(descs, dtype=abi.CHUNK_DESC_DTYPE)
+    descs = np.ascontiguousarray(descs, dtype=layout.CHUNK_DESC_DTYPE)
     cases = np.ascontiguousarray(cases, dtype=np.uint8)
     first = np.zeros(cases.size, np.uint32)
     lib().oracle_cell_tri_offsets(descs.ctypes.data, descs.shape[0], cases.ctypes.data, first.ctypes.data)
     return first
 
 
-def ray_query(params: abi.Params, descs, batch: MeshBatch, origins: np.ndarray, dirs: np.ndarray, rng: int):
+def ray_query(params: layout.Params, descs, batch: MeshBatch, origins: np.ndarray, dirs: np.ndarray, rng: int):
     """Nearest hit per (query, ray) against the triangles around each query point."""
-    descs = np.ascontiguousarray(descs, dtype=abi.CHUNK_DESC_DTYPE)
+    descs = np.ascontiguousarray(descs, dtype=layout.CHUNK_DESC_DTYPE)
     origins = np.ascontiguousarray(origins, dtype=np.float32).reshape(-1, 3)
     nq = origins.shape[0]
     dirs = np.ascontiguousarray(dirs, dtype=np.float32).reshape(nq, -1, 3)
@@ -265,13 +266,13 @@ def ray_query(params: abi.Params, descs, batch: MeshBatch, origins: np.ndarray, 
     return out
 
 
-def schedule_chunks(params: abi.Params, sp, known_descs=None, known_records=None, cap: int = 4096):
+def schedule_chunks(params: layout.Params, sp, known_descs=None, known_records=None, cap: int = 4096):
     """World::update_nearby: (generation list descriptors in GenPrio order, render list (m, 3))."""
     n_known = 0 if known_descs is None else len(known_descs)
-    kd = np.ascontiguousarray(known_descs if n_known else np.zeros(1, abi.CHUNK_DESC_DTYPE), dtype=abi.CHUNK_DESC_DTYPE)
-    kr = np.ascontiguousarray(known_records if n_known else np.zeros(1, abi.CHUNK_RECORD_DTYPE),
-                              dtype=abi.CHUNK_RECORD_DTYPE)
-    gen = np.zeros(cap, abi.CHUNK_DESC_DTYPE)
+    kd = np.ascontiguousarray(known_descs if n_known else np.zeros(1, layout.CHUNK_DESC_DTYPE), dtype=layout.CHUNK_DESC_DTYPE)
+    kr = np.ascontiguousarray(known_records if n_known else np.zeros(1, layout.CHUNK_RECORD_DTYPE),
+                              dtype=layout.CHUNK_RECORD_DTYPE)
+    gen = np.zeros(cap, layout.CHUNK_DESC_DTYPE)
     ren = np.zeros((cap, 3), np.int32)
     counts = np.zeros(2, np.uint32)
     st = lib().oracle_schedule_chunks(C.byref(params), C.byref(sp), kd.ctypes.data, kr.ctypes.data, n_known,
@@ -283,8 +284,31 @@ def schedule_chunks(params: abi.Params, sp, known_descs=None, known_records=None
 
 def shade_vertices(cam, verts: np.ndarray):
     """terrain.wgsl at each vertex: (clip (V, 4), rgb (V, 3), dist_light (V, 2))."""
-    verts = np.ascontiguousarray(verts, dtype=abi.VERT_COLOR_DTYPE)
+    verts = np.ascontiguousarray(verts, dtype=layout.VERT_COLOR_DTYPE)
     nv = verts.shape[0]
     clip, rgb, dl = np.zeros((nv, 4), np.float32), np.zeros((nv, 3), np.float32), np.zeros((nv, 2), np.float32)
     lib().oracle_shade_vertices(C.byref(cam), verts.ctypes.data, nv, clip.ctypes.data, rgb.ctypes.data, dl.ctypes.data)
     return clip, rgb, dl
+
+
+# ---- accuracy of a GPU build against an oracle build of the same chunks -----------
+def fast_vs_reference(got: MeshBatch, ref: MeshBatch) -> dict:
+    """Flipped cells (case indices that differ; both builds need per-cell cases)
+    and the vertex position error over the chunks whose index buffers are
+    identical (same topology, so vertices correspond one to one), in world
+    units: max and median over vertices of the largest coordinate error."""
+    flipped = int(np.count_nonzero(got.cases != ref.cases))
+    errs = []
+    same = got.records["num_inds"] == ref.records["num_inds"]
+    compared = 0
+    for i in np.nonzero(same & (ref.records["num_inds"] > 0))[0]:
+        gv, _, gi = got.chunk(i)
+        rv, _, ri = ref.chunk(i)
+        if np.array_equal(gi, ri):
+            errs.append(np.abs(gv["pos"].astype(np.float64) - rv["pos"].astype(np.float64)).max(axis=1))
+            compared += 1
+    e = np.concatenate(errs) if errs else np.zeros(1)
+    meshed = int((ref.records["num_inds"] > 0).sum())
+    return {"cells": int(ref.cases.size), "flipped_cells": flipped, "max_vertex_err": float(e.max()),
+            "median_vertex_err": float(np.median(e)), "vertices_compared": int(e.size if errs else 0),
+            "meshed_chunks": meshed, "chunks_same_topology": compared}

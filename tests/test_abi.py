@@ -21,7 +21,7 @@ def test_library_exports_every_declared_symbol(built_lib):
 
 
 def test_abi_version_and_status_strings(built_lib):
-    assert abi.lib().uww_abi_version() == 2
+    assert abi.lib().uww_abi_version() == 3
     assert abi.status_string(abi.UWW_ERR_CAPACITY) == "output capacity exceeded"
 
 
@@ -40,6 +40,13 @@ def test_reference_params(built_lib):
     assert p.bias_mode == abi.UWW_BIAS_TERRACED and (p.bias_a, p.bias_b, p.bias_c) == (16.0, 32.0, 0.25)
     assert p.iso_level == np.float32(-0.1)
     assert (p.color_min_z, p.color_max_z) == (-2.0, 2.0)
+
+
+def test_python_reference_params_equal_the_librarys(built_lib):
+    """layout.reference_params() (what the oracle and the benchmark's reference
+    arm use without loading the library) is byte for byte uww_params_reference()."""
+    from underwaterworld_gb300 import layout
+    assert bytes(layout.reference_params()) == bytes(abi.reference_params())
 
 
 def test_layout_cells(built_lib):

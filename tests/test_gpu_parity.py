@@ -420,6 +420,22 @@ def test_depth_bias_bound_decides_far_chunks(ctx_factory, oracle, bias):
     np.testing.assert_array_equal(with_samples.samples, want)
 
 
+def test_depth_shortcut_off_gives_the_same_output(ctx_factory, oracle):
+    """UWW_TUNE_NO_DEPTH_SHORTCUT evaluates the noise of every chunk, also of
+    those the depth bias decides; the output is the same bit for bit."""
+    p, d = workloads.uniform_grid(seed=1, outputs=abi.UWW_OUT_COLOR | abi.UWW_OUT_NORMALS)
+    ref = oracle.build_chunks(p, d)
+    ctx = ctx_factory(p)
+    on = ctx.build_chunks_device(d, *caps(ref))
+    ctx.set_tuning(options=abi.UWW_TUNE_NO_DEPTH_SHORTCUT)
+    off = ctx.build_chunks_device(d, *caps(ref))
+    ctx.set_tuning(options=0)
+    assert_batches_equal(off, ref)
+    assert_batches_equal(on, off)
+    np.testing.assert_array_equal(on.verts, off.verts)
+    np.testing.assert_array_equal(on.normals, off.normals)
+
+
 def test_long_runs_of_bias_decided_chunks(ctx_factory, oracle):
     """A tall column of chunks, nearly all far above or below the surface:
     control warps run through long runs of depth-bias-decided tickets, more

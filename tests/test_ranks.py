@@ -61,6 +61,7 @@ def test_reference_arm_runs_on_rank_zero_only(built_lib, oracle, monkeypatch, ca
     sys.path.insert(0, str(ROOT))
     import bench
     monkeypatch.setattr(bench, "REF_BUDGET_S", 0.5)
+    monkeypatch.setattr(bench, "REF_ONE_THREAD_S", 0.2)
     args = argparse.Namespace(steps=7, warmup=3)
     monkeypatch.setenv("WORLD_SIZE", "2")
     monkeypatch.setenv("RANK", "1")
@@ -74,4 +75,37 @@ def test_reference_arm_runs_on_rank_zero_only(built_lib, oracle, monkeypatch, ca
     assert d["impl"] == "reference" and d["steps"] == 7 and d["warmup"] == 3 and d["n_gpus"] == 2
     assert d["value"] > 0 and d["unit"] == bench.UNIT and d["metric"] == bench.METRIC
     assert d["cpu_baseline"]["value"] == d["value"] and d["e2e"]["h2d_bytes_per_step"] == 0
-    assert 32 <= d["config"]["chunks_per_timed_step"] <= 4096
+    assert 32 <= d["chunks_per_timed_step"] <= 4096
+    assert d["threads"] >= 1 and d["single_thread"]["cores"] == 1 and d["single_thread"]["value"] > 0
+    assert d["config"]["chunks_per_step"] == 4096
+
+
+def _reference_arm_maps(q):
+    """In a fresh process: run the reference arm briefly, then report which
+    shared objects of this repository the process has mapped."""
+    import argparse
+    import io
+    from contextlib import redirect_stdout
+    sys.path.insert(0, str(ROOT))
+    os.environ.update(RANK="0", WORLD_SIZE="1")
+    import bench
+    bench.REF_BUDGET_S, bench.REF_ONE_THREAD_S = 0.3, 0.1
+    with redirect_stdout(io.StringIO()):
+        bench.run_reference(argparse.Namespace(steps=2, warmup=1))
+    maps = Path("/proc/self/maps").read_text()
+    q.put(sorted({line.split()[-1] for line in maps.splitlines() if line.endswith(".so") and str(ROOT) in line}))
+
+
+def test_reference_arm_does_not_load_the_gpu_library(built_lib, oracle):
+    """The reference arm runs the oracle only: libuww_gb300.so is never mapped
+    into its process (its parameters and struct layouts come from
+    underwaterworld_gb300.layout)."""
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    pr = ctx.Process(target=_reference_arm_maps, args=(q,))
+    pr.start()
+    mapped = q.get(timeout=300)
+    pr.join(timeout=60)
+    assert pr.exitcode == 0
+    assert any(m.endswith("liboracle.so") for m in mapped), mapped
+    assert not any("libuww" in Path(m).name for m in mapped), mapped

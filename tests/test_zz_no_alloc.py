@@ -92,6 +92,33 @@ def test_noalloc_matches_allocating_build_twice(math_mode):
             assert_same(buf.fetch(ctx), ref)
 
 
+def test_noalloc_smaller_batch_after_a_larger_one():
+    """The array keeps the last call's contents: a call with fewer chunks
+    after a larger one still starts from cleared scratch and gives the
+    allocating build's output."""
+    p, d = workloads.uniform_grid(seed=9, outputs=OUTPUTS)
+    p.math_mode = abi.UWW_MATH_FAST
+    big = make_descs(d["pos"][:2048], d["cells"][:2048])
+    small = make_descs(d["pos"][1500:1564], d["cells"][1500:1564])
+    vcap, icap = 300_000, 1_000_000
+    with Context(p) as ctx:
+        results = []
+        for descs in (big, small):
+            n, ncells = len(descs), int((descs["cells"].astype(np.int64) ** 3).sum())
+            d_desc = ctx.upload(descs)
+            ref_buf, buf = Buffers(n, ncells, vcap, icap), Buffers(n, ncells, vcap, icap)
+            ref_out, out = ref_buf.out(), buf.out()
+            abi.check(abi.lib().uww_build_chunks(ctx.h, C.c_void_p(d_desc.ptr), n, 12, C.byref(ref_out)))
+            abi.check(abi.lib().uww_build_chunks_noalloc(C.byref(p), C.c_void_p(ctx.stream()), C.c_void_p(d_desc.ptr),
+                                                         n, 12, C.byref(out)))
+            ctx.sync()
+            results.append((buf.fetch(ctx), ref_buf.fetch(ctx)))
+        for got, ref in results:
+            assert int(ref["totals"][2]) == 0 and int(ref["totals"][3]) == 0
+            assert_same(got, ref)
+        assert int(results[1][1]["totals"][1]) > 0
+
+
 def test_noalloc_rejects_sizes_beyond_its_scratch():
     p, d = workloads.uniform_grid(seed=1)
     with Context(p) as ctx:
@@ -104,4 +131,8 @@ def test_noalloc_rejects_sizes_beyond_its_scratch():
                                           C.byref(out)) == abi.UWW_ERR_INVALID_ARG
         # chunks whose working set would need a global scratch slot
         assert L.uww_build_chunks_noalloc(C.byref(p), C.c_void_p(ctx.stream()), C.c_void_p(d_desc.ptr), 4, 48,
+                                          C.byref(out)) == abi.UWW_ERR_INVALID_ARG
+        # no totals: a timeout, bad descriptor or overflow could not be reported
+        out.totals = None
+        assert L.uww_build_chunks_noalloc(C.byref(p), C.c_void_p(ctx.stream()), C.c_void_p(d_desc.ptr), 4, 12,
                                           C.byref(out)) == abi.UWW_ERR_INVALID_ARG

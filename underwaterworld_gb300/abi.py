@@ -15,90 +15,11 @@ ROOT = PKG.parent
 LIB_PATH = PKG / "_build" / "libuww_gb300.so"
 HEADER = ROOT / "include" / "uww.h"
 
-# ---- constants (uww.h) ------------------------------------------------------
-UWW_OK, UWW_ERR_INVALID_ARG, UWW_ERR_CUDA, UWW_ERR_CAPACITY, UWW_ERR_OOM, UWW_ERR_TIMEOUT = range(6)
-UWW_MAX_OCTAVES = 16
-UWW_MAX_CELLS = 64
-UWW_BIAS_NONE, UWW_BIAS_TERRACED, UWW_BIAS_LINEAR = 0, 1, 2
-UWW_MATH_EXACT, UWW_MATH_FAST = 0, 1
-UWW_DEDUP_ORIENTED, UWW_DEDUP_EDGE = 0, 1
-UWW_OUT_COLOR, UWW_OUT_NORMALS, UWW_OUT_CASES, UWW_OUT_SAMPLES = 1, 2, 4, 8
-UWW_CHUNK_EARLY_BLANK, UWW_CHUNK_HAS_MESH, UWW_CHUNK_OVERFLOW = 1, 2, 4
-UWW_ERRFLAG_TIMEOUT, UWW_ERRFLAG_BAD, UWW_ERRFLAG_RANGE = 1, 2, 4
-H2D, D2H, D2D = 0, 1, 2
-
-
-class Params(C.Structure):
-    _fields_ = [
-        ("seed", C.c_uint32), ("octaves", C.c_uint32), ("chunk_size", C.c_int32),
-        ("base_freq", C.c_float), ("lacunarity", C.c_float), ("persistence", C.c_float),
-        ("amplitude", C.c_float), ("normalize", C.c_int32), ("bias_mode", C.c_int32),
-        ("bias_a", C.c_float), ("bias_b", C.c_float), ("bias_c", C.c_float),
-        ("iso_level", C.c_float), ("offset", C.c_float * 3), ("explicit_amps", C.c_int32),
-        ("amps", C.c_float * UWW_MAX_OCTAVES), ("math_mode", C.c_int32), ("dedup_mode", C.c_int32),
-        ("outputs", C.c_uint32), ("color_min_z", C.c_float), ("color_max_z", C.c_float),
-    ]
-
-    def copy(self) -> "Params":
-        q = Params()
-        C.pointer(q)[0] = self
-        return q
-
-
-class ChunkDesc(C.Structure):
-    _fields_ = [("pos", C.c_int32 * 3), ("cells", C.c_uint32), ("cell_offset", C.c_uint32),
-                ("sample_offset", C.c_uint32), ("reserved", C.c_uint32 * 2)]
-
-
-class ChunkRecord(C.Structure):
-    _fields_ = [("num_verts", C.c_uint32), ("num_inds", C.c_uint32), ("vert_offset", C.c_uint32),
-                ("ind_offset", C.c_uint32), ("flags", C.c_uint32), ("num_active_cells", C.c_uint32),
-                ("reserved", C.c_uint32 * 2)]
-
-
-class MeshOut(C.Structure):
-    _fields_ = [("verts", C.c_void_p), ("normals", C.c_void_p), ("inds", C.c_void_p), ("cases", C.c_void_p),
-                ("samples", C.c_void_p), ("records", C.c_void_p), ("totals", C.c_void_p),
-                ("vert_capacity", C.c_uint32), ("ind_capacity", C.c_uint32),
-                ("case_capacity", C.c_uint64), ("sample_capacity", C.c_uint64)]
-
-
-class RayScene(C.Structure):
-    _fields_ = [("chunks", C.c_void_p), ("records", C.c_void_p), ("verts", C.c_void_p), ("inds", C.c_void_p),
-                ("cases", C.c_void_p), ("cell_first", C.c_void_p), ("table", C.c_void_p), ("n", C.c_uint32),
-                ("table_size", C.c_uint32)]
-
-
-class ScheduleParams(C.Structure):
-    _fields_ = [("sub_pos", C.c_float * 3), ("sub_chunk", C.c_int32 * 3), ("view_proj", C.c_float * 16),
-                ("gen_proj", C.c_float * 16), ("generation_dist", C.c_int32), ("view_dist", C.c_int32),
-                ("min_z", C.c_int32), ("max_z", C.c_int32), ("cells", C.c_uint32)]
-
-
-class CameraUniform(C.Structure):
-    _fields_ = [("view_proj", C.c_float * 16), ("fog_color", C.c_float * 3), ("pad1", C.c_float),
-                ("sub_pos", C.c_float * 3), ("pad2", C.c_float), ("sub_forward", C.c_float * 3), ("pad3", C.c_float)]
-
-
-class Tuning(C.Structure):
-    _fields_ = [("threads", C.c_int32), ("blocks_per_sm", C.c_int32), ("smem_cells", C.c_int32),
-                ("reserved", C.c_int32)]
-
-
-assert C.sizeof(ChunkDesc) == 32 and C.sizeof(ChunkRecord) == 32
-
-# numpy views of the structs
-try:
-    import numpy as np
-
-    CHUNK_DESC_DTYPE = np.dtype([("pos", "<i4", 3), ("cells", "<u4"), ("cell_offset", "<u4"),
-                                 ("sample_offset", "<u4"), ("reserved", "<u4", 2)])
-    CHUNK_RECORD_DTYPE = np.dtype([("num_verts", "<u4"), ("num_inds", "<u4"), ("vert_offset", "<u4"),
-                                   ("ind_offset", "<u4"), ("flags", "<u4"), ("num_active_cells", "<u4"),
-                                   ("reserved", "<u4", 2)])
-    VERT_COLOR_DTYPE = np.dtype([("pos", "<f4", 3), ("color", "<f4", 3)])
-except ImportError:  # pragma: no cover
-    np = None
+# Constants, struct layouts and numpy dtypes live in .layout (no library load).
+from .layout import *  # noqa: F401,F403
+from .layout import (CHUNK_DESC_DTYPE, CHUNK_RECORD_DTYPE, VERT_COLOR_DTYPE, UWW_ERR_CUDA,  # noqa: F401
+                     UWW_ERR_OOM, UWW_MAX_OCTAVES, UWW_OK, CameraUniform, ChunkDesc, ChunkRecord, MeshOut,
+                     Params, RayScene, ScheduleParams, Tuning, theta_count)
 
 P = C.c_void_p
 _SIGS = {
@@ -128,7 +49,6 @@ _SIGS = {
     "uww_memcpy": (C.c_int, [P, P, P, C.c_size_t, C.c_int]),
     "uww_memset": (C.c_int, [P, P, C.c_int, C.c_size_t]),
     "uww_density_at": (C.c_int, [P, P, C.c_uint32, P]),
-    "uww_probe_fma": (C.c_int, [P, C.c_uint32, C.c_uint32, P, C.POINTER(C.c_double)]),
     "uww_autotune": (C.c_int, [P, P, C.c_uint32, C.c_uint32, C.POINTER(MeshOut), C.c_char_p, C.POINTER(Tuning),
                                C.POINTER(C.c_float)]),
     "uww_frame_create": (C.c_int, [P, C.c_uint32, C.c_uint32, P, P, C.POINTER(MeshOut), P, P, C.POINTER(P)]),
@@ -149,10 +69,6 @@ _SIGS = {
                                   P, P, P, P]),
 }
 
-
-def theta_count(octaves: int) -> int:
-    """UWW_THETA_COUNT: per-octave amplitudes, base frequency, offset xyz, iso level."""
-    return int(octaves) + 5
 
 _lib = None
 
@@ -198,6 +114,7 @@ def check(status: int, what: str = "") -> None:
 
 
 def reference_params() -> Params:
+    """uww_params_reference() of the library (the same values as layout.reference_params)."""
     p = Params()
     lib().uww_params_reference(C.byref(p))
     return p

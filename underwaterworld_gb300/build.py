@@ -76,7 +76,26 @@ def build(verbose: bool = False, force: bool = False, extra_flags=()) -> Path:
             sys.stderr.write(r.stdout + r.stderr)
             raise RuntimeError("link of libuww_gb300.so failed")
     build_host()
+    build_probe(force=force)
     return LIB
+
+
+PROBE_LIB = OUT / "libuww_bench_probe.so"
+
+
+def build_probe(force: bool = False) -> Path:
+    """The benchmark's measurement kernels (FP32 peak, host-write bandwidth),
+    a library of their own: they are not part of the chunk builder's ABI."""
+    OUT.mkdir(exist_ok=True)
+    src = CSRC / "bench_probe.cu"
+    if force or _stale(PROBE_LIB, [src]):
+        cmd = [nvcc(), *ARCH, "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-shared", "-cudart", "static",
+               str(src), "-o", str(PROBE_LIB)]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode:
+            sys.stderr.write(r.stdout + r.stderr)
+            raise RuntimeError("build of libuww_bench_probe.so failed")
+    return PROBE_LIB
 
 
 def build_oracle() -> Path:

@@ -13,15 +13,12 @@ Everything runs in libuww_gb300.so; there is no CPU path here.
 from __future__ import annotations
 
 import ctypes as C
-from dataclasses import dataclass
-
 import numpy as np
 
 from . import abi
 from .abi import check, lib
-
-CHUNK_SIZE = 16       # chunk.rs:5
-INTERNAL_SIZE = 12    # chunk.rs:6
+from .layout import (CHUNK_SIZE, INTERNAL_SIZE, MeshBatch, make_descs, total_cells,  # noqa: F401
+                     total_samples, totals_status)
 
 
 class DeviceArray:
@@ -71,59 +68,6 @@ class HostArray:
             pass
 
 
-def make_descs(positions, cells) -> np.ndarray:
-    """Chunk descriptors with cell offsets laid out in order."""
-    positions = np.asarray(positions, dtype=np.int32).reshape(-1, 3)
-    cells = np.broadcast_to(np.asarray(cells, dtype=np.uint32), (positions.shape[0],))
-    d = np.zeros(positions.shape[0], dtype=abi.CHUNK_DESC_DTYPE)
-    d["pos"] = positions
-    d["cells"] = cells
-    c3 = cells.astype(np.uint64) ** 3
-    s3 = (cells.astype(np.uint64) + 1) ** 3
-    d["cell_offset"] = (np.cumsum(c3) - c3).astype(np.uint32)
-    d["sample_offset"] = (np.cumsum(s3) - s3).astype(np.uint32)
-    return d
-
-
-def total_cells(descs) -> int:
-    return int((descs["cells"].astype(np.uint64) ** 3).sum()) if len(descs) else 0
-
-
-def total_samples(descs) -> int:
-    return int(((descs["cells"].astype(np.uint64) + 1) ** 3).sum()) if len(descs) else 0
-
-
-def totals_status(totals) -> int:
-    """Status of a finished device build from its totals words."""
-    flags = int(totals[3])
-    if flags & abi.UWW_ERRFLAG_TIMEOUT:
-        return abi.UWW_ERR_TIMEOUT
-    if flags & (abi.UWW_ERRFLAG_BAD | abi.UWW_ERRFLAG_RANGE):
-        return abi.UWW_ERR_INVALID_ARG
-    if int(totals[2]):
-        return abi.UWW_ERR_CAPACITY
-    return abi.UWW_OK
-
-
-@dataclass
-class MeshBatch:
-    """Outputs of a batched build, in chunk order."""
-    records: np.ndarray          # CHUNK_RECORD_DTYPE
-    verts: np.ndarray            # VERT_COLOR_DTYPE
-    normals: np.ndarray | None   # (V, 3) f32
-    inds: np.ndarray             # u32, chunk-local vertex ids
-    cases: np.ndarray | None     # u8 per cell
-    totals: np.ndarray           # u64[4]
-    status: int
-    samples: np.ndarray | None = None  # f32 density samples per chunk
-
-    def chunk(self, i: int):
-        r = self.records[i]
-        v0, nv, i0, ni = int(r["vert_offset"]), int(r["num_verts"]), int(r["ind_offset"]), int(r["num_inds"])
-        nrm = self.normals[v0:v0 + nv] if self.normals is not None else None
-        return self.verts[v0:v0 + nv], nrm, self.inds[i0:i0 + ni]
-
-
 class Context:
     """A noise::Perlin handle plus the chunk builder, on one CUDA stream."""
 
@@ -158,8 +102,14 @@ class Context:
         check(lib().uww_ctx_set_params(self.h, C.byref(params)), "uww_ctx_set_params")
         self.params = params
 
-    def set_tuning(self, threads=0, blocks_per_sm=0, smem_cells=0):
-        t = abi.Tuning(threads, blocks_per_sm, smem_cells, 0)
+    def set_tuning(self, threads=0, blocks_per_sm=0, smem_cells=0, options=None):
+        """Launch shape (0 = automatic) and, when given, the UWW_TUNE_* options;
+        the spin limit and test flags stay as they are."""
+        t = abi.Tuning()
+        check(lib().uww_ctx_get_tuning(self.h, C.byref(t)), "uww_ctx_get_tuning")
+        t.threads, t.blocks_per_sm, t.smem_cells = threads, blocks_per_sm, smem_cells
+        if options is not None:
+            t.options = options
         check(lib().uww_ctx_set_tuning(self.h, C.byref(t)), "uww_ctx_set_tuning")
 
     def stream(self) -> int:

@@ -242,7 +242,9 @@ int launch(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint32_t ma
     a.smem_buf_bytes = cfg.smem_buf;
     a.ztable_offset = cfg.ztable_offset;
     a.smem_cells = cfg.smem_cells;
-    a.spin_limit_cycles = kSpinLimitCycles;
+    a.spin_limit_cycles = ctx->spin_limit > 0 ? ctx->spin_limit : kSpinLimitCycles;
+    a.withhold_first = (ctx->test_flags & UWW_TEST_WITHHOLD_FIRST) ? 1u : 0u;
+    a.no_depth_shortcut = (ctx->options & UWW_TUNE_NO_DEPTH_SHORTCUT) ? 1u : 0u;
     a.edge_ids = edge_ids;
     a.n_dev = n_dev;
     if (host && queue) {
@@ -655,9 +657,14 @@ int uww_ctx_set_tuning(uww_ctx* ctx, const uww_tuning* t)
     if (t->threads > 192 && t->threads < 224) return UWW_ERR_INVALID_ARG;  // between the two kernel shapes
     if (t->blocks_per_sm < 0 || t->blocks_per_sm > 32) return UWW_ERR_INVALID_ARG;
     if (t->smem_cells < 0 || t->smem_cells > UWW_MAX_CELLS) return UWW_ERR_INVALID_ARG;
+    if (t->spin_limit < 0 || (t->test_flags & ~UWW_TEST_WITHHOLD_FIRST)) return UWW_ERR_INVALID_ARG;
+    if (t->options & ~UWW_TUNE_NO_DEPTH_SHORTCUT) return UWW_ERR_INVALID_ARG;
     ctx->threads = t->threads;
     ctx->blocks_per_sm = t->blocks_per_sm;
     ctx->smem_cells = t->smem_cells;
+    ctx->spin_limit = t->spin_limit;
+    ctx->test_flags = t->test_flags;
+    ctx->options = t->options;
     return UWW_OK;
 }
 
@@ -667,7 +674,10 @@ int uww_ctx_get_tuning(const uww_ctx* ctx, uww_tuning* t)
     t->threads = ctx->threads;
     t->blocks_per_sm = ctx->blocks_per_sm;
     t->smem_cells = ctx->smem_cells;
-    t->reserved = 0;
+    t->spin_limit = (int32_t)ctx->spin_limit;
+    t->test_flags = ctx->test_flags;
+    t->options = ctx->options;
+    t->reserved[0] = t->reserved[1] = 0;
     return UWW_OK;
 }
 
@@ -708,13 +718,6 @@ int uww_memset(uww_ctx* ctx, void* dst, int value, size_t bytes)
     if (!ctx || (bytes && !dst)) return UWW_ERR_INVALID_ARG;
     if (!bytes) return UWW_OK;
     return cuda_status(cudaMemsetAsync(dst, value, bytes, ctx->stream));
-}
-
-int uww_probe_fma(uww_ctx* ctx, uint32_t blocks, uint32_t iters, float* d_sink, double* flops)
-{
-    if (!ctx || !d_sink || blocks == 0 || iters == 0) return UWW_ERR_INVALID_ARG;
-    if (flops) *flops = 2.0 * 8.0 * 16.0 * (double)iters * 256.0 * (double)blocks;
-    return cuda_status(launch_fma_probe((int)blocks, iters, d_sink, ctx->stream));
 }
 
 int uww_density_at(uww_ctx* ctx, const float* d_xyz, uint32_t n, float* d_out)

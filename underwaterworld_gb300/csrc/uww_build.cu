@@ -181,6 +181,7 @@ __device__ __forceinline__ unsigned long long pack_counts(unsigned long long tot
 // publishes its inclusive prefix right away).
 __device__ __forceinline__ void lookback_publish(const BuildArgs& a, uint32_t ticket, unsigned long long own)
 {
+    if (a.withhold_first && ticket == 0) return;  // failure injection: successors time out
     st_relaxed(&a.lookback[ticket], (ticket == 0 ? kLbInclusive : kLbAggregate) | own);
 }
 
@@ -242,7 +243,8 @@ __device__ unsigned long long lookback_warp(const BuildArgs& a, uint32_t ticket,
             j -= 128;
         }
     }
-    if (lane == 0) st_relaxed(&a.lookback[ticket], kLbInclusive | sat_add_packed(sum, own));
+    if (lane == 0 && !(a.withhold_first && ticket == 0))
+        st_relaxed(&a.lookback[ticket], kLbInclusive | sat_add_packed(sum, own));
     return sum;
 }
 
@@ -370,7 +372,7 @@ __device__ void chunk_front(const DevParams& p, const BuildArgs& a, SmemTables& 
     // A chunk whose depth bias keeps every sample above (below) the iso level
     // by more than the fBm can reach is blank (solid) without its noise --
     // unless its samples are read or written.
-    const int decided = (!bad && !a.samples_in && !a.samples_out) ? bias_decides(p, N, oz) : 0;
+    const int decided = (!bad && !a.samples_in && !a.samples_out && !a.no_depth_shortcut) ? bias_decides(p, N, oz) : 0;
     int inside = decided == 2, outside = decided == 1;
     if (!bad && !decided) {
         const float s = __fdiv_rn((float)p.chunk_size, (float)N);  // SIZE_SCALE
@@ -843,7 +845,8 @@ __global__ void __launch_bounds__(MAXT, MINB) build_kernel(const DevParams p, co
 
     if (tid >= ncomp) {
         // ---- control warp ----
-        const bool decide = !a.samples_in && !a.samples_out && !((p.outputs & UWW_OUT_CASES) && a.cases);
+        const bool decide = !a.samples_in && !a.samples_out && !((p.outputs & UWW_OUT_CASES) && a.cases) &&
+                            !a.no_depth_shortcut;
         take_work_ticket(p, a, T, T.tk[0], decide);
         for (int i = 0;; ++i) {
             bar_sync(kBarTicket, nthr);  // ticket i staged; chunk i-1's counts visible
@@ -981,23 +984,6 @@ __global__ void density_kernel(const DevParams p, const float* __restrict__ xyz,
         out[i] = density<O, false>(p, P, xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], nullptr);
 }
 
-// FP32 peak probe: 8 independent FMA chains per thread, no memory traffic
-// except one store per thread to keep the chains live.
-__global__ void __launch_bounds__(256) fma_probe_kernel(uint32_t iters, float seed, float* __restrict__ sink)
-{
-    float a0 = seed + threadIdx.x, a1 = a0 + 1.f, a2 = a0 + 2.f, a3 = a0 + 3.f;
-    float a4 = a0 + 4.f, a5 = a0 + 5.f, a6 = a0 + 6.f, a7 = a0 + 7.f;
-    const float m = 0.9999999f, c = 1e-7f;
-    for (uint32_t i = 0; i < iters; ++i) {
-#pragma unroll
-        for (int j = 0; j < 16; ++j) {
-            a0 = fmaf(a0, m, c); a1 = fmaf(a1, m, c); a2 = fmaf(a2, m, c); a3 = fmaf(a3, m, c);
-            a4 = fmaf(a4, m, c); a5 = fmaf(a5, m, c); a6 = fmaf(a6, m, c); a7 = fmaf(a7, m, c);
-        }
-    }
-    sink[blockIdx.x * blockDim.x + threadIdx.x] = ((a0 + a1) + (a2 + a3)) + ((a4 + a5) + (a6 + a7));
-}
-
 using BuildFn = void (*)(const DevParams, const BuildArgs);
 
 // [exact][queue][large]
@@ -1060,12 +1046,6 @@ cudaError_t launch_build(const DevParams& p, const BuildArgs& a, bool queue, int
     const int vgrid = std::max(1, sms * 8);
     if (exact) vertex_kernel<ExactOps><<<vgrid, 256, 0, s>>>(p, a.verts, a.normals, a.totals, a.vert_capacity);
     else vertex_kernel<FastOps><<<vgrid, 256, 0, s>>>(p, a.verts, a.normals, a.totals, a.vert_capacity);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_fma_probe(int blocks, uint32_t iters, float* sink, cudaStream_t s)
-{
-    fma_probe_kernel<<<blocks, 256, 0, s>>>(iters, 1.0f, sink);
     return cudaGetLastError();
 }
 

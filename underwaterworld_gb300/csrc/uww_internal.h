@@ -88,6 +88,8 @@ struct BuildArgs {
     size_t ztable_offset;            // fast build: per-chunk z tables, after the workspaces
     uint32_t smem_cells;             // chunks with cells <= smem_cells work in shared memory
     long long spin_limit_cycles;     // bound on every device-side wait
+    uint32_t withhold_first;         // UWW_TEST_WITHHOLD_FIRST: ticket 0 never publishes its prefix
+    uint32_t no_depth_shortcut;      // UWW_TUNE_NO_DEPTH_SHORTCUT: every chunk evaluates its noise
     uint32_t* edge_ids;              // optional, per output vertex: (first corner sample << 3) | direction
     const uint32_t* n_dev;           // optional device chunk count; the launch builds min(*n_dev, n)
     // Optional streamed host output (batched form): device addresses of
@@ -131,7 +133,6 @@ cudaError_t launch_build(const DevParams& p, const BuildArgs& a, bool queue, int
 cudaError_t build_occupancy(bool queue, bool exact, int threads, size_t dyn_smem, int* blocks_per_sm);
 cudaError_t prepare_build_kernels(size_t optin, size_t* max_dyn_smem);
 cudaError_t launch_density(const DevParams& p, const float* xyz, uint32_t n, float* out, cudaStream_t s);
-cudaError_t launch_fma_probe(int blocks, uint32_t iters, float* sink, cudaStream_t s);
 
 // Batched build on the context (uww_api.cu); edge_ids and n_dev as in BuildArgs.
 int launch_batched(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint32_t max_cells,
@@ -178,6 +179,9 @@ struct uww_ctx {
     int threads = 0;
     int blocks_per_sm = 0;
     int smem_cells = 0;
+    long long spin_limit = 0;     // bound on device-side waits in cycles; 0 = kSpinLimitCycles
+    uint32_t test_flags = 0;      // UWW_TEST_* failure injection
+    uint32_t options = 0;         // UWW_TUNE_*
 
     // device work state
     unsigned long long* d_lookback = nullptr;

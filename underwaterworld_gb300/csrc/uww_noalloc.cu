@@ -27,7 +27,11 @@
 //     the process exits;
 //   * the first call on a device looks up the array's device address
 //     (cudaGetSymbolAddress) and sets the kernels' shared-memory limit; make
-//     that first call before any stream capture.
+//     that first call before any stream capture.  The result is kept for the
+//     life of the process: a cudaDeviceReset() on that device (which creates
+//     a new primary context) is not supported afterwards;
+//   * out->totals is required: the four totals words are the call's only
+//     report of a timed-out wait, a bad descriptor or an output overflow.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -40,7 +44,7 @@ namespace {
 
 constexpr uint32_t kNoAllocMaxChunks = 65536;
 // word 0: ticket counter (low 32 bits); 1..3: overflow count, error flags,
-// finished CTAs; 4..7: totals when the caller passes none; 8..: look-back words
+// finished CTAs; 4..7: unused; 8..: look-back words
 constexpr size_t kHeadWords = 8;
 constexpr size_t kScratchWords = kHeadWords + kNoAllocMaxChunks;
 
@@ -96,15 +100,14 @@ extern "C" int uww_build_chunks_noalloc(const uww_params* params, void* stream, 
     int st = check_params(params);
     if (st) return st;
     if (!out || !out->verts || !out->inds || !out->records) return UWW_ERR_INVALID_ARG;
+    // without totals a timeout, a bad descriptor or an overflow would go unreported
+    if (!out->totals) return UWW_ERR_INVALID_ARG;
     if (out->vert_capacity > kLbVertMax) return UWW_ERR_INVALID_ARG;
     if (!device_out_aligned(out)) return UWW_ERR_INVALID_ARG;
     if (max_cells < 1 || max_cells > UWW_MAX_CELLS) return UWW_ERR_INVALID_ARG;
     if (n > kNoAllocMaxChunks) return UWW_ERR_INVALID_ARG;  // beyond the fixed scratch
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    if (n == 0) {
-        if (out->totals) return status_from_cuda(cudaMemsetAsync(out->totals, 0, 4 * sizeof(uint64_t), s), "cudaMemsetAsync");
-        return UWW_OK;
-    }
+    if (n == 0) return status_from_cuda(cudaMemsetAsync(out->totals, 0, 4 * sizeof(uint64_t), s), "cudaMemsetAsync");
     if (!d_chunks || !aligned_to(d_chunks, 4)) return UWW_ERR_INVALID_ARG;
 
     int dev = 0;
@@ -149,7 +152,7 @@ extern "C" int uww_build_chunks_noalloc(const uww_params* params, void* stream, 
     a.case_capacity = out->case_capacity;
     a.sample_capacity = out->sample_capacity;
     a.records = out->records;
-    a.totals = out->totals ? reinterpret_cast<unsigned long long*>(out->totals) : scratch + 4;
+    a.totals = reinterpret_cast<unsigned long long*>(out->totals);
     a.vert_capacity = out->vert_capacity;
     a.ind_capacity = out->ind_capacity;
     a.lookback = scratch + kHeadWords;

@@ -137,7 +137,6 @@ bool cache_lookup(const char* path, const std::string& key, uww_tuning* t, float
             t->threads = th;
             t->blocks_per_sm = bps;
             t->smem_cells = sc;
-            t->reserved = 0;
             *us = u;
             found = true;  // the last entry for a key wins
         }
@@ -237,6 +236,7 @@ int uww_autotune(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint3
     if (e != cudaSuccess) return status_from_cuda(e, "autotune descriptor read");
     const std::string key = tune_key(ctx, h, max_cells);
     float us = 0.f;
+    uww_ctx_get_tuning(ctx, best);  // a cached entry sets the launch shape; the rest stays the context's
     if (cache_path && cache_lookup(cache_path, key, best, &us)) {
         if (best_us) *best_us = us;
         return uww_ctx_set_tuning(ctx, best);
@@ -250,7 +250,8 @@ int uww_autotune(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint3
     std::vector<int> smem = {0};
     for (int c : {24, 16, 12})
         if ((uint32_t)c < max_cells) smem.push_back(c);
-    const uww_tuning saved = {ctx->threads, ctx->blocks_per_sm, ctx->smem_cells, 0};
+    uww_tuning saved;
+    uww_ctx_get_tuning(ctx, &saved);
     uww_tuning bt = saved;
     float bus = INFINITY;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -300,7 +301,10 @@ int uww_autotune(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint3
                 if (!ok) break;
                 if (best_rep < bus) {
                     bus = best_rep;
-                    bt = {th, bps, sc, 0};
+                    bt = saved;  // keeps the context's spin limit and test flags
+                    bt.threads = th;
+                    bt.blocks_per_sm = bps;
+                    bt.smem_cells = sc;
                 }
             }
             if (st || e != cudaSuccess) break;

@@ -20,12 +20,12 @@ from __future__ import annotations
 
 import numpy as np
 
-from . import abi
-from .chunk import make_descs
+from . import layout
+from .layout import make_descs
 
 
-def reference_grid(iso_level: float = -0.1, seed: int = 0, outputs: int = abi.UWW_OUT_COLOR):
-    p = abi.reference_params()
+def reference_grid(iso_level: float = -0.1, seed: int = 0, outputs: int = layout.UWW_OUT_COLOR):
+    p = layout.reference_params()
     p.seed = seed
     p.iso_level = iso_level
     p.outputs = outputs
@@ -35,8 +35,8 @@ def reference_grid(iso_level: float = -0.1, seed: int = 0, outputs: int = abi.UW
 
 
 def fbm_params(seed: int, octaves: int, freq: float, slope: float, z0: float, iso: float = 0.0,
-               outputs: int = abi.UWW_OUT_COLOR) -> abi.Params:
-    p = abi.reference_params()
+               outputs: int = layout.UWW_OUT_COLOR) -> layout.Params:
+    p = layout.reference_params()
     p.seed = seed
     p.octaves = octaves
     p.base_freq = freq
@@ -44,7 +44,7 @@ def fbm_params(seed: int, octaves: int, freq: float, slope: float, z0: float, is
     p.persistence = 0.5
     p.amplitude = 1.0
     p.normalize = 1
-    p.bias_mode = abi.UWW_BIAS_LINEAR
+    p.bias_mode = layout.UWW_BIAS_LINEAR
     p.bias_a = slope
     p.bias_b = z0
     p.bias_c = 0.0
@@ -53,14 +53,14 @@ def fbm_params(seed: int, octaves: int, freq: float, slope: float, z0: float, is
     return p
 
 
-def uniform_grid(seed: int = 0, side: int = 16, outputs: int = abi.UWW_OUT_COLOR):
+def uniform_grid(seed: int = 0, side: int = 16, outputs: int = layout.UWW_OUT_COLOR):
     p = fbm_params(seed, 4, 0.04, -0.03, 128.0, 0.0, outputs)
     g = np.arange(side)
     pos = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)
     return p, make_descs(pos, 12)
 
 
-def mixed_lod(seed: int = 0, n: int = 2048, outputs: int = abi.UWW_OUT_COLOR):
+def mixed_lod(seed: int = 0, n: int = 2048, outputs: int = layout.UWW_OUT_COLOR):
     p = fbm_params(seed, 6, 0.03, 0.02, 0.0, 0.0, outputs)
     rng = np.random.default_rng(1000 + seed)
     flat = rng.choice(64 * 64 * 16, size=n, replace=False)
@@ -69,7 +69,7 @@ def mixed_lod(seed: int = 0, n: int = 2048, outputs: int = abi.UWW_OUT_COLOR):
     return p, make_descs(pos, cells)
 
 
-def adjoint_batch(seed: int = 0, side: int = 8, cells: int = 24, outputs: int = abi.UWW_OUT_CASES):
+def adjoint_batch(seed: int = 0, side: int = 8, cells: int = 24, outputs: int = layout.UWW_OUT_CASES):
     p = fbm_params(seed, 4, 0.04, -0.03, 128.0, 0.0, outputs)
     g = np.arange(side)
     pos = np.stack(np.meshgrid(g, g, g + 8 - side // 2, indexing="ij"), -1).reshape(-1, 3)
@@ -91,7 +91,7 @@ def cotangents(records: np.ndarray, edge_ids: np.ndarray, seed: int = 0) -> np.n
     chunk = np.zeros(nv, dtype=np.uint64)
     for i, r in enumerate(records):
         o, n = int(r["vert_offset"]), int(r["num_verts"])
-        if n and not (int(r["flags"]) & abi.UWW_CHUNK_OVERFLOW):
+        if n and not (int(r["flags"]) & layout.UWW_CHUNK_OVERFLOW):
             chunk[o:o + n] = i
     with np.errstate(over="ignore"):
         key = (np.uint64(seed) << np.uint64(56)) ^ (chunk << np.uint64(32)) ^ edge_ids.astype(np.uint64)
