@@ -267,6 +267,22 @@ int launch(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint32_t ma
         a.lookback = ctx->d_lookback;
         a.work_counter = ctx->d_counter;
         a.acc = ctx->d_acc;
+        // a batch whose samples and cases are neither read nor written is
+        // planned: a first kernel lists the chunks the depth bias does not
+        // decide, and the build takes only those
+        const bool planned = !samples_in && !a.samples_out && !(a.cases && (ctx->params.outputs & UWW_OUT_CASES)) &&
+                             !a.no_depth_shortcut;
+        if (planned) {
+            // its finish counter is zero between launches: cleared here on
+            // (re)allocation, re-armed by the planning kernel's last CTA
+            if (!ctx->d_plan || ctx->plan_cap < plan_buffer_bytes(n)) {
+                st = grow(&ctx->d_plan, &ctx->plan_cap, plan_buffer_bytes(std::max<uint32_t>(n, 4096)));
+                if (st) return st;
+                cudaError_t e = cudaMemsetAsync(ctx->d_plan, 0, ctx->plan_cap, ctx->stream);
+                if (e != cudaSuccess) return cuda_status(e, "cudaMemsetAsync");
+            }
+            a.plan = ctx->d_plan;
+        }
     }
     if (prepare_only) return UWW_OK;
     return cuda_status(launch_build(ctx->dev, a, queue, cfg.grid, cfg.threads, cfg.dyn_smem, ctx->stream), "build kernel launch");
@@ -445,6 +461,7 @@ int uww_ctx_destroy(uww_ctx* ctx)
     if (!ctx) return UWW_ERR_INVALID_ARG;
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     cudaFree(ctx->d_lookback);
+    cudaFree(ctx->d_plan);
     cudaFree(ctx->d_state);
     cudaFree(ctx->d_totals);
     cudaFree(ctx->d_scratch);

@@ -27,10 +27,17 @@
 // counter).  Each CTA is warp-specialised -- compute warps plus one control
 // warp -- and pipelines two chunks: once the compute warps finish the noise of
 // ticket i, the control warp resolves the look-back of ticket i-1 (while
-// ticket i is classified) and writes its record; once ticket i-1 is emitted
-// it takes ticket i+1 from the queue.  Look-back and record latency thus
-// overlap compute.  The plain form (one chunk per launch) runs
-// front then back with compute warps only.
+// ticket i is classified), writes its record and takes ticket i+1 from the
+// queue while ticket i-1 is emitted.  Look-back, record and ticket latency
+// thus overlap compute.  The plain form (one chunk per launch) runs front then
+// back with compute warps only.
+//
+// Planned batches: when neither samples nor cases are read or written, a
+// one-CTA planning kernel (plan_kernel) first lists, in chunk order, the
+// chunks the depth bias does not decide; the queue hands out only those, and
+// the control warp of each listed chunk writes the records of the decided
+// chunks that follow it (their offsets are its inclusive prefix).  A decided
+// chunk thus costs a record write, not a ticket.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -61,14 +68,15 @@ struct ChunkInfo {
     int32_t N;
     uint32_t flags;               // UWW_CHUNK_EARLY_BLANK decided by the front half
     uint32_t classified;          // the mesh stage ran (not bad, not early blank)
-    uint32_t pad;
+    uint32_t chunk;               // index of the chunk in the batch (records are indexed by it)
     unsigned long long total;     // packed counts
 };
 
 struct Ticket {
     uww_chunk_desc desc;
-    uint32_t ticket;
-    uint32_t pad[3];
+    uint32_t ticket;              // position in the work queue (and of its look-back word)
+    uint32_t chunk;               // the chunk it builds
+    uint32_t pad[2];
 };
 
 struct Offsets {
@@ -76,8 +84,6 @@ struct Offsets {
     uint32_t fits;
     uint32_t pad;
 };
-
-constexpr int kMaxPending = 64;
 
 struct SmemTables {
     float4 gp[256];               // gradient vector of P[i] (fast build: the last hash lookup)
@@ -97,9 +103,8 @@ struct SmemTables {
     uint32_t overflow;            // chunks of this CTA that did not fit (control warp)
     uint32_t errflags;            // UWW_ERRFLAG_* raised by this CTA
     uint32_t last;                // this CTA is the last of the launch to finish
-    uint32_t n;                   // chunks in this launch (min of the device count and BuildArgs::n)
-    uint32_t npend;               // tickets the control warp decided from the depth bias, records pending
-    uint32_t pend[kMaxPending];   // their tickets | kind << 30 (1 blank, 2 solid)
+    uint32_t n;                   // tickets of this launch: the planned chunks, else every chunk
+    uint32_t nchunks;             // chunks in this launch (min of the device count and BuildArgs::n)
 };
 
 // A cell's case from its four corner columns' inside masks (bit z: sample
@@ -199,6 +204,7 @@ __device__ unsigned long long lookback_warp(const BuildArgs& a, uint32_t ticket,
     if (ticket > 0) {
         long long j = (long long)ticket - 1;
         const long long t0 = clock64();
+        unsigned sleep_ns = 32;
         for (;;) {
             unsigned long long w[4];
             int mi = 0x7fffffff, mz = 0x7fffffff;
@@ -222,7 +228,8 @@ __device__ unsigned long long lookback_warp(const BuildArgs& a, uint32_t ticket,
                     sum = kLbVertMax | (kLbIndMax << 30);
                     break;
                 }
-                __nanosleep(64);
+                __nanosleep(sleep_ns);  // back off: the wait overlaps a noise phase
+                sleep_ns = min(2u * sleep_ns, 512u);
                 continue;
             }
             unsigned long long v = 0ull, i = 0ull;
@@ -274,8 +281,8 @@ __device__ __forceinline__ void chunk_record(const BuildArgs& a, SmemTables& T, 
     rec.flags = flags;
     rec.num_active_cells = nA;
     rec.reserved[0] = rec.reserved[1] = 0;
-    a.records[ci.ticket] = rec;
-    if (a.host_records) a.host_records[ci.ticket] = rec;
+    a.records[ci.chunk] = rec;
+    if (a.host_records) a.host_records[ci.chunk] = rec;
     if (!queue || ci.ticket == T.n - 1) {
         a.totals[0] = ev + nV;
         a.totals[1] = ei + nI;
@@ -336,7 +343,7 @@ __device__ __forceinline__ Workspace workspace(const BuildArgs& a, uint8_t* dyn_
 // Front half of a chunk into workspace `buf`.  Every compute thread must call it.
 template <class O, bool QUEUE>
 __device__ void chunk_front(const DevParams& p, const BuildArgs& a, SmemTables& T, uint8_t* dyn_smem,
-                            const uww_chunk_desc d, uint32_t ticket, int buf, int ncomp, int nall)
+                            const uww_chunk_desc d, uint32_t ticket, uint32_t chunk, int buf, int ncomp)
 {
     const int tid = threadIdx.x;
     const int oriented = p.dedup_mode == UWW_DEDUP_ORIENTED;
@@ -387,10 +394,13 @@ __device__ void chunk_front(const DevParams& p, const BuildArgs& a, SmemTables& 
             }
         } else if constexpr (std::is_same<O, FastOps>::value) {
             const ZTable zt = ztable_at(dyn_smem + a.ztable_offset, S, p.octaves);
-            // a chunk in a global scratch slot accumulates its columns in local memory
-            const int io = (uint32_t)N <= a.smem_cells
-                               ? sample_columns_fast<false>(p, T.perm, T.gp, zt, rho, N, ox, oy, oz, ncomp)
-                               : sample_columns_fast<true>(p, T.perm, T.gp, zt, rho, N, ox, oy, oz, ncomp, masks);
+            // the reference's 12^3 chunk accumulates its columns in registers; a
+            // chunk in a global scratch slot accumulates them in local memory
+            const bool in_smem = (uint32_t)N <= a.smem_cells;
+            const int io = (in_smem && S == 13)
+                               ? sample_columns_reg<13>(p, T.perm, T.gp, zt, rho, ox, oy, oz, ncomp)
+                           : in_smem ? sample_columns_fast<false>(p, T.perm, T.gp, zt, rho, N, ox, oy, oz, ncomp)
+                                     : sample_columns_fast<true>(p, T.perm, T.gp, zt, rho, N, ox, oy, oz, ncomp, masks);
             inside = io & 1;
             outside = io >> 1;
         } else {
@@ -410,9 +420,6 @@ __device__ void chunk_front(const DevParams& p, const BuildArgs& a, SmemTables& 
     // every sample below the iso level: every case is 255, no cell is
     // crossed, nothing to classify
     const int solid = bar_and(kBarCompute, ncomp, !outside);
-    // tell the control warp the noise is done: it now resolves the previous
-    // chunk's look-back while this chunk is classified
-    if (QUEUE) bar_arrive(kBarNoiseDone, nall);
     if (samples_ok) {
         float* dst = a.samples_out + d.sample_offset;
         for (int idx = tid; idx < S * S * S; idx += ncomp) dst[idx] = rho[idx];
@@ -511,6 +518,7 @@ __device__ void chunk_front(const DevParams& p, const BuildArgs& a, SmemTables& 
     if (tid == 0) {
         ChunkInfo& ci = T.ci[buf];
         ci.ticket = ticket;
+        ci.chunk = chunk;
         ci.ox = ox; ci.oy = oy; ci.oz = oz;
         ci.N = N;
         ci.flags = (!bad && !any_inside) ? UWW_CHUNK_EARLY_BLANK : 0u;
@@ -698,84 +706,63 @@ __device__ void chunk_emit(const DevParams& p, const BuildArgs& a, SmemTables& T
     }
 }
 
-// Control warp: take a ticket from the work queue and stage its descriptor.
+// Control warp: take a ticket from the work queue and stage its chunk's
+// descriptor (the planned chunk list maps tickets to chunks).
 __device__ __forceinline__ void take_ticket(const BuildArgs& a, uint32_t n, Ticket& tk)
 {
     const int lane = threadIdx.x & 31;
-    uint32_t t = 0;
-    if (lane == 0) t = atomicAdd(a.work_counter, 1u);
+    uint32_t t = 0, c = 0;
+    if (lane == 0) {
+        t = atomicAdd(a.work_counter, 1u);
+        c = (a.plan && t < n) ? __ldcg(&a.plan[kPlanList + t]) : t;
+    }
     t = __shfl_sync(0xffffffffu, t, 0);
+    c = __shfl_sync(0xffffffffu, c, 0);
     if (t < n && lane < 8)
-        reinterpret_cast<uint32_t*>(&tk.desc)[lane] = reinterpret_cast<const uint32_t*>(&a.chunks[t])[lane];
-    if (lane == 0) tk.ticket = t;
+        reinterpret_cast<uint32_t*>(&tk.desc)[lane] = reinterpret_cast<const uint32_t*>(&a.chunks[c])[lane];
+    if (lane == 0) {
+        tk.ticket = t;
+        tk.chunk = c;
+    }
     __syncwarp();
 }
 
-// The record of a chunk the depth bias decided (no cells crossed): empty,
-// early blank when every sample is above the iso level; by lane 0.
-__device__ __forceinline__ void decided_record(const BuildArgs& a, SmemTables& T, uint32_t ticket, int kind,
-                                               unsigned long long ex)
+// The record of chunk j, which the depth bias decided (kind 1: every sample
+// above the iso level, early blank; 2: every sample below it): no vertices,
+// no indices, offsets at the prefix (ev, ei).  Returns whether it fits.
+__device__ __forceinline__ bool decided_record(const BuildArgs& a, uint32_t j, int kind, unsigned long long ev,
+                                               unsigned long long ei)
 {
-    ChunkInfo ci;
-    ci.ticket = ticket;
-    ci.ox = ci.oy = ci.oz = 0;
-    ci.N = 0;
-    ci.flags = kind == 1 ? UWW_CHUNK_EARLY_BLANK : 0u;
-    ci.classified = 0;
-    ci.pad = 0;
-    ci.total = 0ull;
-    Offsets off;
-    chunk_record(a, T, ci, ex, off, true);
+    const bool fits = ev <= a.vert_capacity && ei <= a.ind_capacity;
+    uww_chunk_record rec;
+    rec.num_verts = 0;
+    rec.num_inds = 0;
+    rec.vert_offset = (uint32_t)(ev > 0xffffffffull ? 0xffffffffull : ev);
+    rec.ind_offset = (uint32_t)(ei > 0xffffffffull ? 0xffffffffull : ei);
+    rec.flags = (kind == 1 ? UWW_CHUNK_EARLY_BLANK : 0u) | (fits ? 0u : UWW_CHUNK_OVERFLOW);
+    rec.num_active_cells = 0;
+    rec.reserved[0] = rec.reserved[1] = 0;
+    a.records[j] = rec;
+    if (a.host_records) a.host_records[j] = rec;
+    return fits;
 }
 
-// Control warp: take tickets until one needs the compute warps.  A chunk the
-// depth bias decides (when neither its samples nor its cases are wanted) is
-// settled here: its empty aggregate is published at once, so no successor
-// waits on it, and its record -- which needs its prefix -- is written when the
-// control warp has no other work (kMaxPending at a time; beyond that at once).
-__device__ void take_work_ticket(const DevParams& p, const BuildArgs& a, SmemTables& T, Ticket& tk, bool decide)
+// Control warp, planned batches: the records of the decided chunks
+// [lo, hi) that follow a listed chunk, at that chunk's inclusive prefix.
+__device__ void decided_tail(const DevParams& p, const BuildArgs& a, SmemTables& T, uint32_t lo, uint32_t hi,
+                             unsigned long long incl)
 {
     const int lane = threadIdx.x & 31;
-    for (;;) {
-        take_ticket(a, T.n, tk);
-        const uint32_t t = tk.ticket;
-        if (!decide || t >= T.n) return;
-        const uww_chunk_desc d = tk.desc;
-        if (d.cells < 1 || d.cells > a.max_cells || d.cells > UWW_MAX_CELLS) return;
+    const unsigned long long ev = incl & kLbVertMax, ei = (incl >> 30) & kLbIndMax;
+    uint32_t over = 0;
+    for (uint32_t j = lo + lane; j < hi; j += 32) {
+        const uww_chunk_desc d = a.chunks[j];
         const int kind = bias_decides(p, (int)d.cells, d.pos[2] * p.chunk_size);
-        if (kind == 0) return;
-        if (t == 0) {
-            if (lane == 0) {
-                lookback_publish(a, 0u, 0ull);  // ticket 0: its inclusive prefix
-                decided_record(a, T, 0u, kind, 0ull);
-            }
-        } else if (T.npend < kMaxPending) {
-            if (lane == 0) {
-                lookback_publish(a, t, 0ull);
-                T.pend[T.npend] = t | ((uint32_t)kind << 30);
-                T.npend = T.npend + 1;
-            }
-        } else {
-            if (lane == 0) lookback_publish(a, t, 0ull);
-            __syncwarp();
-            const unsigned long long ex = lookback_warp(a, t, 0ull, &T.errflags);
-            if (lane == 0) decided_record(a, T, t, kind, ex);
-        }
-        __syncwarp();
+        over += decided_record(a, j, kind, ev, ei) ? 0u : 1u;
     }
-}
-
-// Control warp, after its last ticket: the pending records, in ticket order.
-__device__ void settle_pending(const BuildArgs& a, SmemTables& T)
-{
-    const int lane = threadIdx.x & 31;
-    for (uint32_t k = 0; k < T.npend; ++k) {
-        const uint32_t t = T.pend[k] & 0x3fffffffu;
-        const int kind = (int)(T.pend[k] >> 30);
-        const unsigned long long ex = lookback_warp(a, t, 0ull, &T.errflags);
-        if (lane == 0) decided_record(a, T, t, kind, ex);
-        __syncwarp();
-    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) over += __shfl_xor_sync(0xffffffffu, over, o);
+    if (lane == 0) T.overflow += over;
 }
 
 // MAXT/MINB: the launch bounds of an instantiation.  Chunks of up to 16 cells
@@ -821,16 +808,24 @@ __global__ void __launch_bounds__(MAXT, MINB) build_kernel(const DevParams p, co
         grad_vec(T.perm[i], gx, gy, gz);
         T.gp[i] = make_float4(gx, gy, gz, 0.f);
     }
+    // a planned batch reads the chunk list of the planning kernel launched
+    // just before it (as a programmatic dependent: the table setup above
+    // overlaps the planning)
+    if (QUEUE && a.plan) asm volatile("griddepcontrol.wait;" ::: "memory");
+    // the vertex pass, launched after this kernel as its programmatic
+    // dependent, may take SMs as this kernel's CTAs finish (it waits for the
+    // whole build before reading anything)
+    if (QUEUE) asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     if (tid == 0) {
         T.errflags = 0;
         T.overflow = 0;
-        T.n = a.n_dev ? min(*a.n_dev, a.n) : a.n;
-        T.npend = 0;
+        T.nchunks = a.n_dev ? min(*a.n_dev, a.n) : a.n;
+        T.n = (QUEUE && a.plan) ? __ldcg(&a.plan[kPlanCount]) : T.nchunks;
     }
     __syncthreads();
 
     if (!QUEUE) {
-        chunk_front<O, QUEUE>(p, a, T, dyn_smem, a.chunks[0], 0u, 0, ncomp, 0);
+        chunk_front<O, QUEUE>(p, a, T, dyn_smem, a.chunks[0], 0u, 0u, 0, ncomp);
         bar_sync(kBarCompute, ncomp);
         if (tid == 0) chunk_record(a, T, T.ci[0], 0ull, T.off[0], false);
         bar_sync(kBarCompute, ncomp);
@@ -845,43 +840,42 @@ __global__ void __launch_bounds__(MAXT, MINB) build_kernel(const DevParams p, co
 
     if (tid >= ncomp) {
         // ---- control warp ----
-        const bool decide = !a.samples_in && !a.samples_out && !((p.outputs & UWW_OUT_CASES) && a.cases) &&
-                            !a.no_depth_shortcut;
-        take_work_ticket(p, a, T, T.tk[0], decide);
+        take_ticket(a, T.n, T.tk[0]);
         for (int i = 0;; ++i) {
             bar_sync(kBarTicket, nthr);  // ticket i staged; chunk i-1's counts visible
             const bool valid = T.tk[i & 1].ticket < T.n;
-            // the look-back of chunk i-1 waits until chunk i's noise is done, so
-            // its predecessors have had a whole noise phase to publish
-            if (valid) bar_sync(kBarNoiseDone, nthr);
+            // the look-back of chunk i-1 runs while the compute warps sample
+            // chunk i, so its offsets are ready when they finish chunk i's
+            // front half
             if (i > 0) {
                 const ChunkInfo ci = T.ci[(i - 1) & 1];
-                const unsigned long long ex = lookback_warp(a, ci.ticket, pack_counts(ci.total), &T.errflags);
+                const unsigned long long own = pack_counts(ci.total);
+                const unsigned long long ex = lookback_warp(a, ci.ticket, own, &T.errflags);
                 if ((tid & 31) == 0) chunk_record(a, T, ci, ex, T.off[(i - 1) & 1], true);
                 __syncwarp();
                 bar_sync(kBarOffsets, nthr);
+                if (a.plan) {
+                    // the decided chunks up to the next listed one
+                    const uint32_t next = ci.ticket + 1 < T.n ? __ldcg(&a.plan[kPlanList + ci.ticket + 1]) : T.nchunks;
+                    decided_tail(p, a, T, ci.chunk + 1, next, sat_add_packed(ex, own));
+                }
             }
-            // take the next ticket only once chunk i-1 is emitted: a ticket's
-            // front half then starts as soon as it is taken, so the chunks
-            // that follow it in the queue do not wait on a late aggregate
             if (!valid) break;
-            if (i > 0) bar_sync(kBarEmitDone, nthr);
-            take_work_ticket(p, a, T, T.tk[(i + 1) & 1], decide);
+            // the next ticket, while chunk i-1 is emitted
+            take_ticket(a, T.n, T.tk[(i + 1) & 1]);
         }
-        settle_pending(a, T);
     } else {
         // ---- compute warps ----
         for (int i = 0;; ++i) {
             bar_sync(kBarTicket, nthr);
             const Ticket tk = T.tk[i & 1];
             const bool valid = tk.ticket < T.n;
-            if (valid) chunk_front<O, QUEUE>(p, a, T, dyn_smem, tk.desc, tk.ticket, i & 1, ncomp, nthr);
+            if (valid) chunk_front<O, QUEUE>(p, a, T, dyn_smem, tk.desc, tk.ticket, tk.chunk, i & 1, ncomp);
             bar_sync(kBarCompute, ncomp);
             if (i > 0) {
                 bar_sync(kBarOffsets, nthr);
                 chunk_emit<O, QUEUE>(p, a, T, dyn_smem, (i - 1) & 1, T.off[(i - 1) & 1], ncomp);
                 bar_sync(kBarCompute, ncomp);  // workspace (i-1)&1 is reused by chunk i+1
-                if (valid) bar_arrive(kBarEmitDone, nthr);
             }
             if (!valid) break;
         }
@@ -919,15 +913,101 @@ __global__ void __launch_bounds__(MAXT, MINB) build_kernel(const DevParams p, co
     }
 }
 
+// Planning pass of a batched build: the chunks the build kernel must take,
+// in chunk order, into plan[1..n] and their number into plan[0].  A chunk
+// whose depth bias alone decides every sample (bias_decides, the same test
+// the build applies) needs neither noise nor mesh and is left out; a
+// descriptor the build will flag as bad is listed.  Every CTA decides a slice
+// of the batch (one descriptor per thread, so the reads are spread over the
+// SMs) into one byte per chunk; the last CTA to finish compacts the bytes in
+// chunk order, writes the records of the decided chunks before the first
+// listed chunk (prefix 0; the build writes the others after the listed chunk
+// before them) and re-arms the finish counter for the next launch.
+constexpr int kPlanThreads = 256;
+constexpr int kPlanPerThread = 16;  // chunks per thread in the compaction
+
+__device__ __forceinline__ uint8_t* plan_kinds(uint32_t* plan, uint32_t n)
+{
+    return reinterpret_cast<uint8_t*>(plan) + plan_kinds_offset(n);
+}
+
+__global__ void __launch_bounds__(kPlanThreads) plan_kernel(const DevParams p, const BuildArgs a)
+{
+    // the build kernel may start its table setup now; it waits for this
+    // grid's writes (griddepcontrol.wait) before reading the list
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    __shared__ uint32_t warp_count[kPlanThreads / 32];
+    __shared__ uint32_t base;
+    __shared__ int last;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint32_t n = a.n_dev ? min(*a.n_dev, a.n) : a.n;
+    uint8_t* kinds = plan_kinds(a.plan, a.n);
+    const float B = fbm_bound(p);
+    for (uint32_t i = blockIdx.x * kPlanThreads + tid; i < n; i += gridDim.x * kPlanThreads) {
+        const uint32_t cells = __ldg(&a.chunks[i].cells);
+        const int oz = __ldg(&a.chunks[i].pos[2]) * p.chunk_size;
+        const bool ok = cells >= 1 && cells <= a.max_cells && cells <= UWW_MAX_CELLS;
+        kinds[i] = ok ? (uint8_t)bias_decides_with(p, B, __fdiv_rn((float)p.chunk_size, (float)cells), (int)cells, oz)
+                      : (uint8_t)0;
+    }
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) last = atomicAdd(&a.plan[kPlanDone], 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    // the last CTA: compact, in chunk order
+    if (tid == 0) base = 0;
+    __syncthreads();
+    constexpr uint32_t kTile = (uint32_t)kPlanThreads * kPlanPerThread;
+    for (uint32_t t0 = 0; t0 < n; t0 += kTile) {
+        const uint32_t i0 = t0 + (uint32_t)tid * kPlanPerThread;
+        unsigned mine = 0;  // bit k: chunk i0 + k is listed
+#pragma unroll
+        for (int k = 0; k < kPlanPerThread; ++k)
+            if (i0 + k < n && __ldcg(&kinds[i0 + k]) == 0) mine |= 1u << k;
+        const uint32_t cnt = __popc(mine);
+        uint32_t incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        if (lane == 31) warp_count[warp] = incl;
+        __syncthreads();
+        uint32_t before = 0, total = 0;
+#pragma unroll
+        for (int w = 0; w < kPlanThreads / 32; ++w) {
+            const uint32_t v = warp_count[w];
+            before += w < warp ? v : 0u;
+            total += v;
+        }
+        uint32_t pos = kPlanList + base + before + incl - cnt;
+        for (int k = 0; k < kPlanPerThread; ++k)
+            if (mine & (1u << k)) a.plan[pos++] = i0 + k;
+        __syncthreads();
+        if (tid == 0) base += total;
+        __syncthreads();
+    }
+    const uint32_t count = base;
+    if (tid == 0) {
+        a.plan[kPlanCount] = count;
+        a.plan[kPlanDone] = 0u;  // re-armed for the next launch
+    }
+    const uint32_t first = count ? a.plan[kPlanList] : n;  // written by this CTA before the last barrier
+    for (uint32_t j = tid; j < first; j += kPlanThreads) decided_record(a, j, __ldcg(&kinds[j]), 0ull, 0ull);
+}
+
 // Pass 2 of the batched build over every vertex of the batch: vertex counts
 // are very uneven across chunks, so the per-vertex colour and analytic-normal
 // work is spread over the whole GPU instead of staying with the CTA that
 // built the chunk.  The vertex count is read from totals[0].
+// totals and verts are written by the build kernel this one may overlap (a
+// programmatic dependent): neither is read through the read-only path, and
+// nothing is read before griddepcontrol.wait.
 template <class O>
-__global__ void __launch_bounds__(256) vertex_kernel(const DevParams p, uww_vert_color* __restrict__ verts,
-                                                     float* __restrict__ normals,
-                                                     const unsigned long long* __restrict__ totals,
-                                                     uint32_t vert_capacity)
+__global__ void __launch_bounds__(256) vertex_kernel(const DevParams p, uww_vert_color* verts, float* normals,
+                                                     const unsigned long long* totals, uint32_t vert_capacity)
 {
     __shared__ __align__(16) uint8_t P[256];
     __shared__ float4 gp[256];
@@ -940,7 +1020,9 @@ __global__ void __launch_bounds__(256) vertex_kernel(const DevParams p, uww_vert
         gp[i] = make_float4(gx, gy, gz, 0.f);
     }
     __syncthreads();
-    const uint32_t nv = (uint32_t)min(*totals, (unsigned long long)vert_capacity);
+    // launched as a programmatic dependent of the build: wait for all of it
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    const uint32_t nv = (uint32_t)min(__ldcg(totals), (unsigned long long)vert_capacity);
     const bool want_color = (p.outputs & UWW_OUT_COLOR) != 0;
     const bool want_normals = (p.outputs & UWW_OUT_NORMALS) != 0 && normals != nullptr;
     for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += gridDim.x * blockDim.x)
@@ -985,6 +1067,7 @@ __global__ void density_kernel(const DevParams p, const float* __restrict__ xyz,
 }
 
 using BuildFn = void (*)(const DevParams, const BuildArgs);
+using VertexFn = void (*)(const DevParams, uww_vert_color*, float*, const unsigned long long*, uint32_t);
 
 // [exact][queue][large]
 BuildFn kernel_for(bool exact, bool queue, bool large)
@@ -1034,19 +1117,51 @@ cudaError_t launch_build(const DevParams& p, const BuildArgs& a, bool queue, int
                          cudaStream_t s)
 {
     const bool exact = p.math_mode == UWW_MATH_EXACT;
-    kernel_for(exact, queue, threads > 224)<<<grid, threads, dyn_smem, s>>>(p, a);
-    cudaError_t e = cudaGetLastError();
+    cudaError_t e = cudaSuccess;
+    if (queue && a.plan) {
+        // the planning kernel, then the build as its programmatic dependent
+        const uint32_t nblk = std::max(1u, std::min((a.n + kPlanThreads - 1) / kPlanThreads, 1024u));
+        plan_kernel<<<nblk, kPlanThreads, 0, s>>>(p, a);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)grid);
+        cfg.blockDim = dim3((unsigned)threads);
+        cfg.dynamicSmemBytes = dyn_smem;
+        cfg.stream = s;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        e = cudaLaunchKernelEx(&cfg, kernel_for(exact, queue, threads > 224), p, a);
+    } else {
+        kernel_for(exact, queue, threads > 224)<<<grid, threads, dyn_smem, s>>>(p, a);
+        e = cudaGetLastError();
+    }
     // streamed host output finishes its vertices inside the build kernel
     if (e != cudaSuccess || !queue || a.host_verts || !(p.outputs & (UWW_OUT_COLOR | UWW_OUT_NORMALS))) return e;
-    // the batched form's pass 2, over the whole batch
+    // the batched form's pass 2, over the whole batch: one wave of resident
+    // CTAs striding over the vertices, launched as a programmatic dependent
+    // of the build so that its launch and table setup overlap the build's
+    // last CTAs
     int dev = 0, sms = 0;
     e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
-    const int vgrid = std::max(1, sms * 8);
-    if (exact) vertex_kernel<ExactOps><<<vgrid, 256, 0, s>>>(p, a.verts, a.normals, a.totals, a.vert_capacity);
-    else vertex_kernel<FastOps><<<vgrid, 256, 0, s>>>(p, a.verts, a.normals, a.totals, a.vert_capacity);
-    return cudaGetLastError();
+    const VertexFn vfn = exact ? vertex_kernel<ExactOps> : vertex_kernel<FastOps>;
+    int vbps = 0;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&vbps, vfn, 256, 0)) != cudaSuccess) return e;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)std::max(1, sms * std::max(1, vbps)));
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, vfn, p, a.verts, a.normals, (const unsigned long long*)a.totals, a.vert_capacity);
 }
 
 cudaError_t launch_copy_out(const CopyOut& c, const unsigned long long* totals, int blocks_x, cudaStream_t s)

@@ -43,12 +43,21 @@ __host__ __device__ inline ChunkLayout chunk_layout(int N)
 }
 
 // Bytes of the fast build's per-chunk z tables for S samples per edge:
-// (dz, fade) and (first z, cell) per octave and z, run counts, z bias.
+// (dz, fade) and (first z, cell) per octave and z, run counts, z bias, run
+// start masks.
 __host__ __device__ inline size_t ztable_bytes(int S, int octaves)
 {
     return (size_t)octaves * S * (sizeof(float2) + sizeof(int2)) + (size_t)octaves * sizeof(int) +
-           (size_t)S * sizeof(float) + 16;
+           (size_t)S * sizeof(float) + (size_t)octaves * sizeof(unsigned) + 16;
 }
+
+// Plan buffer of a planned batched build of n chunks: u32 [0] the planning
+// kernel's finish counter (zero between launches, at a fixed place whatever
+// n), [1] the number of listed chunks, [2 .. n+1] the listed chunks in
+// order, then one decision byte per chunk.
+constexpr uint32_t kPlanDone = 0, kPlanCount = 1, kPlanList = 2;
+__host__ __device__ inline size_t plan_kinds_offset(uint32_t n) { return ((size_t)n + kPlanList) * sizeof(uint32_t); }
+__host__ __device__ inline size_t plan_buffer_bytes(uint32_t n) { return plan_kinds_offset(n) + n; }
 
 // Lookback word: [63:62] status, [61:30] indices, [29:0] vertices.
 constexpr unsigned long long kLbAggregate = 1ull << 62;
@@ -92,6 +101,7 @@ struct BuildArgs {
     uint32_t no_depth_shortcut;      // UWW_TUNE_NO_DEPTH_SHORTCUT: every chunk evaluates its noise
     uint32_t* edge_ids;              // optional, per output vertex: (first corner sample << 3) | direction
     const uint32_t* n_dev;           // optional device chunk count; the launch builds min(*n_dev, n)
+    uint32_t* plan;                  // planned batch: finish counter, count, list (plan_kernel; kPlan*)
     // Optional streamed host output (batched form): device addresses of
     // page-locked host memory.  Pass 2 then runs inside the build kernel, and
     // each chunk's record, indices, vertices and normals go there as soon as
@@ -186,6 +196,8 @@ struct uww_ctx {
     // device work state
     unsigned long long* d_lookback = nullptr;
     size_t lookback_cap = 0;
+    uint32_t* d_plan = nullptr;   // planned batch: chunk count + list
+    size_t plan_cap = 0;
     unsigned long long* d_state = nullptr;
     unsigned int* d_counter = nullptr;
     unsigned long long* d_acc = nullptr;

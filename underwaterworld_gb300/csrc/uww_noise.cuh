@@ -11,13 +11,10 @@ namespace uww {
 namespace {
 
 // Named barriers: 0 = whole CTA, 1 = compute warps, 2 = ticket hand-off,
-// 3 = offsets hand-off, 4 = noise done, 5 = emission done (2-5: compute
-// warps + control warp).
+// 3 = offsets hand-off (2-3: compute warps + control warp).
 constexpr int kBarCompute = 1;
 constexpr int kBarTicket = 2;
 constexpr int kBarOffsets = 3;
-constexpr int kBarNoiseDone = 4;  // compute warps arrive (no wait) once a chunk's noise is done
-constexpr int kBarEmitDone = 5;   // compute warps arrive (no wait) once the previous chunk is emitted
 
 __device__ __forceinline__ void bar_arrive(int id, int count)
 {
@@ -136,8 +133,8 @@ constexpr float kPerlinBound = 1.11f;
 __device__ __forceinline__ float fbm_bound(const DevParams& p)
 {
     float sa = 0.f;
-    for (int k = 0; k < p.octaves; ++k) sa += fabsf(p.amp[k]);
-    return kPerlinBound * fabsf(fbm_norm(p)) * sa;
+    for (int k = 0; k < p.octaves; ++k) sa = __fadd_rn(sa, fabsf(p.amp[k]));
+    return __fmul_rn(__fmul_rn(kPerlinBound, fabsf(fbm_norm(p))), sa);
 }
 
 // Whether the depth bias alone decides every sample of a chunk with N cells
@@ -145,10 +142,12 @@ __device__ __forceinline__ float fbm_bound(const DevParams& p)
 // early blank chunk), 2 when every sample is below it (every case 255), 0
 // otherwise.  The margin covers f32 rounding and, for the terraced bias, a
 // step of the staircase (the parity and fast builds may round the depth to
-// either side of a step).
-__device__ __forceinline__ int bias_decides(const DevParams& p, int N, int oz)
+// either side of a step).  Every operation is explicitly rounded, so the
+// planning kernel and the build kernel reach the same decision.
+// B = fbm_bound(p) and s = chunk_size / N passed in (per-launch and per-LOD
+// constants).
+__device__ __forceinline__ int bias_decides_with(const DevParams& p, float B, float s, int N, int oz)
 {
-    const float s = __fdiv_rn((float)p.chunk_size, (float)N);
     float lo = 3.0e38f, hi = -3.0e38f;
     bool ok = true;
     // the linear bias is monotonic in z: its ends suffice
@@ -159,13 +158,18 @@ __device__ __forceinline__ int bias_decides(const DevParams& p, int N, int oz)
         lo = fminf(lo, b);
         hi = fmaxf(hi, b);
     }
-    const float B = fbm_bound(p), iso = p.iso_level;
+    const float iso = p.iso_level;
     if (!ok || !(B < 1.0e30f) || !(fabsf(iso) < 1.0e30f)) return 0;
-    float m = 1.0e-3f * (1.f + B + fmaxf(fabsf(lo), fabsf(hi)));
-    if (p.bias_mode == UWW_BIAS_TERRACED) m += fabsf(p.bias_c);
-    if (lo - B - m > iso) return 1;
-    if (hi + B + m < iso) return 2;
+    float m = __fmul_rn(1.0e-3f, __fadd_rn(__fadd_rn(1.f, B), fmaxf(fabsf(lo), fabsf(hi))));
+    if (p.bias_mode == UWW_BIAS_TERRACED) m = __fadd_rn(m, fabsf(p.bias_c));
+    if (__fsub_rn(__fsub_rn(lo, B), m) > iso) return 1;
+    if (__fadd_rn(__fadd_rn(hi, B), m) < iso) return 2;
     return 0;
+}
+
+__device__ __forceinline__ int bias_decides(const DevParams& p, int N, int oz)
+{
+    return bias_decides_with(p, fbm_bound(p), __fdiv_rn((float)p.chunk_size, (float)N), N, oz);
 }
 
 // noise coordinate of a column: (i s + o + offset) f
@@ -236,10 +240,11 @@ __device__ __forceinline__ float run_value(const RunPoly& q, float2 t)
 }
 
 struct ZTable {
-    float2* dzc;   // [octave][z]: (dz, fade(dz))
-    int2* runs;    // [octave][run]: (first z, z lattice cell)
-    int* nruns;    // [octave]
-    float* bias;   // [z]
+    float2* dzc;      // [octave][z]: (dz, fade(dz))
+    int2* runs;       // [octave][run]: (first z, z lattice cell)
+    int* nruns;       // [octave]
+    float* bias;      // [z]
+    unsigned* rmask;  // [octave]: bit z set where a run starts (S <= 32)
 };
 
 __device__ __forceinline__ ZTable ztable_at(uint8_t* base, int S, int octaves)
@@ -250,7 +255,100 @@ __device__ __forceinline__ ZTable ztable_at(uint8_t* base, int S, int octaves)
     t.nruns = reinterpret_cast<int*>(base + (size_t)octaves * S * (sizeof(float2) + sizeof(int2)));
     t.bias = reinterpret_cast<float*>(base + (size_t)octaves * S * (sizeof(float2) + sizeof(int2)) +
                                       (size_t)octaves * sizeof(int));
+    t.rmask = reinterpret_cast<unsigned*>(base + (size_t)octaves * S * (sizeof(float2) + sizeof(int2)) +
+                                          (size_t)octaves * sizeof(int) + (size_t)S * sizeof(float));
     return t;
+}
+
+// The z tables of one chunk of S <= 32 samples per edge, one warp per octave:
+// lane z computes its entry and its predecessor's lattice cell, a ballot
+// marks the run starts, and each start is written to its run slot.  The same
+// entries and runs as the serial compaction of sample_columns_fast.  Every
+// compute thread calls it; the caller synchronises the compute warps after.
+__device__ __forceinline__ void ztable_warps(const DevParams& p, const ZTable Z, int S, float s, float zoff, int oz,
+                                             int ncomp)
+{
+    const int K = p.octaves, lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = ncomp >> 5;
+    for (int k = warp; k < K; k += nwarps) {
+        float dz, fd, dzp, fdp;
+        int cell, cellp;
+        z_entry(p, k, lane, s, zoff, dz, fd, cell);
+        z_entry(p, k, lane - 1, s, zoff, dzp, fdp, cellp);
+        const bool on = lane < S;
+        const unsigned m = __ballot_sync(0xffffffffu, on && (lane == 0 || cellp != cell));
+        if (on) Z.dzc[k * S + lane] = make_float2(dz, fd);
+        if ((m >> lane) & 1u) Z.runs[k * S + __popc(m & ((1u << lane) - 1u))] = make_int2(lane, cell);
+        if (lane == 0) {
+            Z.nruns[k] = __popc(m);
+            Z.rmask[k] = m;
+        }
+    }
+    for (int z = threadIdx.x; z < S; z += ncomp) Z.bias[z] = z_bias(p, z, s, oz);
+}
+
+// sample_columns_fast for chunks of S samples per edge (a compile-time S <=
+// 32) in shared memory: each thread's column is accumulated in registers,
+// over a fully unrolled z loop whose run starts are uniform branches, and
+// written to rho once.  Operation for operation the arithmetic of
+// sample_columns_fast (and of the sampling kernel), so the samples are the
+// same bits.  Returns the same votes.  Every compute thread must call it.
+template <int S>
+__device__ __forceinline__ int sample_columns_reg(const DevParams& p, const uint8_t* __restrict__ P,
+                                                  const float4* __restrict__ gp, const ZTable Z,
+                                                  float* __restrict__ rho, int ox, int oy, int oz, int ncomp)
+{
+    constexpr int SS = S * S;
+    const int K = p.octaves;
+    const float s = __fdiv_rn((float)p.chunk_size, (float)(S - 1));
+    const float bf = p.base_freq;
+    const float norm = fbm_norm(p);
+    const float zoff = __fadd_rn((float)oz, p.offset[2]);
+    const float iso = p.iso_level;
+    ztable_warps(p, Z, S, s, zoff, oz, ncomp);
+    bar_sync(kBarCompute, ncomp);
+
+    int inside = 0, outside = 0;
+    for (int col = threadIdx.x; col < SS; col += ncomp) {
+        const int x = col / S, y = col - x * S;
+        const float nx = column_coord((float)x, s, ox, p.offset[0], bf);
+        const float ny = column_coord((float)y, s, oy, p.offset[1], bf);
+        float acc[S];
+#pragma unroll
+        for (int z = 0; z < S; ++z) acc[z] = Z.bias[z];
+        for (int k = 0; k < K; ++k) {
+            const ColumnOctave co = column_octave(p, P, nx, ny, k, norm);
+            const unsigned rm = Z.rmask[k];
+            const int2* runs = Z.runs + k * S;
+            const float2* dzc = Z.dzc + k * S;
+            float SA0 = 0.f, SG0 = 0.f, SA1 = 0.f, SG1 = 0.f;
+            RunPoly q = {0.f, 0.f, 0.f, 0.f};
+            int prev = 0, r = 0;
+#pragma unroll
+            for (int z = 0; z < S; ++z) {
+                if (rm & (1u << z)) {  // the same for every column
+                    const int c = runs[r++].y;
+                    if (z > 0 && c == prev + 1) {
+                        SA0 = SA1;
+                        SG0 = SG1;
+                    } else {
+                        column_face(co, gp, c & 255, SA0, SG0);
+                    }
+                    column_face(co, gp, (c + 1) & 255, SA1, SG1);
+                    prev = c;
+                    q = run_poly(SA0, SG0, SA1, SG1);
+                }
+                acc[z] = __fadd_rn(run_value(q, dzc[z]), acc[z]);
+            }
+        }
+        float* out = rho + col * S;
+#pragma unroll
+        for (int z = 0; z < S; ++z) {
+            out[z] = acc[z];
+            inside |= !(acc[z] > iso);
+            outside |= !(acc[z] < iso);
+        }
+    }
+    return inside | (outside << 1);
 }
 
 // Returns bit 0: a sample of this thread's columns is not above the iso
