@@ -323,6 +323,16 @@ struct Workspace {
     }
 };
 
+// Whether a chunk's emission finds each triangle's cell in a triangle map
+// rather than by a search over its active cells: chunks of up to 16 cells per
+// edge with 16-bit index positions and no more triangles than cells, whose
+// map (x | y << 4 | z << 8 | row << 12 per triangle) fits in the ibase array.
+__device__ __forceinline__ bool direct_triangles(const Workspace& W, int N, unsigned long long total)
+{
+    const uint32_t nT = (uint32_t)((total >> kIndShift) & kField22) / 3u;
+    return N <= 16 && W.idx16 && nT <= (uint32_t)(N * N * N);
+}
+
 __device__ __forceinline__ Workspace workspace(const BuildArgs& a, uint8_t* dyn_smem, int buf, int N)
 {
     const ChunkLayout L = chunk_layout(N);
@@ -434,6 +444,10 @@ __device__ void chunk_front(const DevParams& p, const BuildArgs& a, SmemTables& 
         // ---- classify + count, contiguous runs of cells per thread ----
         const int R = (NC + ncomp - 1) / ncomp;
         const int c0 = min(tid * R, NC), c1 = min(c0 + R, NC);
+        // up to 16 cells of a run keep their counts in registers for the
+        // second pass, 8 bits a cell: triangles | new vertices << 3
+        const bool keep = R <= 16;
+        unsigned long long kept0 = 0ull, kept1 = 0ull;
         unsigned long long mine = 0ull;
         {
             int x = c0 / (N * N), y = (c0 / N) % N, z = c0 % N;
@@ -470,6 +484,11 @@ __device__ void chunk_front(const DevParams& p, const BuildArgs& a, SmemTables& 
                     const unsigned own = T.owned[oriented][boundary_flags(x, y, z, N)];
                     const unsigned nv = __popc(T.edges[cs] & own);
                     mine += (unsigned long long)nv | ((unsigned long long)(3 * nt) << kIndShift) | (1ull << kActShift);
+                    if (keep) {
+                        const int i = c - c0;
+                        const unsigned long long v = (unsigned long long)(nt | (nv << 3)) << (8 * (i & 7));
+                        if (i < 8) kept0 |= v; else kept1 |= v;
+                    }
                 }
                 if (++z == N) { z = 0; if (++y == N) { y = 0; ++x; } }
             }
@@ -477,37 +496,52 @@ __device__ void chunk_front(const DevParams& p, const BuildArgs& a, SmemTables& 
         unsigned long long run = block_exclusive_scan(mine, T, total, ncomp);
         // publish the aggregate as soon as the counts are known
         if (QUEUE && tid == 0) lookback_publish(a, ticket, pack_counts(total));
+        const bool direct = direct_triangles(W, N, total);
         {
-            // second pass over the same runs: each cell's first vertex id and
-            // the active-cell list with its first index position
+            // second pass over the same runs: each active cell's first vertex
+            // id (only active cells need one: every owner cell of a crossed
+            // edge is active) and where its triangles go -- the triangle map
+            // (direct), else the active-cell list with first index positions
             int x = c0 / (N * N), y = (c0 / N) % N, z = c0 % N;
             unsigned long long m00 = 0, m10 = 0, m01 = 0, m11 = 0;
             int mcol = -1;
             for (int c = c0; c < c1; ++c) {
-                int cs;
-                if (masks) {
-                    // the case again from the masks (no read of the global cases); only
-                    // active cells need a first vertex id: every owner cell of a crossed
-                    // edge is active
-                    const int col = x * S + y;
-                    if (col != mcol) {
-                        m00 = masks[col]; m10 = masks[col + S]; m01 = masks[col + 1]; m11 = masks[col + S + 1];
-                        mcol = col;
-                    }
-                    cs = mask_case(m00, m10, m01, m11, z);
+                int nt;
+                unsigned nv;
+                if (keep) {
+                    const int i = c - c0;
+                    const unsigned v = (unsigned)(((i < 8 ? kept0 : kept1) >> (8 * (i & 7))) & 0xffu);
+                    nt = (int)(v & 7u);
+                    nv = v >> 3;
                 } else {
-                    cs = cases[c];
-                    W.set_vbase(c, (uint32_t)(run & kField22));
+                    int cs;
+                    if (masks) {
+                        // the case again from the masks (no read of the global cases)
+                        const int col = x * S + y;
+                        if (col != mcol) {
+                            m00 = masks[col]; m10 = masks[col + S]; m01 = masks[col + 1]; m11 = masks[col + S + 1];
+                            mcol = col;
+                        }
+                        cs = mask_case(m00, m10, m01, m11, z);
+                    } else {
+                        cs = cases[c];
+                    }
+                    nt = T.ntri[cs];
+                    nv = nt ? __popc(T.edges[cs] & T.owned[oriented][boundary_flags(x, y, z, N)]) : 0u;
                 }
-                const int nt = T.ntri[cs];
                 if (nt) {
-                    if (masks) W.set_vbase(c, (uint32_t)(run & kField22));
-                    const uint32_t ar = (uint32_t)(run >> kActShift);
-                    W.set_active(ar, c);
-                    W.set_ibase(ar, (uint32_t)((run >> kIndShift) & kField22));
-                    const unsigned own = T.owned[oriented][boundary_flags(x, y, z, N)];
-                    run += (unsigned long long)__popc(T.edges[cs] & own) | ((unsigned long long)(3 * nt) << kIndShift) |
-                           (1ull << kActShift);
+                    W.set_vbase(c, (uint32_t)(run & kField22));
+                    const uint32_t ir = (uint32_t)((run >> kIndShift) & kField22);
+                    if (direct) {
+                        uint16_t* tmap = reinterpret_cast<uint16_t*>(W.ibase) + ir / 3u;
+                        const unsigned xyz = (unsigned)x | ((unsigned)y << 4) | ((unsigned)z << 8);
+                        for (int k = 0; k < nt; ++k) tmap[k] = (uint16_t)(xyz | ((unsigned)k << 12));
+                    } else {
+                        const uint32_t ar = (uint32_t)(run >> kActShift);
+                        W.set_active(ar, c);
+                        W.set_ibase(ar, ir);
+                    }
+                    run += (unsigned long long)nv | ((unsigned long long)(3 * nt) << kIndShift) | (1ull << kActShift);
                 }
                 if (++z == N) { z = 0; if (++y == N) { y = 0; ++x; } }
             }
@@ -620,22 +654,35 @@ __device__ void chunk_emit(const DevParams& p, const BuildArgs& a, SmemTables& T
         // triangle's cell is the last active cell whose first index position
         // is at or before it
         const uint32_t nT = (uint32_t)((ci.total >> kIndShift) & kField22) / 3u;
+        const bool direct = direct_triangles(W, N, ci.total);
         for (uint32_t t = tid; t < nT; t += ncomp) {
             const uint32_t g = 3u * t;
-            uint32_t ai = 0, len = nA;
-            while (len > 1) {
-                const uint32_t h = len >> 1;
-                if (W.get_ibase(ai + h) <= g) ai += h;
-                len -= h;
+            int c, x, y, z, j0;
+            if (direct) {
+                const unsigned e = reinterpret_cast<const uint16_t*>(W.ibase)[t];
+                x = (int)(e & 15u);
+                y = (int)((e >> 4) & 15u);
+                z = (int)((e >> 8) & 15u);
+                j0 = 3 * (int)(e >> 12);
+                c = (x * N + y) * N + z;
+            } else {
+                uint32_t ai = 0, len = nA;
+                while (len > 1) {
+                    const uint32_t h = len >> 1;
+                    if (W.get_ibase(ai + h) <= g) ai += h;
+                    len -= h;
+                }
+                c = W.get_active(ai);
+                x = c / (N * N);
+                y = (c / N) % N;
+                z = c % N;
+                j0 = (int)(g - W.get_ibase(ai));
             }
-            const int c = W.get_active(ai);
-            const int x = c / (N * N), y = (c / N) % N, z = c % N;
             const int cs = cases[c];
             const int8_t* row = T.tri[cs];
             const unsigned own_mask = T.owned[oriented][boundary_flags(x, y, z, N)];
             const unsigned fr = T.first_ref[cs];
             const uint32_t vb = W.get_vbase(c);
-            const int j0 = (int)(g - W.get_ibase(ai));
             const uint16_t* before = UWW_EDGE_BEFORE[cs];
 #pragma unroll
             for (int m = 0; m < 3; ++m) {
