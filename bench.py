@@ -580,11 +580,16 @@ def leg_terrain_fit(stream, steps=200):
     tfb = statistics.mean([timed(stream, fb) for _ in range(5)])
     cells = len(d) * 16 ** 3
     rmse0, rmse1 = float(np.sqrt(losses[0])), float(np.sqrt(losses[-1]))
+    g = fit.last_grad
     ctx.close()
+    tail = losses[-20:]
     return {"cells": cells, "steps": steps, "seconds": el, "step_ms": 1e3 * el / steps,
             "fwd_bwd_ms": 1e3 * tfb, "fwd_adjoint_mvoxels_per_s": cells / tfb / 1e6,
             "loss_first": losses[0], "loss_last": losses[-1], "rms_height_error_first": rmse0,
-            "rms_height_error_last": rmse1, "peak_device_bytes": int(free0 - min_free)}
+            "rms_height_error_last": rmse1, "peak_device_bytes": int(free0 - min_free),
+            "final_grad_norm": float(np.linalg.norm(g)),
+            "final_scaled_grad_norm": float(np.linalg.norm(g * fit.scale)),
+            "loss_change_last_20_steps": float((tail[-1] - tail[0]) / tail[0])}
 
 
 def leg_queries(stream, flush, steps):

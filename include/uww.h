@@ -334,7 +334,10 @@ int uww_backward(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint3
  * (x0, y0), cols_x by cols_y; L = sum over columns holding a vertex of
  * (mean vertex z - d_target[col])^2 / (cols_x * cols_y), col = cy * cols_x + cx.
  * Writes *d_loss and d_pos_grad = dL/d(position) (3 floats per vertex);
- * d_work: 2 * cols_x * cols_y floats of scratch.  Asynchronous. */
+ * d_work: 4 * cols_x * cols_y floats of scratch, 8-byte aligned.  The column
+ * sums are fixed point (2^-16 world units) with order-independent integer
+ * atomics and the loss is reduced in a fixed order, so the result does not
+ * change from run to run.  Asynchronous. */
 int uww_height_loss(uww_ctx* ctx, const uww_vert_color* d_verts, const uint64_t* d_totals, uint32_t vert_capacity,
                     float x0, float y0, float column, uint32_t cols_x, uint32_t cols_y, const float* d_target,
                     float* d_work, float* d_pos_grad, float* d_loss);

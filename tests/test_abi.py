@@ -96,7 +96,7 @@ def test_totals_status_maps_every_error_flag():
 
 
 def test_rust_binding_declares_every_entry_point():
-    """The extern "C" block a Rust host adds declares every
+    """The Rust `extern "C"` block of the integration guide declares every
     function of include/uww.h, each once."""
     import re
     from pathlib import Path

@@ -207,7 +207,7 @@ def test_height_loss_matches_numpy(ctx_factory):
     cols, col = 4, 16.0
     target = gaussian_heightmap(cols, col, seed=1, base=20.0)
     d_t = ctx.upload(target)
-    d_work, d_loss = DeviceArray(2 * cols * cols * 4), DeviceArray(4)
+    d_work, d_loss = DeviceArray(4 * cols * cols * 4), DeviceArray(4)
     abi.check(abi.lib().uww_height_loss(ctx.h, C.c_void_p(a.d_verts.ptr), C.c_void_p(a.d_tot.ptr), a.vcap, 0.0, 0.0,
                                         col, cols, cols, C.c_void_p(d_t.ptr), C.c_void_p(d_work.ptr),
                                         C.c_void_p(a.d_pos_grad.ptr), C.c_void_p(d_loss.ptr)))
@@ -239,3 +239,44 @@ def test_terrain_fit_reduces_the_loss(ctx_factory):
     res = fit.run(30)
     assert np.all(np.isfinite(res["losses"]))
     assert min(res["losses"][-5:]) < 0.7 * res["losses"][0], res["losses"]
+
+
+def test_terrain_fit_state_round_trips_through_a_checkpoint_file(tmp_path):
+    """The fit's state (theta0, scales, phi, Adam moments and step count,
+    learning rate) survives save/load unchanged.  No GPU: the state is set
+    on an instance without a context."""
+    fit = TerrainFit.__new__(TerrainFit)
+    rng = np.random.default_rng(3)
+    fit.theta0, fit.scale, fit.phi = rng.normal(size=13), rng.uniform(0.1, 2, 13), rng.normal(size=13)
+    fit.m, fit.v, fit.t, fit.lr = rng.normal(size=13), rng.uniform(0, 1, 13), 17, 0.01
+    path = tmp_path / "fit.npz"
+    fit.save(path)
+    other = TerrainFit.__new__(TerrainFit)
+    other.theta0 = np.zeros(13)
+    other.load(path)
+    for k, v in fit.state_dict().items():
+        np.testing.assert_array_equal(np.asarray(other.state_dict()[k]), np.asarray(v), err_msg=k)
+    wrong = TerrainFit.__new__(TerrainFit)
+    wrong.theta0 = np.zeros(9)
+    with pytest.raises(ValueError):
+        wrong.load(path)
+
+
+@pytest.mark.gpu
+def test_terrain_fit_resumes_from_a_checkpoint(ctx_factory, tmp_path):
+    """Ten steps straight equal five steps, a checkpoint, and five more steps
+    of a new fit loaded from it: forward, heightmap loss and backward are
+    deterministic, so the losses and theta agree bit for bit."""
+    p, descs = terrain_volume(chunks_per_edge=4, cells=16, octaves=4)
+    target = gaussian_heightmap(2, 32.0, n_bumps=2, seed=4, sigma=(10.0, 30.0), height=(5.0, 15.0), base=24.0)
+    kw = dict(vert_capacity=1 << 20, ind_capacity=1 << 22, lr=2e-2)
+    straight = TerrainFit(ctx_factory(p.copy()), descs, target, 32.0, **kw).run(10)
+    ck = tmp_path / "fit.npz"
+    first = TerrainFit(ctx_factory(p.copy()), descs, target, 32.0, **kw)
+    head = first.run(5, checkpoint=ck, every=5)
+    resumed = TerrainFit(ctx_factory(p.copy()), descs, target, 32.0, **kw)
+    resumed.load(ck)
+    tail = resumed.run(5)
+    assert head["losses"] + tail["losses"] == straight["losses"]
+    np.testing.assert_array_equal(tail["theta"], straight["theta"])
+    assert np.isfinite(tail["grad_norm"])

@@ -160,7 +160,7 @@ class TerrainFit:
         self.column = float(column)
         self.origin = origin
         self.d_target = ctx.upload(np.ascontiguousarray(target, dtype=np.float32))
-        self.d_work = DeviceArray(2 * target.size * 4)
+        self.d_work = DeviceArray(4 * target.size * 4)
         self.d_loss = DeviceArray(4)
         self.theta0 = theta_from_params(ctx.params).astype(np.float64)
         K = int(ctx.params.octaves)
@@ -216,16 +216,57 @@ class TerrainFit:
         mh = self.m / (1 - b1 ** self.t)
         vh = self.v / (1 - b2 ** self.t)
         self.phi = self.phi - self.lr * mh / (np.sqrt(vh) + eps)
+        self.last_grad = g
         return loss, g
 
-    def run(self, steps: int) -> dict:
+    # ---- checkpoint / resume ---------------------------------------------------
+    # A chunk's mesh is a function of (parameters, seed, position) alone -- the
+    # reference regenerates chunks from them (world.rs:236-247) -- so the fit's
+    # whole state is theta's parametrisation and Adam's moments.
+    def state_dict(self) -> dict:
+        """Everything a resumed fit needs: theta0, the per-entry scales, phi,
+        Adam's moments and step count, the learning rate."""
+        return {"theta0": self.theta0.copy(), "scale": self.scale.copy(), "phi": self.phi.copy(),
+                "m": self.m.copy(), "v": self.v.copy(), "t": np.int64(self.t), "lr": np.float64(self.lr)}
+
+    def load_state_dict(self, st: dict) -> None:
+        theta0 = np.asarray(st["theta0"], np.float64)
+        if theta0.shape != self.theta0.shape:
+            raise ValueError(f"checkpoint has {theta0.size} parameters, this fit {self.theta0.size}")
+        self.theta0 = theta0.copy()
+        self.scale = np.asarray(st["scale"], np.float64).copy()
+        self.phi = np.asarray(st["phi"], np.float64).copy()
+        self.m = np.asarray(st["m"], np.float64).copy()
+        self.v = np.asarray(st["v"], np.float64).copy()
+        self.t = int(st["t"])
+        self.lr = float(st["lr"])
+
+    def save(self, path) -> None:
+        """Write the state to an .npz file (atomically: a temporary file, then a rename)."""
+        import os
+        tmp = f"{path}.tmp.npz"
+        np.savez(tmp, **self.state_dict())
+        os.replace(tmp, path)
+
+    def load(self, path) -> None:
+        with np.load(path) as z:
+            self.load_state_dict({k: z[k] for k in z.files})
+
+    def run(self, steps: int, checkpoint=None, every: int = 0) -> dict:
+        """`steps` Adam steps; with `checkpoint` (a path) and `every` > 0 the
+        state is saved after every `every` steps and after the last one."""
         losses = []
         t0 = time.perf_counter()
-        for _ in range(steps):
+        for k in range(steps):
             loss, _ = self.step()
             losses.append(loss)
+            if checkpoint is not None and every > 0 and ((k + 1) % every == 0 or k + 1 == steps):
+                self.save(checkpoint)
         el = time.perf_counter() - t0
-        return {"losses": losses, "seconds": el, "theta": self.theta.copy()}
+        g = getattr(self, "last_grad", None)
+        return {"losses": losses, "seconds": el, "theta": self.theta.copy(),
+                "grad_norm": float(np.linalg.norm(g)) if g is not None else None,
+                "scaled_grad_norm": float(np.linalg.norm(g * self.scale)) if g is not None else None}
 
 
 def terrain_volume(chunks_per_edge: int = 32, cells: int = 16, chunk_size: int = 16, octaves: int = 8, seed: int = 0,

@@ -383,6 +383,12 @@ __global__ void __launch_bounds__(kBwdThreads) backward_kernel(const DevParams p
 // ---- heightmap loss --------------------------------------------------------
 // Column c = (floor((x - x0) / w), floor((y - y0) / w)); over the columns
 // holding at least one vertex, L = sum (mean z - target)^2 / (cols_x cols_y).
+// Deterministic: each column's heights are summed in 2^-16 fixed point with
+// integer atomics (their order does not change the sum), and the loss is
+// reduced over the columns in a fixed order by one CTA, so a terrain-fitting
+// run repeats exactly.
+constexpr double kHeightFix = 65536.0;  // fixed-point scale of the column sums
+
 struct HeightArgs {
     const uww_vert_color* verts;
     const unsigned long long* totals;   // totals[0] = vertex count
@@ -390,10 +396,16 @@ struct HeightArgs {
     float x0, y0, inv_w;
     uint32_t cols_x, cols_y;
     const float* target;
-    float* work;                        // [2][cols]: sum z, count
+    long long* sum_z;                   // [cols] sum of z * kHeightFix, rounded per vertex
+    unsigned long long* count;          // [cols]
     float* pos_grad;
     float* loss;
 };
+
+__device__ __forceinline__ float column_mean(const HeightArgs& h, int c)
+{
+    return (float)((double)h.sum_z[c] / kHeightFix / (double)h.count[c]);
+}
 
 __device__ __forceinline__ int column_of(const HeightArgs& h, float x, float y)
 {
@@ -410,9 +422,11 @@ __global__ void height_accumulate(const HeightArgs h)
         const uww_vert_color q = h.verts[v];
         const int c = column_of(h, q.pos[0], q.pos[1]);
         if (c < 0) continue;
-        atomicAdd(h.work + c, q.pos[2]);
-        atomicAdd(h.work + cols + c, 1.f);
+        atomicAdd(reinterpret_cast<unsigned long long*>(h.sum_z + c),
+                  (unsigned long long)__double2ll_rn((double)q.pos[2] * kHeightFix));
+        atomicAdd(h.count + c, 1ull);
     }
+    (void)cols;
 }
 
 __global__ void height_grad(const HeightArgs h)
@@ -420,30 +434,40 @@ __global__ void height_grad(const HeightArgs h)
     const uint32_t nv = (uint32_t)min(*h.totals, (unsigned long long)h.vert_capacity);
     const uint32_t cols = h.cols_x * h.cols_y;
     const float inv_cols = 1.f / (float)cols;
-    float part = 0.f;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < max(nv, cols); i += gridDim.x * blockDim.x) {
-        if (i < cols) {
-            const float cnt = h.work[cols + i];
-            if (cnt > 0.f) {
-                const float r = h.work[i] / cnt - h.target[i];
-                part += r * r * inv_cols;
-            }
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nv; i += gridDim.x * blockDim.x) {
+        const uww_vert_color q = h.verts[i];
+        const int c = column_of(h, q.pos[0], q.pos[1]);
+        float gz = 0.f;
+        if (c >= 0) {
+            const float cnt = (float)h.count[c];
+            gz = 2.f * (column_mean(h, c) - h.target[c]) / cnt * inv_cols;
         }
-        if (i < nv) {
-            const uww_vert_color q = h.verts[i];
-            const int c = column_of(h, q.pos[0], q.pos[1]);
-            float gz = 0.f;
-            if (c >= 0) {
-                const float cnt = h.work[cols + c];
-                gz = 2.f * (h.work[c] / cnt - h.target[c]) / cnt * inv_cols;
-            }
-            h.pos_grad[3 * (size_t)i] = 0.f;
-            h.pos_grad[3 * (size_t)i + 1] = 0.f;
-            h.pos_grad[3 * (size_t)i + 2] = gz;
-        }
+        h.pos_grad[3 * (size_t)i] = 0.f;
+        h.pos_grad[3 * (size_t)i + 1] = 0.f;
+        h.pos_grad[3 * (size_t)i + 2] = gz;
     }
-    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
-    if ((threadIdx.x & 31) == 0 && part != 0.f) atomicAdd(h.loss, part);
+}
+
+// The loss, by one CTA of 1024 threads in a fixed order: per thread a strided
+// sum over the columns, then a tree over the threads.
+__global__ void __launch_bounds__(1024) height_loss_reduce(const HeightArgs h)
+{
+    __shared__ float part[1024];
+    const uint32_t cols = h.cols_x * h.cols_y;
+    const float inv_cols = 1.f / (float)cols;
+    float s = 0.f;
+    for (uint32_t c = threadIdx.x; c < cols; c += blockDim.x)
+        if (h.count[c]) {
+            const float r = column_mean(h, (int)c) - h.target[c];
+            s += r * r * inv_cols;
+        }
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (unsigned o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) part[threadIdx.x] += part[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *h.loss = part[0];
 }
 
 template <class O, int KMAX>
@@ -562,10 +586,10 @@ int uww_height_loss(uww_ctx* ctx, const uww_vert_color* d_verts, const uint64_t*
 {
     if (!ctx || !d_verts || !d_totals || !d_target || !d_work || !d_pos_grad || !d_loss) return UWW_ERR_INVALID_ARG;
     if (!(column > 0.f) || cols_x == 0 || cols_y == 0) return UWW_ERR_INVALID_ARG;
+    if (!aligned_to(d_work, 8)) return UWW_ERR_INVALID_ARG;
     cudaStream_t s = ctx->stream;
     const size_t cols = (size_t)cols_x * cols_y;
-    cudaError_t e = cudaMemsetAsync(d_work, 0, 2 * cols * sizeof(float), s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(d_loss, 0, sizeof(float), s);
+    cudaError_t e = cudaMemsetAsync(d_work, 0, 4 * cols * sizeof(float), s);
     if (e != cudaSuccess) return status_from_cuda(e, "cudaMemsetAsync");
     HeightArgs h;
     h.verts = d_verts;
@@ -577,12 +601,14 @@ int uww_height_loss(uww_ctx* ctx, const uww_vert_color* d_verts, const uint64_t*
     h.cols_x = cols_x;
     h.cols_y = cols_y;
     h.target = d_target;
-    h.work = d_work;
+    h.sum_z = reinterpret_cast<long long*>(d_work);
+    h.count = reinterpret_cast<unsigned long long*>(d_work) + cols;
     h.pos_grad = d_pos_grad;
     h.loss = d_loss;
     const int grid = std::max(1, std::min<int>(ctx->num_sms * 8, (int)((std::max<size_t>(vert_capacity, cols) + 255) / 256)));
     height_accumulate<<<grid, 256, 0, s>>>(h);
     height_grad<<<grid, 256, 0, s>>>(h);
+    height_loss_reduce<<<1, 1024, 0, s>>>(h);
     return status_from_cuda(cudaGetLastError(), "height loss kernel launch");
 }
 
