@@ -56,13 +56,18 @@ FLOPS_PER_VERTEX_EXTRA = 60    # interpolation, colour ramp, normalisation
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one build_kernel
 # launch on this workload, from a single-kernel ncu capture of this script's
 # own step (-k regex:build_kernel -s 12 -c 1 of
-# `bench.py --steps 5 --warmup 3 --quick --no-cpu`, caches flushed before the
-# launch): 257.5 KB read + 4.1 KB written.  The outputs stay in L2
-# (write-back) when the kernel ends, so this is below the algorithmic output
-# bytes.
-NCU_DRAM_BYTES_PER_LAUNCH = 261_632
-NCU_TRAFFIC_SOURCE = ("ncu --set full -k regex:build_kernel -s 12 -c 1, python bench.py --steps 5 --warmup 3 "
-                      "--quick --no-cpu: dram__bytes_read.sum + dram__bytes_write.sum of that launch")
+# `bench.py --steps 5 --warmup 3 --quick --no-cpu --clock-window 0`, caches
+# flushed before the launch): 889.3 KB read + 16.4 KB written.  The outputs
+# stay in L2 (write-back) when the kernel ends, so this is below the
+# algorithmic output bytes.
+NCU_DRAM_BYTES_PER_LAUNCH = 905_728
+NCU_TRAFFIC_SOURCE = ("ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum -k regex:build_kernel -s 12 -c 1, "
+                      "python bench.py --steps 5 --warmup 3 --quick --no-cpu --clock-window 0")
+# FP32 flops the noise-stage kernel executes per launch of this workload
+# (2 x FFMA + FADD + FMUL thread instructions, ncu sm__sass_thread_inst_executed_op_*_pred_on.sum,
+# -k regex:sample_kernel_fast -s 3 -c 1 of the same command): the column form
+# runs 4.3x fewer flops than the reference formulation counted above.
+NCU_SAMPLE_EXECUTED_FLOPS = 728_236_800
 
 
 def parse():
@@ -80,6 +85,9 @@ def parse():
     ap.add_argument("--fit-steps", type=int, default=200, help="Adam steps of the terrain-fitting leg")
     ap.add_argument("--leg", default="", choices=["", "mixed_lod", "adjoint", "queries", "terrain_fit"],
                     help="with --quick: also run this one leg (profiling runs)")
+    ap.add_argument("--clock-window", type=float, default=CLOCK_WINDOW_S,
+                    help="seconds nvidia-smi watches the build (untimed steps fill what the timed ones leave); "
+                         "0 for profiling runs that must launch few kernels")
     return ap.parse_args()
 
 
@@ -775,7 +783,7 @@ def main():
     # keep running the same step, untimed, until the sampler has watched it
     # for CLOCK_WINDOW_S
     extra_steps = 0
-    while time.perf_counter() - t_window < CLOCK_WINDOW_S:
+    while time.perf_counter() - t_window < args.clock_window:
         flush.zero_()
         step(args.steps + extra_steps)
         extra_steps += 1
@@ -938,8 +946,13 @@ def main():
     ns_leg = extra.get("noise_stage")
     if ns_leg:
         ns_leg["frac_of_fp32_peak"] = ns_leg["tflops"] / fp32_peak
+        executed = NCU_SAMPLE_EXECUTED_FLOPS / (ns_leg["us"] * 1e-6) / 1e12
         line["roofline"]["noise_stage"] = {"bound": "fp32", "achieved": ns_leg["tflops"], "peak": fp32_peak,
                                            "unit": "TFLOP/s", "frac": ns_leg["tflops"] / fp32_peak,
+                                           "flops": "algorithmic: the reference formulation's 348 per sample",
+                                           "executed_tflops": executed, "executed_frac": executed / fp32_peak,
+                                           "executed_flops_source": "ncu FP32 instruction counts of one launch "
+                                                                    "(profiles/sample_kernel_fast_uniform_grid_4096.md)",
                                            "kernel": "sample_kernel_fast (uww_sample_chunks), 4096 x 13^3 samples"}
     line.update({k: v for k, v in extra.items() if k != "e2e"})
     if "adjoint" in extra:
