@@ -929,7 +929,8 @@ def main():
         "mean_verts_per_step": mean_v, "mean_inds_per_step": mean_i, "chunks_decided_by_depth_bias": decided,
         "mvoxels_per_s": value * 12 ** 3 / 1e6,
         "msamples_per_s": value * 13 ** 3 / 1e6,
-        "gpu_launches": args.steps * (2 if params[0].outputs & (abi.UWW_OUT_COLOR | abi.UWW_OUT_NORMALS) else 1),
+        # per step: the planning kernel, the build, the colour/normal pass
+        "gpu_launches": args.steps * (2 + (1 if params[0].outputs & (abi.UWW_OUT_COLOR | abi.UWW_OUT_NORMALS) else 0)),
         "clocks": clk,
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": achieved / fp32_peak, "traffic": NCU_DRAM_BYTES_PER_LAUNCH,
