@@ -250,6 +250,13 @@ typedef struct uww_tuning {
  * output does not change; for measuring the per-chunk cost of the full
  * path). */
 #define UWW_TUNE_NO_DEPTH_SHORTCUT 1u
+/* PIPELINED: build every batch with the single pipelined kernel (look-back
+ * prefix sum, one CTA emits the chunks it sampled).  By default a batch whose
+ * chunks all fit one shared-memory workspace (<= 256 compute threads, no
+ * streamed host output, no failure injection) is built in two kernels
+ * instead: the front half of every chunk, then the emission of every
+ * triangle of the batch.  Both give the same output. */
+#define UWW_TUNE_PIPELINED 2u
 
 /* Failure injection (uww_tuning.test_flags).  WITHHOLD_FIRST: the first chunk
  * of every batched build never publishes its prefix, so the look-back waits

@@ -14,6 +14,10 @@
 * The fast build (UWW_MATH_FAST) on the whole uniform grid against the F64
   oracle (the reference's f64 noise): flipped cells and vertex error,
   bounded.
+* The two batched builds -- the split build (front kernel, then emission of
+  every triangle; the default for these 12^3 chunks) and the single
+  pipelined kernel (UWW_TUNE_PIPELINED) -- give the same bytes on the whole
+  uniform grid, fast build with the benchmark's outputs.
 
 The oracle follows chunk.rs:105-264 and perlin_util.rs:6-29.
 """
@@ -77,3 +81,24 @@ def test_fast_build_whole_grid_against_f64_oracle(ctx_factory, oracle):
     assert flips <= 1e-5 * cells, flips
     assert worst < 0.01 * 16.0 / 12, worst  # 1 % of a cell
     assert max(r["median_vertex_err"] for r in rows) < 1e-4
+
+
+@pytest.mark.parametrize("seed", [0, 3, 7])
+def test_split_and_pipelined_builds_give_the_same_bytes(ctx_factory, seed):
+    p, d = workloads.uniform_grid(seed=seed, outputs=COLOR_NORMALS)
+    p.math_mode = abi.UWW_MATH_FAST
+    ctx = ctx_factory(p)
+    split = ctx.build_chunks_device(d, 400_000, 1_500_000)
+    ctx.set_tuning(options=abi.UWW_TUNE_PIPELINED)
+    piped = ctx.build_chunks_device(d, 400_000, 1_500_000)
+    ctx.set_tuning(options=0)
+    again = ctx.build_chunks_device(d, 400_000, 1_500_000)
+    for b in (split, piped, again):
+        assert b.status == abi.UWW_OK
+    assert (split.records["flags"] & abi.UWW_CHUNK_HAS_MESH).sum() > 1000
+    for other in (piped, again):
+        np.testing.assert_array_equal(split.records, other.records)
+        np.testing.assert_array_equal(split.totals, other.totals)
+        np.testing.assert_array_equal(split.inds, other.inds)
+        np.testing.assert_array_equal(split.verts.view(np.uint32), other.verts.view(np.uint32))
+        np.testing.assert_array_equal(split.normals.view(np.uint32), other.normals.view(np.uint32))

@@ -23,6 +23,22 @@ def caps(ref):
     return max(int(ref.totals[0]), 1), max(int(ref.totals[1]), 1)
 
 
+@pytest.fixture(params=["split", "pipelined"])
+def ctx_factory(request, ctx_factory):
+    """Every test here runs twice: with the default batched build (the split
+    build wherever every chunk fits a shared-memory workspace) and with the
+    single pipelined kernel (UWW_TUNE_PIPELINED)."""
+    if request.param == "split":
+        return ctx_factory
+
+    def make(params=None):
+        c = ctx_factory(params)
+        c.set_tuning(options=abi.UWW_TUNE_PIPELINED)
+        return c
+
+    return make
+
+
 @pytest.mark.parametrize("name", ["single_cell", "single_cell_random", "grids"])
 def test_known_answers_from_samples(ctx_factory, oracle, name):
     g = load_golden(name)

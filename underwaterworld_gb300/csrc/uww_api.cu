@@ -143,21 +143,40 @@ struct LaunchCfg {
     size_t ztable_offset;  // fast build z tables, after the workspaces
     size_t dyn_smem;
     int grid;
+    int occupancy;         // resident CTAs per SM of the build's (front) kernel
     size_t scratch_slot;
+    bool split;            // the split build: front kernel, then emission over every triangle
 };
 
-int plan_launch(uww_ctx* ctx, uint32_t n, uint32_t max_cells, bool queue, LaunchCfg* cfg)
+// split_ok: nothing of the launch needs the pipelined kernel (streamed host
+// output does)
+int plan_launch(uww_ctx* ctx, uint32_t n, uint32_t max_cells, bool queue, LaunchCfg* cfg, bool split_ok = true)
 {
-    // The batched form pipelines two chunks per CTA, so it holds two workspaces.
-    const uint32_t slots = queue ? 2u : 1u;
     const size_t cap = ctx->smem_dyn_max;
+    const int compute = ctx->threads > 0 ? ctx->threads : default_compute_threads(max_cells);
+    const size_t zt_max = ctx->dev.math_mode == UWW_MATH_FAST ? ztable_bytes((int)max_cells + 1, ctx->dev.octaves) : 0;
+    // A batch whose every chunk fits one shared-memory workspace is built in
+    // two kernels (the front half of every chunk, then the emission of every
+    // triangle); the look-back test flag and the PIPELINED option keep the
+    // single pipelined kernel.
+    cfg->split = queue && split_ok && compute <= 256 && !(ctx->options & UWW_TUNE_PIPELINED) &&
+                 !(ctx->test_flags & UWW_TEST_WITHHOLD_FIRST) &&
+                 (ctx->smem_cells <= 0 || (uint32_t)ctx->smem_cells >= max_cells) &&
+                 chunk_layout((int)max_cells).total + zt_max <= cap;
+    // The pipelined batched form keeps two chunks per CTA in flight, so it
+    // holds two workspaces.
+    const uint32_t slots = (queue && !cfg->split) ? 2u : 1u;
     // by default chunks up to 16 cells work in shared memory; a batch with
     // larger ones keeps 12 there (small workspaces, more CTAs per SM) and the
-    // rest in global scratch
-    uint32_t smem_cells = ctx->smem_cells > 0 ? (uint32_t)ctx->smem_cells : (max_cells > 16 ? 12u : max_cells);
+    // rest in global scratch -- except in the split build, where every chunk
+    // does
+    uint32_t smem_cells = cfg->split               ? max_cells
+                          : ctx->smem_cells > 0    ? (uint32_t)ctx->smem_cells
+                          : max_cells > 16         ? 12u
+                                                   : max_cells;
     smem_cells = std::min(smem_cells, max_cells);
     // the fast build also keeps per-chunk z tables (sized for the largest chunk)
-    const size_t zt = ctx->dev.math_mode == UWW_MATH_FAST ? ztable_bytes((int)max_cells + 1, ctx->dev.octaves) : 0;
+    const size_t zt = zt_max;
     while (smem_cells > 0 && (size_t)slots * chunk_layout((int)smem_cells).total + zt > cap) --smem_cells;
     cfg->smem_cells = smem_cells;
     cfg->slots = slots;
@@ -169,19 +188,19 @@ int plan_launch(uww_ctx* ctx, uint32_t n, uint32_t max_cells, bool queue, Launch
     // 512 above (one CTA per SM: a 25^2-column chunk in global scratch is
     // latency-bound, 1.7x faster than with 256); the batched form adds one
     // control warp
-    const int compute = ctx->threads > 0 ? ctx->threads : default_compute_threads(max_cells);
-    cfg->threads = compute + (queue ? 32 : 0);
+    cfg->threads = compute + ((queue && !cfg->split) ? 32 : 0);
     cfg->scratch_slot = max_cells > smem_cells ? chunk_layout((int)max_cells).total : 0;
+    cfg->occupancy = 0;
     if (!queue) {
         cfg->grid = 1;
         return UWW_OK;
     }
-    int bps = ctx->blocks_per_sm;
-    if (bps <= 0) {
-        cudaError_t e = build_occupancy(true, ctx->dev.math_mode == UWW_MATH_EXACT, cfg->threads, cfg->dyn_smem, &bps);
-        if (e != cudaSuccess) return cuda_status(e);
-        if (bps < 1) return UWW_ERR_INVALID_ARG;
-    }
+    const bool exact = ctx->dev.math_mode == UWW_MATH_EXACT;
+    cudaError_t e = cfg->split ? front_occupancy(exact, cfg->threads, cfg->dyn_smem, &cfg->occupancy)
+                               : build_occupancy(true, exact, cfg->threads, cfg->dyn_smem, &cfg->occupancy);
+    if (e != cudaSuccess) return cuda_status(e);
+    int bps = ctx->blocks_per_sm > 0 ? ctx->blocks_per_sm : cfg->occupancy;
+    if (bps < 1) return UWW_ERR_INVALID_ARG;
     const long long g = (long long)bps * ctx->num_sms;
     cfg->grid = (int)std::min<long long>(g, n);
     return UWW_OK;
@@ -203,7 +222,7 @@ int launch(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint32_t ma
            const HostOut* host = nullptr)
 {
     LaunchCfg cfg;
-    int st = plan_launch(ctx, n, max_cells, queue, &cfg);
+    int st = plan_launch(ctx, n, max_cells, queue, &cfg, host == nullptr);
     if (st) return st;
     // the work buffers a captured frame graph refers to: a reallocation
     // moves the context's generation on, and such a frame recaptures itself
@@ -283,6 +302,47 @@ int launch(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint32_t ma
             }
             a.plan = ctx->d_plan;
         }
+        if (cfg.split) {
+            // The counters, the tile sums, per chunk its counts word, the
+            // mesh list and the work queues -- laid out for the chunk count
+            // the buffer was sized for, so that they stay in place from one
+            // launch to the next -- then per chunk a workspace slot.  The
+            // counters and tile sums are zero at launch: cleared here on
+            // (re)allocation and left zero by every launch's emission kernel.
+            const size_t slot = align16(chunk_layout((int)max_cells).total);
+            auto fixed_bytes = [](uint32_t m) {
+                const size_t ntiles = ((size_t)m + kTileChunks - 1) / kTileChunks;
+                return kCtrWords * 4 + ((ntiles * 8 + 15) & ~size_t(15)) + (((size_t)m * 8 + 15) & ~size_t(15)) +
+                       (((size_t)m * 4 + 15) & ~size_t(15)) + (((size_t)m * 4 * kPlanRanks + 15) & ~size_t(15));
+            };
+            const uint32_t m = std::max(n, ctx->split_n);
+            if (!ctx->d_split || ctx->split_n < n || ctx->split_cap < fixed_bytes(m) + (size_t)n * slot) {
+                const uint32_t mm = std::max(m, 4096u);
+                st = grow(&ctx->d_split, &ctx->split_cap, fixed_bytes(mm) + (size_t)mm * slot);
+                if (st) return st;
+                ctx->split_n = mm;
+                const size_t ntiles = ((size_t)mm + kTileChunks - 1) / kTileChunks;
+                cudaError_t e = cudaMemsetAsync(ctx->d_split, 0, kCtrWords * 4 + ntiles * 8, ctx->stream);
+                if (e != cudaSuccess) return cuda_status(e, "cudaMemsetAsync");
+            }
+            const uint32_t nc = ctx->split_n;
+            const size_t ntiles = ((size_t)nc + kTileChunks - 1) / kTileChunks;
+            uint8_t* b = ctx->d_split;
+            a.split_ctr = reinterpret_cast<uint32_t*>(b);
+            b += kCtrWords * 4;
+            a.tile_sum = reinterpret_cast<unsigned long long*>(b);
+            b += (ntiles * 8 + 15) & ~size_t(15);
+            a.tinfo = reinterpret_cast<unsigned long long*>(b);
+            b += ((size_t)nc * 8 + 15) & ~size_t(15);
+            a.mesh_list = reinterpret_cast<uint32_t*>(b);
+            b += ((size_t)nc * 4 + 15) & ~size_t(15);
+            a.split_queue = reinterpret_cast<uint32_t*>(b);
+            b += ((size_t)nc * 4 * kPlanRanks + 15) & ~size_t(15);
+            a.slots = b;
+            a.slot_bytes = slot;
+            a.split_planned = a.plan != nullptr;
+            a.plan = nullptr;  // the split build plans into its own queues
+        }
     }
     if (prepare_only) return UWW_OK;
     return cuda_status(launch_build(ctx->dev, a, queue, cfg.grid, cfg.threads, cfg.dyn_smem, ctx->stream), "build kernel launch");
@@ -331,7 +391,8 @@ int prepare_batched(uww_ctx* ctx, uint32_t n, uint32_t max_cells, const uww_mesh
 {
     return launch(ctx, nullptr, n, max_cells, out, true, nullptr, 0, nullptr, nullptr, true);
 }
-int plan_batched(uww_ctx* ctx, uint32_t n, uint32_t max_cells, int* threads, int* grid, size_t* dyn_smem)
+int plan_batched(uww_ctx* ctx, uint32_t n, uint32_t max_cells, int* threads, int* grid, size_t* dyn_smem,
+                 int* occupancy)
 {
     LaunchCfg cfg;
     const int st = plan_launch(ctx, n, max_cells, true, &cfg);
@@ -339,6 +400,7 @@ int plan_batched(uww_ctx* ctx, uint32_t n, uint32_t max_cells, int* threads, int
     *threads = cfg.threads;
     *grid = cfg.grid;
     *dyn_smem = cfg.dyn_smem;
+    *occupancy = cfg.occupancy;
     return UWW_OK;
 }
 }  // namespace uww
@@ -462,6 +524,7 @@ int uww_ctx_destroy(uww_ctx* ctx)
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     cudaFree(ctx->d_lookback);
     cudaFree(ctx->d_plan);
+    cudaFree(ctx->d_split);
     cudaFree(ctx->d_state);
     cudaFree(ctx->d_totals);
     cudaFree(ctx->d_scratch);
@@ -606,7 +669,45 @@ int uww_build_chunks_host(uww_ctx* ctx, const uww_chunk_desc* h_chunks, uint32_t
     void* ds = want_samples ? device_view(h_out->samples) : nullptr;
     // (the streamed words are 4-byte stores: host buffers off a 4-byte boundary take the copy path)
     const bool words_ok = aligned_to(dv, 4) && aligned_to(dn, 4) && aligned_to(di, 4) && aligned_to(dr, 4);
-    if (dv && di && dr && words_ok && (!want_normals || dn) && (!want_cases || dc) && (!want_samples || ds)) {
+    const bool mapped = dv && di && dr && (!want_normals || dn) && (!want_cases || dc) && (!want_samples || ds);
+    LaunchCfg probe;
+    if (mapped && plan_launch(ctx, n, max_cells, true, &probe) == UWW_OK && probe.split) {
+        // The split build on the device, then one copy kernel that moves
+        // every output to the host buffers, the vertex, normal and index
+        // spans sized from the device totals: no host round trip in between.
+        if ((st = launch(ctx, ctx->d_chunks, n, max_cells, &d_out, true))) return st;
+        CopyOut c;
+        std::memset(&c, 0, sizeof(c));
+        auto seg = [&](const void* src, void* dst, unsigned long long fixed, int count_idx, uint32_t elem,
+                       unsigned long long cap) {
+            CopySeg& g = c.seg[c.nseg++];
+            g.src = static_cast<const uint8_t*>(src);
+            g.dst = static_cast<uint8_t*>(dst);
+            g.fixed_bytes = fixed;
+            g.count_idx = count_idx;
+            g.elem_bytes = elem;
+            g.cap_elems = cap;
+        };
+        seg(ctx->d_records, dr, (unsigned long long)n * sizeof(uww_chunk_record), -1, 0, 0);
+        seg(ctx->d_verts, dv, 0, 0, (uint32_t)sizeof(uww_vert_color), h_out->vert_capacity);
+        if (want_normals) seg(ctx->d_normals, dn, 0, 0, 12u, h_out->vert_capacity);
+        seg(ctx->d_inds, di, 0, 1, 4u, h_out->ind_capacity);
+        if (want_cases && case_bytes) seg(ctx->d_cases, dc, case_bytes, -1, 0, 0);
+        if (want_samples && sample_count) seg(ctx->d_samples, ds, sample_count * 4, -1, 0, 0);
+        void* dt = device_view(ctx->h_totals);
+        if (dt) seg(ctx->d_totals, dt, 4 * sizeof(unsigned long long), -1, 0, 0);
+        if ((e = launch_copy_out(c, ctx->d_totals, ctx->num_sms * 2, s)) != cudaSuccess) return cuda_status(e);
+        if (!dt &&
+            (e = cudaMemcpyAsync(ctx->h_totals, ctx->d_totals, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+            return cuda_status(e);
+        if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_status(e);
+        if (h_out->totals) std::memcpy(h_out->totals, ctx->h_totals, 4 * sizeof(uint64_t));
+        if (ctx->h_totals[3] & kErrTimeout) return UWW_ERR_TIMEOUT;
+        if (ctx->h_totals[3] & (kErrBadChunk | kErrRange)) return UWW_ERR_INVALID_ARG;
+        if (ctx->h_totals[2]) return UWW_ERR_CAPACITY;
+        return UWW_OK;
+    }
+    if (mapped && words_ok) {
         HostOut ho;
         ho.verts = static_cast<uww_vert_color*>(dv);
         ho.normals = static_cast<float*>(dn);
@@ -675,7 +776,7 @@ int uww_ctx_set_tuning(uww_ctx* ctx, const uww_tuning* t)
     if (t->blocks_per_sm < 0 || t->blocks_per_sm > 32) return UWW_ERR_INVALID_ARG;
     if (t->smem_cells < 0 || t->smem_cells > UWW_MAX_CELLS) return UWW_ERR_INVALID_ARG;
     if (t->spin_limit < 0 || (t->test_flags & ~UWW_TEST_WITHHOLD_FIRST)) return UWW_ERR_INVALID_ARG;
-    if (t->options & ~UWW_TUNE_NO_DEPTH_SHORTCUT) return UWW_ERR_INVALID_ARG;
+    if (t->options & ~(UWW_TUNE_NO_DEPTH_SHORTCUT | UWW_TUNE_PIPELINED)) return UWW_ERR_INVALID_ARG;
     ctx->threads = t->threads;
     ctx->blocks_per_sm = t->blocks_per_sm;
     ctx->smem_cells = t->smem_cells;

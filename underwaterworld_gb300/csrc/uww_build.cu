@@ -59,6 +59,11 @@ namespace {
 constexpr int kIndShift = 22;
 constexpr int kActShift = 44;
 constexpr unsigned long long kField22 = (1ull << 22) - 1;
+// split build: a chunk's counts word (tinfo) is the packed counts and, in
+// bit 62, the early-blank flag
+constexpr unsigned long long kInfoEarlyBlank = 1ull << 62;
+__device__ __forceinline__ uint32_t rec_off32(unsigned long long v) { return (uint32_t)(v > 0xffffffffull ? 0xffffffffull : v); }
+
 
 
 // Per in-flight chunk, kept in shared memory between the front and back halves.
@@ -97,6 +102,8 @@ struct SmemTables {
     uint16_t first_ref[256];      // per case: row positions that are their edge's first reference
     unsigned long long warp_sums[32];
     unsigned long long chunk_total;
+    unsigned long long warp_sums2[32];  // split build: second component of its scans
+    unsigned long long chunk_total2;
     ChunkInfo ci[2];              // the chunks in flight (front / back)
     Ticket tk[2];                 // tickets handed from the control warp
     Offsets off[2];               // offsets handed from the control warp
@@ -532,13 +539,16 @@ __device__ void chunk_front(const DevParams& p, const BuildArgs& a, SmemTables& 
                 if (nt) {
                     W.set_vbase(c, (uint32_t)(run & kField22));
                     const uint32_t ir = (uint32_t)((run >> kIndShift) & kField22);
+                    // the active-cell list (the split build's vertex work searches
+                    // it), and the triangle map or each active cell's first
+                    // index position
+                    const uint32_t ar = (uint32_t)(run >> kActShift);
+                    W.set_active(ar, c);
                     if (direct) {
                         uint16_t* tmap = reinterpret_cast<uint16_t*>(W.ibase) + ir / 3u;
                         const unsigned xyz = (unsigned)x | ((unsigned)y << 4) | ((unsigned)z << 8);
                         for (int k = 0; k < nt; ++k) tmap[k] = (uint16_t)(xyz | ((unsigned)k << 12));
                     } else {
-                        const uint32_t ar = (uint32_t)(run >> kActShift);
-                        W.set_active(ar, c);
                         W.set_ibase(ar, ir);
                     }
                     run += (unsigned long long)nv | ((unsigned long long)(3 * nt) << kIndShift) | (1ull << kActShift);
@@ -565,12 +575,10 @@ __device__ void chunk_front(const DevParams& p, const BuildArgs& a, SmemTables& 
 // colour slot 0, the owner's corner b (the value ramp's input, chunk.rs:215);
 // write its colour and unit normal.
 template <class O>
-__device__ __forceinline__ void vertex_outputs(const DevParams& p, const uint8_t* P, const float4* gp,
-                                               const uww_vert_color* verts, uint32_t v, bool want_color,
-                                               bool want_normals, float2 out[3], float g[3])
+__device__ __forceinline__ void vertex_values(const DevParams& p, const uint8_t* P, const float4* gp, float2 p01,
+                                              float2 p2c, bool want_color, bool want_normals, float2 out[3],
+                                              float g[3])
 {
-    const float2* v2 = reinterpret_cast<const float2*>(verts + v);
-    const float2 p01 = v2[0], p2c = v2[1];
     const int cb = (int)p2c.y;
     out[0] = p01;
     if (want_color) {
@@ -592,6 +600,17 @@ __device__ __forceinline__ void vertex_outputs(const DevParams& p, const uint8_t
 }
 
 template <class O>
+__device__ __forceinline__ void vertex_outputs(const DevParams& p, const uint8_t* P, const float4* gp,
+                                               const uww_vert_color* verts, uint32_t v, bool want_color,
+                                               bool want_normals, float2 out[3], float g[3])
+{
+    // position and carried corner from L2: written by another thread of the
+    // batch (pass 1), in this grid or the one before it
+    const float2* v2 = reinterpret_cast<const float2*>(verts + v);
+    vertex_values<O>(p, P, gp, __ldcg(v2), __ldcg(v2 + 1), want_color, want_normals, out, g);
+}
+
+template <class O>
 __device__ __forceinline__ void finish_vertex(const DevParams& p, const uint8_t* P, const float4* gp,
                                               uww_vert_color* verts, float* normals, uint32_t v, bool want_color,
                                               bool want_normals)
@@ -605,6 +624,129 @@ __device__ __forceinline__ void finish_vertex(const DevParams& p, const uint8_t*
     if (want_normals) {
         float* nn = normals + 3 * (size_t)v;
         nn[0] = g[0]; nn[1] = g[1]; nn[2] = g[2];
+    }
+}
+
+// The vertex on edge e of cell (x, y, z): its chunk-local position (plus
+// the chunk origin ox, oy, oz), the cell's corner b of the edge (the colour
+// ramp's input) and, for the adjoint, its edge id (first-corner sample index
+// << 3 | direction of corner b from corner a: +x -x +y -y +z -z).
+struct EdgeVertex {
+    float x, y, z;
+    int cb;
+    uint32_t edge_id;
+};
+
+template <class O>
+__device__ __forceinline__ EdgeVertex edge_vertex(const DevParams& p, const SmemTables& T, const float* rho, int S,
+                                                  int x, int y, int z, int e, float s, int ox, int oy, int oz)
+{
+    const float iso = p.iso_level;
+    const int ca = T.corners[e][0], cb = T.corners[e][1];
+    const int ax = x + ((0x66 >> ca) & 1), ay = y + (ca >> 2), az = z + ((0xcc >> ca) & 1);
+    const int bx = x + ((0x66 >> cb) & 1), by = y + (cb >> 2), bz = z + ((0xcc >> cb) & 1);
+    const float ia = rho[(ax * S + ay) * S + az];
+    const float ibv = rho[(bx * S + by) * S + bz];
+    const float sax = O::mul((float)ax, s), say = O::mul((float)ay, s), saz = O::mul((float)az, s);
+    const float sbx = O::mul((float)bx, s), sby = O::mul((float)by, s), sbz = O::mul((float)bz, s);
+    const float tt = O::div(O::sub(iso, ia), O::sub(ibv, ia));
+    const float mx = O::add(sax, O::mul(tt, O::sub(sbx, sax)));
+    const float my = O::add(say, O::mul(tt, O::sub(sby, say)));
+    const float mz = O::add(saz, O::mul(tt, O::sub(sbz, saz)));
+    EdgeVertex v;
+    v.x = O::add(mx, (float)ox);
+    v.y = O::add(my, (float)oy);
+    v.z = O::add(mz, (float)oz);
+    v.cb = cb;
+    const int dir = bx != ax ? (bx < ax) : by != ay ? 2 + (by < ay) : 4 + (bz < az);
+    v.edge_id = ((uint32_t)((ax * S + ay) * S + az) << 3) | (uint32_t)dir;
+    return v;
+}
+
+// Where pass 1 writes: the batch's outputs, or the split build's staging
+// buffers.
+struct EmitOut {
+    uww_vert_color* verts;
+    uint32_t* inds;
+    uint32_t* edge_ids;
+};
+
+// Pass 1 for triangle t of a chunk's index stream: its cell from the
+// triangle map (else a binary search over the active cells), its three
+// chunk-local vertex ids into inds, and the positions of the vertices its
+// cell creates (the first reference of an owned edge).  The workspace W is
+// in shared memory or a scratch slot (the build kernel) or in a global slot
+// (the split build's emission kernel); the arithmetic is the same either way.
+// carry_corner: pass 2 follows, and colour slot 0 carries the owner's corner b.
+// positions: write the vertices the cell creates (the split build's vertex
+// work writes them instead).
+template <class O>
+__device__ __forceinline__ void emit_triangle(const DevParams& p, const EmitOut& a, const SmemTables& T,
+                                              const Workspace& W, int N, uint32_t nA, bool direct, uint32_t t,
+                                              uint32_t voff, uint32_t ioff, int ox, int oy, int oz, float s,
+                                              bool carry_corner, bool positions = true)
+{
+    const int oriented = p.dedup_mode == UWW_DEDUP_ORIENTED;
+    const int S = N + 1;
+    const float* rho = W.rho;
+    const uint8_t* cases = W.cases;
+    const uint32_t g = 3u * t;
+    int c, x, y, z, j0;
+    if (direct) {
+        const unsigned e = reinterpret_cast<const uint16_t*>(W.ibase)[t];
+        x = (int)(e & 15u);
+        y = (int)((e >> 4) & 15u);
+        z = (int)((e >> 8) & 15u);
+        j0 = 3 * (int)(e >> 12);
+        c = (x * N + y) * N + z;
+    } else {
+        uint32_t ai = 0, len = nA;
+        while (len > 1) {
+            const uint32_t h = len >> 1;
+            if (W.get_ibase(ai + h) <= g) ai += h;
+            len -= h;
+        }
+        c = W.get_active(ai);
+        x = c / (N * N);
+        y = (c / N) % N;
+        z = c % N;
+        j0 = (int)(g - W.get_ibase(ai));
+    }
+    const int cs = cases[c];
+    const int8_t* row = T.tri[cs];
+    const unsigned own_mask = T.owned[oriented][boundary_flags(x, y, z, N)];
+    const unsigned fr = T.first_ref[cs];
+    const uint32_t vb = W.get_vbase(c);
+    const uint16_t* before = UWW_EDGE_BEFORE[cs];
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+        const int i = j0 + m;
+        const int e = row[i];
+        const unsigned bit = 1u << e;
+        uint32_t id;
+        if (own_mask & bit) {
+            // the cell numbers its owned edges' vertices in first-reference order
+            id = vb + __popc(own_mask & __ldg(before + e));
+            if (positions && ((fr >> i) & 1u)) {
+                const EdgeVertex ev = edge_vertex<O>(p, T, rho, S, x, y, z, e, s, ox, oy, oz);
+                if (a.edge_ids) a.edge_ids[voff + id] = ev.edge_id;
+                float2* v2 = reinterpret_cast<float2*>(a.verts + voff + id);
+                v2[0] = make_float2(ev.x, ev.y);
+                // colour slot 0 carries the owner's corner b (the value ramp's
+                // input, chunk.rs:215) to pass 2, which overwrites it
+                v2[1] = make_float2(ev.z, carry_corner ? (float)ev.cb : 0.f);
+                v2[2] = make_float2(0.f, 0.f);
+            }
+        } else {
+            // the owner: the first cell in stream order holding this edge
+            const int ow = T.owner[oriented][(x == 0) | ((y == 0) << 1) | ((z == 0) << 2)][e];
+            const int qx = x - ((ow >> 4) & 1), qy = y - ((ow >> 5) & 1), qz = z - ((ow >> 6) & 1);
+            const int oe = ow & 15;
+            const int oc = (qx * N + qy) * N + qz;
+            const unsigned oown = T.owned[oriented][boundary_flags(qx, qy, qz, N)];
+            id = W.get_vbase(oc) + __popc(oown & __ldg(&UWW_EDGE_BEFORE[cases[oc]][oe]));
+        }
+        a.inds[ioff + g + m] = id;
     }
 }
 
@@ -636,99 +778,24 @@ __device__ void chunk_emit(const DevParams& p, const BuildArgs& a, SmemTables& T
     const uint32_t nV = (uint32_t)(ci.total & kField22);
     const uint32_t nA = (uint32_t)(ci.total >> kActShift);
     if (!(ci.classified && off.fits && nA > 0)) return;
-    const int oriented = p.dedup_mode == UWW_DEDUP_ORIENTED;
     const bool want_color = (p.outputs & UWW_OUT_COLOR) != 0;
     const bool want_normals = (p.outputs & UWW_OUT_NORMALS) != 0 && a.normals != nullptr;
-    const int N = ci.N, S = N + 1;
+    const int N = ci.N;
     const uint32_t voff = (uint32_t)(off.excl & 0xffffffffull);
     const uint32_t ioff = (uint32_t)(off.excl >> 32);
     const Workspace W = workspace(a, dyn_smem, buf, N);
-    const float* rho = W.rho;
-    const uint8_t* cases = W.cases;
     const int ox = ci.ox, oy = ci.oy, oz = ci.oz;
     {
         const float s = __fdiv_rn((float)p.chunk_size, (float)N);
-        const float iso = p.iso_level;
         // one thread per triangle of the chunk's index stream, so a dense
         // chunk's emission is spread over the CTA like a sparse one's; a
         // triangle's cell is the last active cell whose first index position
         // is at or before it
         const uint32_t nT = (uint32_t)((ci.total >> kIndShift) & kField22) / 3u;
         const bool direct = direct_triangles(W, N, ci.total);
-        for (uint32_t t = tid; t < nT; t += ncomp) {
-            const uint32_t g = 3u * t;
-            int c, x, y, z, j0;
-            if (direct) {
-                const unsigned e = reinterpret_cast<const uint16_t*>(W.ibase)[t];
-                x = (int)(e & 15u);
-                y = (int)((e >> 4) & 15u);
-                z = (int)((e >> 8) & 15u);
-                j0 = 3 * (int)(e >> 12);
-                c = (x * N + y) * N + z;
-            } else {
-                uint32_t ai = 0, len = nA;
-                while (len > 1) {
-                    const uint32_t h = len >> 1;
-                    if (W.get_ibase(ai + h) <= g) ai += h;
-                    len -= h;
-                }
-                c = W.get_active(ai);
-                x = c / (N * N);
-                y = (c / N) % N;
-                z = c % N;
-                j0 = (int)(g - W.get_ibase(ai));
-            }
-            const int cs = cases[c];
-            const int8_t* row = T.tri[cs];
-            const unsigned own_mask = T.owned[oriented][boundary_flags(x, y, z, N)];
-            const unsigned fr = T.first_ref[cs];
-            const uint32_t vb = W.get_vbase(c);
-            const uint16_t* before = UWW_EDGE_BEFORE[cs];
-#pragma unroll
-            for (int m = 0; m < 3; ++m) {
-                const int i = j0 + m;
-                const int e = row[i];
-                const unsigned bit = 1u << e;
-                uint32_t id;
-                if (own_mask & bit) {
-                    // the cell numbers its owned edges' vertices in first-reference order
-                    id = vb + __popc(own_mask & __ldg(before + e));
-                    if ((fr >> i) & 1u) {
-                        const int ca = T.corners[e][0], cb = T.corners[e][1];
-                        const int ax = x + ((0x66 >> ca) & 1), ay = y + (ca >> 2), az = z + ((0xcc >> ca) & 1);
-                        const int bx = x + ((0x66 >> cb) & 1), by = y + (cb >> 2), bz = z + ((0xcc >> cb) & 1);
-                        const float ia = rho[(ax * S + ay) * S + az];
-                        const float ibv = rho[(bx * S + by) * S + bz];
-                        const float sax = O::mul((float)ax, s), say = O::mul((float)ay, s), saz = O::mul((float)az, s);
-                        const float sbx = O::mul((float)bx, s), sby = O::mul((float)by, s), sbz = O::mul((float)bz, s);
-                        const float tt = O::div(O::sub(iso, ia), O::sub(ibv, ia));
-                        const float mx = O::add(sax, O::mul(tt, O::sub(sbx, sax)));
-                        const float my = O::add(say, O::mul(tt, O::sub(sby, say)));
-                        const float mz = O::add(saz, O::mul(tt, O::sub(sbz, saz)));
-                        if (a.edge_ids) {
-                            // direction of corner b from corner a: +x -x +y -y +z -z
-                            const int dir = bx != ax ? (bx < ax) : by != ay ? 2 + (by < ay) : 4 + (bz < az);
-                            a.edge_ids[voff + id] = ((uint32_t)((ax * S + ay) * S + az) << 3) | (uint32_t)dir;
-                        }
-                        float2* v2 = reinterpret_cast<float2*>(a.verts + voff + id);
-                        v2[0] = make_float2(O::add(mx, (float)ox), O::add(my, (float)oy));
-                        // colour slot 0 carries the owner's corner b (the value ramp's
-                        // input, chunk.rs:215) to pass 2, which overwrites it
-                        v2[1] = make_float2(O::add(mz, (float)oz), (want_color || want_normals) ? (float)cb : 0.f);
-                        v2[2] = make_float2(0.f, 0.f);
-                    }
-                } else {
-                    // the owner: the first cell in stream order holding this edge
-                    const int ow = T.owner[oriented][(x == 0) | ((y == 0) << 1) | ((z == 0) << 2)][e];
-                    const int qx = x - ((ow >> 4) & 1), qy = y - ((ow >> 5) & 1), qz = z - ((ow >> 6) & 1);
-                    const int oe = ow & 15;
-                    const int oc = (qx * N + qy) * N + qz;
-                    const unsigned oown = T.owned[oriented][boundary_flags(qx, qy, qz, N)];
-                    id = W.get_vbase(oc) + __popc(oown & __ldg(&UWW_EDGE_BEFORE[cases[oc]][oe]));
-                }
-                a.inds[ioff + g + m] = id;
-            }
-        }
+        for (uint32_t t = tid; t < nT; t += ncomp)
+            emit_triangle<O>(p, EmitOut{a.verts, a.inds, a.edge_ids}, T, W, N, nA, direct, t, voff, ioff, ox, oy, oz, s,
+                             want_color || want_normals);
     }
     // pass 2 (colour and normal per vertex): inline for one chunk per launch
     // and for streamed host output; otherwise the batched form runs it as
@@ -812,20 +879,12 @@ __device__ void decided_tail(const DevParams& p, const BuildArgs& a, SmemTables&
     if (lane == 0) T.overflow += over;
 }
 
-// MAXT/MINB: the launch bounds of an instantiation.  Chunks of up to 16 cells
-// per edge run with <= 224 threads (192 compute + the control warp) and at
-// least 4 CTAs per SM (<= 72
-// registers); larger chunks run with up to 544 threads.
-template <class O, bool QUEUE, int MAXT, int MINB>
-__global__ void __launch_bounds__(MAXT, MINB) build_kernel(const DevParams p, const BuildArgs a)
+// Per-CTA setup: the marching-cubes tables, the permutation and its gradient
+// table into shared memory (coalesced loads from global memory; per-thread
+// addresses into the constant bank would be serialised).  The caller
+// synchronises the CTA before use.
+__device__ __forceinline__ void load_tables(const DevParams& p, SmemTables& T, int tid, int nthr)
 {
-    extern __shared__ __align__(16) uint8_t dyn_smem[];
-    __shared__ SmemTables T;
-    const int tid = threadIdx.x, nthr = blockDim.x;
-    // batched form: the last warp is the control warp
-    const int ncomp = QUEUE ? nthr - 32 : nthr;
-
-    // ---- per-CTA setup: tables into shared memory ----
     {
         const int4* src = reinterpret_cast<const int4*>(&UWW_TRI_TABLE[0][0]);
         int4* dst = reinterpret_cast<int4*>(&T.tri[0][0]);
@@ -855,6 +914,22 @@ __global__ void __launch_bounds__(MAXT, MINB) build_kernel(const DevParams p, co
         grad_vec(T.perm[i], gx, gy, gz);
         T.gp[i] = make_float4(gx, gy, gz, 0.f);
     }
+}
+
+// MAXT/MINB: the launch bounds of an instantiation.  Chunks of up to 16 cells
+// per edge run with <= 224 threads (192 compute + the control warp) and at
+// least 4 CTAs per SM (<= 72
+// registers); larger chunks run with up to 544 threads.
+template <class O, bool QUEUE, int MAXT, int MINB>
+__global__ void __launch_bounds__(MAXT, MINB) build_kernel(const DevParams p, const BuildArgs a)
+{
+    extern __shared__ __align__(16) uint8_t dyn_smem[];
+    __shared__ SmemTables T;
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    // batched form: the last warp is the control warp
+    const int ncomp = QUEUE ? nthr - 32 : nthr;
+
+    load_tables(p, T, tid, nthr);
     // a planned batch reads the chunk list of the planning kernel launched
     // just before it (as a programmatic dependent: the table setup above
     // overlaps the planning)
@@ -1045,6 +1120,322 @@ __global__ void __launch_bounds__(kPlanThreads) plan_kernel(const DevParams p, c
     for (uint32_t j = tid; j < first; j += kPlanThreads) decided_record(a, j, __ldcg(&kinds[j]), 0ull, 0ull);
 }
 
+// ---------------------------------------------------------------------------
+// Split build, for batches whose chunks all work in shared memory: the front
+// half and the emission run as separate kernels instead of one pipelined one.
+//   split_plan_kernel (planned batches): one pass, one thread per chunk -- a
+//     chunk the depth bias decides gets its counts word (zero, early-blank
+//     flag) at once; the others go to one of kPlanRanks work queues by cost
+//     rank (bias_decides_with), the likely costliest first.
+//   front_kernel: persistent, every thread a compute thread, one chunk per CTA
+//     at a time from the queues -- noise, votes, classification and block scan
+//     (chunk_front); a meshed chunk's workspace goes to its slot, its counts
+//     to tinfo and to its tile's sum, the chunk to the mesh list.  No
+//     look-back, no control warp, no hand-offs, no ordering between CTAs.
+//   emit_kernel, the front kernel's programmatic dependent (its CTAs load
+//     their tables as front CTAs finish): per CTA a meshed chunk, its slot
+//     copied to shared memory asynchronously (cp.async) while the CTA writes
+//     the records of a tile of chunks and sums its chunk's prefix from the
+//     tile sums; then one thread per triangle as in the pipelined back half,
+//     then the chunk's vertices' colours and normals (pass 2).  The last CTA
+//     writes the totals and leaves the counters zero.
+// The same device functions as the pipelined build: the same bits.  The work
+// order (queues, mesh list) varies from run to run; the outputs do not.
+
+__device__ __forceinline__ Workspace workspace_at(uint8_t* base, int N)
+{
+    const ChunkLayout L = chunk_layout(N);
+    Workspace w;
+    w.rho = reinterpret_cast<float*>(base + L.rho);
+    w.cases = base + L.cases;
+    w.vbase = base + L.vbase;
+    w.active = base + L.active;
+    w.ibase = base + L.ibase;
+    w.idx16 = L.idx16;
+    w.active16 = L.active16;
+    return w;
+}
+
+// counts word of a chunk the depth bias decides (kind 1: every sample above
+// the iso level -- early blank; 2: every sample below it)
+__device__ __forceinline__ unsigned long long decided_info(int kind) { return kind == 1 ? kInfoEarlyBlank : 0ull; }
+
+__global__ void __launch_bounds__(kPlanThreads) split_plan_kernel(const DevParams p, const BuildArgs a)
+{
+    // the front kernel may start its table setup now; it waits for this
+    // grid's writes (griddepcontrol.wait) before taking work
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    const uint32_t n = a.n_dev ? min(*a.n_dev, a.n) : a.n;
+    const float B = fbm_bound(p);
+    for (uint32_t i = blockIdx.x * kPlanThreads + threadIdx.x; i < n; i += gridDim.x * kPlanThreads) {
+        const uint32_t cells = __ldg(&a.chunks[i].cells);
+        const int oz = __ldg(&a.chunks[i].pos[2]) * p.chunk_size;
+        const bool ok = cells >= 1 && cells <= a.max_cells && cells <= UWW_MAX_CELLS;
+        int rank = 0;
+        const int kind =
+            ok ? bias_decides_with(p, B, __fdiv_rn((float)p.chunk_size, (float)cells), (int)cells, oz, &rank) : 0;
+        if (kind) {
+            a.tinfo[i] = decided_info(kind);
+        } else {
+            // (the counters are zero at launch, so pos < n; checked all the same)
+            const uint32_t pos = atomicAdd(&a.split_ctr[kCtrQueued + rank], 1u);
+            if (pos < a.n) a.split_queue[(size_t)rank * a.n + pos] = i;
+        }
+    }
+}
+
+// Exclusive scan of two u64 components over the CTA in thread order; the
+// totals go to *ta, *tb.  Every thread calls it.
+__device__ __forceinline__ void block_scan2(unsigned long long& a, unsigned long long& b, unsigned long long* ta,
+                                            unsigned long long* tb, SmemTables& T)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    unsigned long long ia = a, ib = b;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned long long xa = __shfl_up_sync(0xffffffffu, ia, o), xb = __shfl_up_sync(0xffffffffu, ib, o);
+        if (lane >= o) { ia += xa; ib += xb; }
+    }
+    if (lane == 31) { T.warp_sums[warp] = ia; T.warp_sums2[warp] = ib; }
+    __syncthreads();
+    if (warp == 0) {
+        const unsigned long long wa = lane < nw ? T.warp_sums[lane] : 0ull, wb = lane < nw ? T.warp_sums2[lane] : 0ull;
+        unsigned long long sa = wa, sb = wb;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned long long xa = __shfl_up_sync(0xffffffffu, sa, o), xb = __shfl_up_sync(0xffffffffu, sb, o);
+            if (lane >= o) { sa += xa; sb += xb; }
+        }
+        if (lane < nw) { T.warp_sums[lane] = sa - wa; T.warp_sums2[lane] = sb - wb; }
+        if (lane == nw - 1) { T.chunk_total = sa; T.chunk_total2 = sb; }
+    }
+    __syncthreads();
+    a = T.warp_sums[warp] + ia - a;
+    b = T.warp_sums2[warp] + ib - b;
+    *ta = T.chunk_total;
+    *tb = T.chunk_total2;
+    __syncthreads();  // the shared words are free for the next call
+}
+
+// The split build's next piece of work for this CTA (thread 0): a chunk from
+// the first queue with work left (planned), else the next chunk in order;
+// kNoChunk when there is none.
+constexpr uint32_t kNoChunk = 0xffffffffu;
+__device__ __forceinline__ uint32_t split_take(const BuildArgs& a, uint32_t nchunks, uint32_t& rank)
+{
+    if (!a.split_planned) {
+        const uint32_t k = atomicAdd(&a.split_ctr[kCtrTaken], 1u);
+        return k < nchunks ? k : kNoChunk;
+    }
+    while (rank < (uint32_t)kPlanRanks) {
+        const uint32_t k = atomicAdd(&a.split_ctr[kCtrTaken + rank], 1u);
+        if (k < min(__ldcg(&a.split_ctr[kCtrQueued + rank]), a.n)) return __ldcg(&a.split_queue[(size_t)rank * a.n + k]);
+        ++rank;
+    }
+    return kNoChunk;
+}
+
+template <class O, int MAXT, int MINB>
+__global__ void __launch_bounds__(MAXT, MINB) front_kernel(const DevParams p, const BuildArgs a)
+{
+    extern __shared__ __align__(16) uint8_t dyn_smem[];
+    __shared__ SmemTables T;
+    __shared__ uint32_t rank;
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    load_tables(p, T, tid, nthr);
+    // the planning kernel's queues (this kernel is its programmatic dependent)
+    if (a.split_planned) asm volatile("griddepcontrol.wait;" ::: "memory");
+    // the emission kernel, launched after this one as its programmatic
+    // dependent, may take SMs as this kernel's CTAs finish (it loads its
+    // tables, then waits for the whole front kernel before reading any of it)
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    if (tid == 0) {
+        T.errflags = 0;
+        T.nchunks = a.n_dev ? min(*a.n_dev, a.n) : a.n;
+        rank = 0;
+        // the emission kernel adds the chunks that do not fit
+        if (blockIdx.x == 0) a.totals[2] = 0ull;
+    }
+    __syncthreads();
+    for (;;) {
+        if (tid == 0) {
+            const uint32_t c = split_take(a, T.nchunks, rank);
+            T.tk[0].chunk = c;
+            if (c != kNoChunk) T.tk[0].desc = a.chunks[c];
+        }
+        __syncthreads();
+        const uint32_t c = T.tk[0].chunk;
+        if (c == kNoChunk) break;
+        chunk_front<O, false>(p, a, T, dyn_smem, T.tk[0].desc, c, c, 0, nthr);
+        __syncthreads();
+        const ChunkInfo ci = T.ci[0];
+        const uint32_t nV = (uint32_t)(ci.total & kField22), nI = (uint32_t)((ci.total >> kIndShift) & kField22);
+        if (tid == 0) {
+            a.tinfo[c] = ci.total | ((ci.flags & UWW_CHUNK_EARLY_BLANK) ? kInfoEarlyBlank : 0ull);
+            if (nV | nI) atomicAdd(&a.tile_sum[c / kTileChunks], (unsigned long long)nV | ((unsigned long long)nI << 32));
+            if (nI) {
+                const uint32_t m = atomicAdd(&a.split_ctr[kCtrMeshed], 1u);
+                if (m < a.n) a.mesh_list[m] = c;
+            }
+        }
+        if (nI) {
+            // the workspace (samples, cases, vertex bases, triangle map or
+            // active list) to the chunk's slot, in 16-byte words
+            const uint32_t words = chunk_layout(ci.N).total / 16u;
+            const uint4* src = reinterpret_cast<const uint4*>(dyn_smem);
+            uint4* dst = reinterpret_cast<uint4*>(a.slots + (size_t)c * a.slot_bytes);
+            for (uint32_t i = tid; i < words; i += nthr) dst[i] = src[i];
+        }
+        __syncthreads();  // the workspace and the staged ticket are reused
+    }
+    if (tid == 0 && T.errflags) atomicOr(&a.acc[1], (unsigned long long)T.errflags);
+}
+
+// Sum over the CTA of the counts of the chunks before chunk c: the tile sums
+// of the tiles before its tile, then the chunks of its tile before it.  Every
+// thread calls it; returns verts | inds << 32 (each saturated to 32 bits).
+__device__ __forceinline__ unsigned long long chunk_prefix(const BuildArgs& a, uint32_t c, SmemTables& T)
+{
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    const uint32_t tile = c / kTileChunks, t0 = tile * kTileChunks;
+    unsigned long long v = 0ull, i = 0ull;
+    for (uint32_t k = tid; k < tile; k += nthr) {
+        const unsigned long long w = __ldcg(&a.tile_sum[k]);
+        v += w & 0xffffffffull;
+        i += w >> 32;
+    }
+    for (uint32_t j = t0 + tid; j < c; j += nthr) {
+        const unsigned long long w = __ldcg(&a.tinfo[j]);
+        v += w & kField22;
+        i += (w >> kIndShift) & kField22;
+    }
+    unsigned long long tv = 0ull, ti = 0ull;
+    block_scan2(v, i, &tv, &ti, T);
+    return rec_off32(tv) | ((unsigned long long)rec_off32(ti) << 32);
+}
+
+template <class O>
+__global__ void __launch_bounds__(256, 4) emit_kernel(const DevParams p, const BuildArgs a)
+{
+    extern __shared__ __align__(16) uint8_t dyn_smem[];
+    __shared__ SmemTables T;
+    __shared__ int last;
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    load_tables(p, T, tid, nthr);
+    // launched as a programmatic dependent of the front kernel: everything it
+    // wrote is read after this, and through L2 (no L1 line of it can be stale)
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    const uint32_t nchunks = a.n_dev ? min(*a.n_dev, a.n) : a.n;
+    const uint32_t nmesh = min(__ldcg(&a.split_ctr[kCtrMeshed]), a.n);
+    const uint32_t ntiles = (nchunks + kTileChunks - 1) / kTileChunks;
+    // this CTA's first meshed chunk: its slot on its way to shared memory
+    // while the records are written and its prefix is summed
+    uint32_t c = blockIdx.x < nmesh ? __ldcg(&a.mesh_list[blockIdx.x]) : kNoChunk;
+    auto copy_slot = [&](uint32_t ch) {
+        const uint32_t words = chunk_layout((int)a.chunks[ch].cells).total / 16u;
+        const uint8_t* src = a.slots + (size_t)ch * a.slot_bytes;
+        for (uint32_t k = tid; k < words; k += nthr) {
+            const uint32_t dst = (uint32_t)__cvta_generic_to_shared(dyn_smem + 16u * k);
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src + 16u * k) : "memory");
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+    if (c != kNoChunk) copy_slot(c);
+    // the records, a tile of kTileChunks chunks per CTA (one per thread)
+    unsigned long long over = 0;
+    for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const uint32_t j = tile * kTileChunks + tid;
+        const unsigned long long w = j < nchunks ? __ldcg(&a.tinfo[j]) : 0ull;
+        const uint32_t nV = (uint32_t)(w & kField22), nI = (uint32_t)((w >> kIndShift) & kField22);
+        unsigned long long tv = 0ull, ti = 0ull, pv = 0ull, pi = 0ull;
+        for (uint32_t k = tid; k < tile; k += nthr) {
+            const unsigned long long s = __ldcg(&a.tile_sum[k]);
+            pv += s & 0xffffffffull;
+            pi += s >> 32;
+        }
+        block_scan2(pv, pi, &tv, &ti, T);  // tv, ti: the tiles before this one
+        unsigned long long ev = nV, ei = nI, sv = 0ull, si = 0ull;
+        block_scan2(ev, ei, &sv, &si, T);
+        ev += tv;
+        ei += ti;
+        if (j < nchunks) {
+            const bool fits = ev + nV <= a.vert_capacity && ei + nI <= a.ind_capacity;
+            uww_chunk_record rec;
+            rec.num_verts = nV;
+            rec.num_inds = nI;
+            rec.vert_offset = rec_off32(ev);
+            rec.ind_offset = rec_off32(ei);
+            rec.flags = ((w & kInfoEarlyBlank) ? UWW_CHUNK_EARLY_BLANK : 0u) | (nI ? UWW_CHUNK_HAS_MESH : 0u) |
+                        (fits ? 0u : UWW_CHUNK_OVERFLOW);
+            rec.num_active_cells = (uint32_t)((w >> kActShift) & 0x3ffffull);
+            rec.reserved[0] = rec.reserved[1] = 0;
+            a.records[j] = rec;
+            over += fits ? 0u : 1u;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) over += __shfl_xor_sync(0xffffffffu, over, o);
+    if ((tid & 31) == 0 && over) atomicAdd(&a.totals[2], over);
+    // the meshed chunks, one per CTA at a time: pass 1 (one thread per
+    // triangle), then pass 2 over the chunk's vertices (colour and normal)
+    const bool want_color = (p.outputs & UWW_OUT_COLOR) != 0;
+    const bool want_normals = (p.outputs & UWW_OUT_NORMALS) != 0 && a.normals != nullptr;
+    for (uint32_t m = blockIdx.x; m < nmesh; m += gridDim.x) {
+        if (m != blockIdx.x) {
+            c = __ldcg(&a.mesh_list[m]);
+            __syncthreads();  // the previous chunk is done with the workspace
+            copy_slot(c);
+        }
+        const unsigned long long pre = chunk_prefix(a, c, T);
+        const unsigned long long w = __ldcg(&a.tinfo[c]);
+        const uww_chunk_desc d = a.chunks[c];
+        asm volatile("cp.async.wait_all;" ::: "memory");
+        __syncthreads();
+        const uint32_t nV = (uint32_t)(w & kField22), nI = (uint32_t)((w >> kIndShift) & kField22);
+        const uint32_t voff = (uint32_t)pre, ioff = (uint32_t)(pre >> 32);
+        if ((unsigned long long)voff + nV > a.vert_capacity || (unsigned long long)ioff + nI > a.ind_capacity) continue;
+        const int N = (int)d.cells;
+        const Workspace W = workspace_at(dyn_smem, N);
+        const uint32_t nT = nI / 3u, nA = (uint32_t)((w >> kActShift) & 0x3ffffull);
+        const bool direct = direct_triangles(W, N, w & (kInfoEarlyBlank - 1));
+        const float s = __fdiv_rn((float)p.chunk_size, (float)N);
+        const EmitOut eo{a.verts, a.inds, a.edge_ids};
+        for (uint32_t tr = tid; tr < nT; tr += nthr)
+            emit_triangle<O>(p, eo, T, W, N, nA, direct, tr, voff, ioff, d.pos[0] * p.chunk_size,
+                             d.pos[1] * p.chunk_size, d.pos[2] * p.chunk_size, s, want_color || want_normals);
+        if (want_color || want_normals) {
+            __syncthreads();  // the chunk's vertex positions, written by this CTA
+            for (uint32_t v = tid; v < nV; v += nthr)
+                finish_vertex<O>(p, T.perm, T.gp, a.verts, a.normals, voff + v, want_color, want_normals);
+        }
+    }
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    // the last CTA: the totals, and the tile sums and counters left zero for
+    // the next launch
+    __syncthreads();
+    if (tid == 0) {
+        __threadfence();
+        last = atomicAdd(&a.split_ctr[kCtrDone], 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    unsigned long long v = 0ull, i = 0ull, tv = 0ull, ti = 0ull;
+    for (uint32_t k = tid; k < ntiles; k += nthr) {
+        const unsigned long long s = __ldcg(&a.tile_sum[k]);
+        v += s & 0xffffffffull;
+        i += s >> 32;
+    }
+    block_scan2(v, i, &tv, &ti, T);
+    for (uint32_t k = tid; k < ntiles; k += nthr) a.tile_sum[k] = 0ull;
+    if (tid == 0) {
+        a.totals[0] = tv;
+        a.totals[1] = ti;
+        a.totals[3] = atomicExch(&a.acc[1], 0ull);
+    }
+    if (tid < kCtrWords) a.split_ctr[tid] = 0u;
+}
+
 // Pass 2 of the batched build over every vertex of the batch: vertex counts
 // are very uneven across chunks, so the per-vertex colour and analytic-normal
 // work is spread over the whole GPU instead of staying with the CTA that
@@ -1142,14 +1533,29 @@ size_t set_smem_attr(BuildFn fn, size_t optin)
     return 0;
 }
 
+using FrontFn = void (*)(const DevParams, const BuildArgs);
+
+// The split build's emission kernel.
+FrontFn emit_for(bool exact) { return exact ? emit_kernel<ExactOps> : emit_kernel<FastOps>; }
+
+// The split build's front kernel for a CTA of `threads` (<= 256) threads.
+FrontFn front_for(bool exact, int threads)
+{
+    if (threads <= 192) return exact ? front_kernel<ExactOps, 192, 4> : front_kernel<FastOps, 192, 4>;
+    return exact ? front_kernel<ExactOps, 256, 3> : front_kernel<FastOps, 256, 3>;
+}
+
 }  // namespace
 
 cudaError_t prepare_build_kernels(size_t optin, size_t* max_dyn_smem)
 {
     size_t m = ~size_t(0);
-    for (int e = 0; e < 2; ++e)
+    for (int e = 0; e < 2; ++e) {
         for (int q = 0; q < 2; ++q)
             for (int l = 0; l < 2; ++l) m = std::min(m, set_smem_attr(kernel_for(e, q, l), optin));
+        for (int th : {192, 256}) m = std::min(m, set_smem_attr(front_for(e, th), optin));
+        m = std::min(m, set_smem_attr(emit_for(e), optin));
+    }
     *max_dyn_smem = m;
     return m >= 16384 ? cudaSuccess : cudaErrorInvalidValue;
 }
@@ -1160,12 +1566,54 @@ cudaError_t build_occupancy(bool queue, bool exact, int threads, size_t dyn_smem
                                                          threads, dyn_smem);
 }
 
+cudaError_t front_occupancy(bool exact, int threads, size_t dyn_smem, int* blocks_per_sm)
+{
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, front_for(exact, threads), threads, dyn_smem);
+}
+
 cudaError_t launch_build(const DevParams& p, const BuildArgs& a, bool queue, int grid, int threads, size_t dyn_smem,
                          cudaStream_t s)
 {
     const bool exact = p.math_mode == UWW_MATH_EXACT;
     cudaError_t e = cudaSuccess;
-    if (queue && a.plan) {
+    if (queue && a.slots) {
+        // the split build: [planning ->] front -> emission (-> vertex pass below)
+        if (a.split_planned) {
+            const uint32_t nblk = std::max(1u, std::min((a.n + kPlanThreads - 1) / kPlanThreads, 1024u));
+            split_plan_kernel<<<nblk, kPlanThreads, 0, s>>>(p, a);
+            if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        }
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)grid);
+        cfg.blockDim = dim3((unsigned)threads);
+        cfg.dynamicSmemBytes = dyn_smem;
+        cfg.stream = s;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = a.split_planned ? 1 : 0;
+        if ((e = cudaLaunchKernelEx(&cfg, front_for(exact, threads), p, a)) != cudaSuccess) return e;
+        // the emission (with pass 2) as the front kernel's programmatic
+        // dependent: its CTAs load their tables as front CTAs finish
+        int dev = 0, sms = 0, ebps = 0;
+        const FrontFn efn = emit_for(exact);
+        e = cudaGetDevice(&dev);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ebps, efn, 256, a.slot_bytes);
+        if (e != cudaSuccess) return e;
+        cudaLaunchConfig_t ecfg = {};
+        ecfg.gridDim = dim3((unsigned)std::max(1, sms * std::max(1, ebps)));
+        ecfg.blockDim = dim3(256);
+        ecfg.dynamicSmemBytes = a.slot_bytes;
+        ecfg.stream = s;
+        cudaLaunchAttribute pdl[1];
+        pdl[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        pdl[0].val.programmaticStreamSerializationAllowed = 1;
+        ecfg.attrs = pdl;
+        ecfg.numAttrs = 1;
+        return cudaLaunchKernelEx(&ecfg, efn, p, a);
+    } else if (queue && a.plan) {
         // the planning kernel, then the build as its programmatic dependent
         const uint32_t nblk = std::max(1u, std::min((a.n + kPlanThreads - 1) / kPlanThreads, 1024u));
         plan_kernel<<<nblk, kPlanThreads, 0, s>>>(p, a);

@@ -59,6 +59,16 @@ constexpr uint32_t kPlanDone = 0, kPlanCount = 1, kPlanList = 2;
 __host__ __device__ inline size_t plan_kinds_offset(uint32_t n) { return ((size_t)n + kPlanList) * sizeof(uint32_t); }
 __host__ __device__ inline size_t plan_buffer_bytes(uint32_t n) { return plan_kinds_offset(n) + n; }
 
+// Split build (uww_build.cu): chunks per tile of the tile sums (the emission
+// kernel writes a tile's records with one thread per chunk), cost ranks of
+// the planning kernel's work queues, and the words of the counter block:
+// [kCtrQueued + r] chunks queued at rank r, [kCtrTaken + r] taken from queue
+// r, the meshed chunks, the emission CTAs finished.  All zero between
+// launches.
+constexpr uint32_t kTileChunks = 256;
+constexpr int kPlanRanks = 8;
+constexpr uint32_t kCtrQueued = 0, kCtrTaken = 8, kCtrMeshed = 16, kCtrDone = 17, kCtrWords = 32;
+
 // Lookback word: [63:62] status, [61:30] indices, [29:0] vertices.
 constexpr unsigned long long kLbAggregate = 1ull << 62;
 constexpr unsigned long long kLbInclusive = 2ull << 62;
@@ -102,6 +112,18 @@ struct BuildArgs {
     uint32_t* edge_ids;              // optional, per output vertex: (first corner sample << 3) | direction
     const uint32_t* n_dev;           // optional device chunk count; the launch builds min(*n_dev, n)
     uint32_t* plan;                  // planned batch: finish counter, count, list (plan_kernel; kPlan*)
+    // Split build (every chunk in shared memory, no streamed host output).
+    // Per chunk c: its counts word tinfo[c] (packed counts, early-blank flag
+    // in bit 62) and, when meshed, its workspace in slot c; per tile of
+    // kTileChunks chunks the sum of its counts (verts | inds << 32).
+    uint8_t* slots;                  // chunks x slot_bytes, 16-byte aligned
+    size_t slot_bytes;
+    unsigned long long* tinfo;
+    unsigned long long* tile_sum;    // zero at launch; re-zeroed by the emission kernel's last CTA
+    uint32_t* mesh_list;             // the meshed chunks, in the order the front kernel finished them
+    uint32_t* split_queue;           // planned: kPlanRanks work queues of n entries
+    uint32_t* split_ctr;             // kCtrWords counters, zero at launch (kCtr*)
+    uint32_t split_planned;          // the planning kernel runs first and fills the queues
     // Optional streamed host output (batched form): device addresses of
     // page-locked host memory.  Pass 2 then runs inside the build kernel, and
     // each chunk's record, indices, vertices and normals go there as soon as
@@ -141,6 +163,8 @@ int default_compute_threads(uint32_t max_cells);
 cudaError_t launch_build(const DevParams& p, const BuildArgs& a, bool queue, int grid, int threads,
                          size_t dyn_smem, cudaStream_t s);
 cudaError_t build_occupancy(bool queue, bool exact, int threads, size_t dyn_smem, int* blocks_per_sm);
+// the split build's front kernel: resident CTAs per SM for this shape
+cudaError_t front_occupancy(bool exact, int threads, size_t dyn_smem, int* blocks_per_sm);
 cudaError_t prepare_build_kernels(size_t optin, size_t* max_dyn_smem);
 cudaError_t launch_density(const DevParams& p, const float* xyz, uint32_t n, float* out, cudaStream_t s);
 
@@ -152,7 +176,9 @@ int check_mesh_out(const uww_mesh_out* out);
 // a later launch can be captured into a CUDA graph)
 int prepare_batched(uww_ctx* ctx, uint32_t n, uint32_t max_cells, const uww_mesh_out* out);
 // the launch shape a batched build of n chunks would use
-int plan_batched(uww_ctx* ctx, uint32_t n, uint32_t max_cells, int* threads, int* grid, size_t* dyn_smem);
+// and the resident CTAs per SM of its (front) kernel
+int plan_batched(uww_ctx* ctx, uint32_t n, uint32_t max_cells, int* threads, int* grid, size_t* dyn_smem,
+                 int* occupancy);
 // (re)allocate *ptr to at least `bytes` of device memory (contents not kept)
 int ensure_device_bytes(void** ptr, size_t* cap, size_t bytes);
 // The build writes vertex positions and the totals with 8-byte stores and
@@ -198,6 +224,9 @@ struct uww_ctx {
     size_t lookback_cap = 0;
     uint32_t* d_plan = nullptr;   // planned batch: chunk count + list
     size_t plan_cap = 0;
+    uint8_t* d_split = nullptr;   // split build: counters, tile sums, counts, queues, slots
+    size_t split_cap = 0;
+    uint32_t split_n = 0;         // the chunk count its layout is made for
     unsigned long long* d_state = nullptr;
     unsigned int* d_counter = nullptr;
     unsigned long long* d_acc = nullptr;

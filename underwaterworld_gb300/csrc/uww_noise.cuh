@@ -146,7 +146,8 @@ __device__ __forceinline__ float fbm_bound(const DevParams& p)
 // planning kernel and the build kernel reach the same decision.
 // B = fbm_bound(p) and s = chunk_size / N passed in (per-launch and per-LOD
 // constants).
-__device__ __forceinline__ int bias_decides_with(const DevParams& p, float B, float s, int N, int oz)
+__device__ __forceinline__ int bias_decides_with(const DevParams& p, float B, float s, int N, int oz,
+                                                 int* rank = nullptr)
 {
     float lo = 3.0e38f, hi = -3.0e38f;
     bool ok = true;
@@ -164,6 +165,13 @@ __device__ __forceinline__ int bias_decides_with(const DevParams& p, float B, fl
     if (p.bias_mode == UWW_BIAS_TERRACED) m = __fadd_rn(m, fabsf(p.bias_c));
     if (__fsub_rn(__fsub_rn(lo, B), m) > iso) return 1;
     if (__fadd_rn(__fadd_rn(hi, B), m) < iso) return 2;
+    if (rank) {
+        // how far the bias range stays from the iso level, in eighths of the
+        // reach B + m: 0 when it contains the iso level (such a chunk most
+        // likely holds the surface, and meshing makes it the costliest)
+        const float gap = lo > iso ? lo - iso : (hi < iso ? iso - hi : 0.f);
+        *rank = min(7, (int)(8.f * gap / (B + m)));
+    }
     return 0;
 }
 

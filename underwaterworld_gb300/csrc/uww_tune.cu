@@ -270,9 +270,8 @@ int uww_autotune(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint3
             ctx->blocks_per_sm = 0;
             int thr = 0, grid = 0;
             size_t dyn = 0;
-            if (plan_batched(ctx, n, max_cells, &thr, &grid, &dyn)) continue;
             int occ = 0;
-            if (build_occupancy(true, ctx->dev.math_mode == UWW_MATH_EXACT, thr, dyn, &occ) != cudaSuccess || occ < 1) {
+            if (plan_batched(ctx, n, max_cells, &thr, &grid, &dyn, &occ) || occ < 1) {
                 cudaGetLastError();
                 continue;
             }

@@ -88,6 +88,7 @@ class Tuning(C.Structure):
 
 UWW_TEST_WITHHOLD_FIRST = 1
 UWW_TUNE_NO_DEPTH_SHORTCUT = 1
+UWW_TUNE_PIPELINED = 2
 
 
 assert C.sizeof(ChunkDesc) == 32 and C.sizeof(ChunkRecord) == 32 and C.sizeof(Tuning) == 32
