@@ -144,6 +144,7 @@ struct LaunchCfg {
     size_t dyn_smem;
     int grid;
     int occupancy;         // resident CTAs per SM of the build's (front) kernel
+    uint32_t mask_offset;  // split front kernel: column masks in dynamic shared memory (0: none)
     size_t scratch_slot;
     bool split;            // the split build: front kernel, then emission over every triangle
 };
@@ -183,6 +184,16 @@ int plan_launch(uww_ctx* ctx, uint32_t n, uint32_t max_cells, bool queue, Launch
     cfg->smem_buf = smem_cells > 0 ? chunk_layout((int)smem_cells).total : 0;
     cfg->ztable_offset = (size_t)slots * cfg->smem_buf;
     cfg->dyn_smem = cfg->ztable_offset + zt;
+    // the split front kernel's 13^3-sample chunks (register-column noise)
+    // also keep each column's below-iso mask, for the classification
+    cfg->mask_offset = 0;
+    if (cfg->split && ctx->dev.math_mode == UWW_MATH_FAST && max_cells == 12) {
+        const size_t mo = (cfg->dyn_smem + 15) & ~size_t(15);
+        if (mo + 13 * 13 * sizeof(unsigned long long) <= cap) {
+            cfg->mask_offset = (uint32_t)mo;
+            cfg->dyn_smem = mo + 13 * 13 * sizeof(unsigned long long);
+        }
+    }
     // compute threads: by default 192 for chunks of up to 12 cells (one per
     // sample column of a 13^3 grid), 256 up to 16 cells (two CTAs per SM) and
     // 512 above (one CTA per SM: a 25^2-column chunk in global scratch is
@@ -260,6 +271,7 @@ int launch(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint32_t ma
     a.slots_per_cta = cfg.slots;
     a.smem_buf_bytes = cfg.smem_buf;
     a.ztable_offset = cfg.ztable_offset;
+    a.mask_offset = cfg.mask_offset;
     a.smem_cells = cfg.smem_cells;
     a.spin_limit_cycles = ctx->spin_limit > 0 ? ctx->spin_limit : kSpinLimitCycles;
     a.withhold_first = (ctx->test_flags & UWW_TEST_WITHHOLD_FIRST) ? 1u : 0u;

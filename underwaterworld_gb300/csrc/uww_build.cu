@@ -386,10 +386,15 @@ __device__ void chunk_front(const DevParams& p, const BuildArgs& a, SmemTables& 
     const int ox = d.pos[0] * p.chunk_size, oy = d.pos[1] * p.chunk_size, oz = d.pos[2] * p.chunk_size;
     // a chunk in global scratch leaves the shared workspace `buf` free: its
     // columns' inside bits go there (fast build, up to 64 samples a column)
+    // a 13^3-sample chunk in shared memory (register-column noise) writes
+    // them to the mask area when the launch has one
     unsigned long long* masks =
         (std::is_same<O, FastOps>::value && (uint32_t)N > a.smem_cells && S <= 64 && !a.samples_in &&
          (size_t)S * S * sizeof(unsigned long long) <= a.smem_buf_bytes)
             ? reinterpret_cast<unsigned long long*>(dyn_smem + (size_t)buf * a.smem_buf_bytes)
+        : (std::is_same<O, FastOps>::value && (uint32_t)N <= a.smem_cells && S == 13 && !a.samples_in &&
+           a.mask_offset)
+            ? reinterpret_cast<unsigned long long*>(dyn_smem + a.mask_offset)
             : nullptr;
 
     // ---- density grid (build_iso) + early blank and solid votes ----
@@ -415,7 +420,7 @@ __device__ void chunk_front(const DevParams& p, const BuildArgs& a, SmemTables& 
             // chunk in a global scratch slot accumulates them in local memory
             const bool in_smem = (uint32_t)N <= a.smem_cells;
             const int io = (in_smem && S == 13)
-                               ? sample_columns_reg<13>(p, T.perm, T.gp, zt, rho, ox, oy, oz, ncomp)
+                               ? sample_columns_reg<13>(p, T.perm, T.gp, zt, rho, ox, oy, oz, ncomp, masks)
                            : in_smem ? sample_columns_fast<false>(p, T.perm, T.gp, zt, rho, N, ox, oy, oz, ncomp)
                                      : sample_columns_fast<true>(p, T.perm, T.gp, zt, rho, N, ox, oy, oz, ncomp, masks);
             inside = io & 1;
@@ -456,14 +461,16 @@ __device__ void chunk_front(const DevParams& p, const BuildArgs& a, SmemTables& 
         const bool keep = R <= 16;
         unsigned long long kept0 = 0ull, kept1 = 0ull;
         unsigned long long mine = 0ull;
+        unsigned actbits = 0;  // (keep) bit i: cell c0 + i is active
+        const int x0 = c0 / (N * N), y0 = (c0 / N) % N, z0 = c0 % N;
         {
-            int x = c0 / (N * N), y = (c0 / N) % N, z = c0 % N;
+            int x = x0, y = y0, z = z0;
             const float iso = p.iso_level;
             const int SS = S * S;
             // the z+1 face of a cell is the z face of the next cell in the
             // run: carry its 4 inside bits (corners 3,2,7,6 -> 0,1,4,5)
             int lo = -1;
-            unsigned long long m00 = 0, m10 = 0, m01 = 0, m11 = 0;
+            unsigned long long m00 = 0, m10 = 0, m01 = 0, m11 = 0, quiet = 0, allin = 0;
             int mcol = -1;
             for (int c = c0; c < c1; ++c) {
                 int cs;
@@ -473,6 +480,16 @@ __device__ void chunk_front(const DevParams& p, const BuildArgs& a, SmemTables& 
                     if (col != mcol) {
                         m00 = masks[col]; m10 = masks[col + S]; m01 = masks[col + 1]; m11 = masks[col + S + 1];
                         mcol = col;
+                        // bit z: cell z has all eight corners below (allin) or
+                        // all above-or-at the iso level -- case 255 or 0
+                        const unsigned long long an = m00 & m10 & m01 & m11, no = ~(m00 | m10 | m01 | m11);
+                        allin = an & (an >> 1);
+                        quiet = allin | (no & (no >> 1));
+                    }
+                    if ((quiet >> z) & 1ull) {
+                        cases[c] = ((allin >> z) & 1ull) ? 255 : 0;
+                        if (++z == N) { z = 0; if (++y == N) { y = 0; ++x; } }
+                        continue;
                     }
                     cs = mask_case(m00, m10, m01, m11, z);
                 } else {
@@ -495,6 +512,7 @@ __device__ void chunk_front(const DevParams& p, const BuildArgs& a, SmemTables& 
                         const int i = c - c0;
                         const unsigned long long v = (unsigned long long)(nt | (nv << 3)) << (8 * (i & 7));
                         if (i < 8) kept0 |= v; else kept1 |= v;
+                        actbits |= 1u << i;
                     }
                 }
                 if (++z == N) { z = 0; if (++y == N) { y = 0; ++x; } }
@@ -504,55 +522,52 @@ __device__ void chunk_front(const DevParams& p, const BuildArgs& a, SmemTables& 
         // publish the aggregate as soon as the counts are known
         if (QUEUE && tid == 0) lookback_publish(a, ticket, pack_counts(total));
         const bool direct = direct_triangles(W, N, total);
-        {
-            // second pass over the same runs: each active cell's first vertex
-            // id (only active cells need one: every owner cell of a crossed
-            // edge is active) and where its triangles go -- the triangle map
-            // (direct), else the active-cell list with first index positions
-            int x = c0 / (N * N), y = (c0 / N) % N, z = c0 % N;
+        // second pass over the same runs: each active cell's first vertex id
+        // (only active cells need one: every owner cell of a crossed edge is
+        // active) and where its triangles go -- the triangle map (direct),
+        // else the active-cell list with first index positions
+        auto place = [&](int c, int x, int y, int z, int nt, unsigned nv) {
+            W.set_vbase(c, (uint32_t)(run & kField22));
+            const uint32_t ir = (uint32_t)((run >> kIndShift) & kField22);
+            if (direct) {
+                uint16_t* tmap = reinterpret_cast<uint16_t*>(W.ibase) + ir / 3u;
+                const unsigned xyz = (unsigned)x | ((unsigned)y << 4) | ((unsigned)z << 8);
+                for (int k = 0; k < nt; ++k) tmap[k] = (uint16_t)(xyz | ((unsigned)k << 12));
+            } else {
+                const uint32_t ar = (uint32_t)(run >> kActShift);
+                W.set_active(ar, c);
+                W.set_ibase(ar, ir);
+            }
+            run += (unsigned long long)nv | ((unsigned long long)(3 * nt) << kIndShift) | (1ull << kActShift);
+        };
+        if (keep) {
+            // the active cells of the run, in order, from the kept counts
+            for (unsigned bits = actbits; bits; bits &= bits - 1) {
+                const int i = __ffs(bits) - 1;
+                int x = x0, y = y0, z = z0 + i;
+                while (z >= N) { z -= N; if (++y == N) { y = 0; ++x; } }
+                const unsigned v = (unsigned)(((i < 8 ? kept0 : kept1) >> (8 * (i & 7))) & 0xffu);
+                place(c0 + i, x, y, z, (int)(v & 7u), v >> 3);
+            }
+        } else {
+            int x = x0, y = y0, z = z0;
             unsigned long long m00 = 0, m10 = 0, m01 = 0, m11 = 0;
             int mcol = -1;
             for (int c = c0; c < c1; ++c) {
-                int nt;
-                unsigned nv;
-                if (keep) {
-                    const int i = c - c0;
-                    const unsigned v = (unsigned)(((i < 8 ? kept0 : kept1) >> (8 * (i & 7))) & 0xffu);
-                    nt = (int)(v & 7u);
-                    nv = v >> 3;
+                int cs;
+                if (masks) {
+                    // the case again from the masks (no read of the global cases)
+                    const int col = x * S + y;
+                    if (col != mcol) {
+                        m00 = masks[col]; m10 = masks[col + S]; m01 = masks[col + 1]; m11 = masks[col + S + 1];
+                        mcol = col;
+                    }
+                    cs = mask_case(m00, m10, m01, m11, z);
                 } else {
-                    int cs;
-                    if (masks) {
-                        // the case again from the masks (no read of the global cases)
-                        const int col = x * S + y;
-                        if (col != mcol) {
-                            m00 = masks[col]; m10 = masks[col + S]; m01 = masks[col + 1]; m11 = masks[col + S + 1];
-                            mcol = col;
-                        }
-                        cs = mask_case(m00, m10, m01, m11, z);
-                    } else {
-                        cs = cases[c];
-                    }
-                    nt = T.ntri[cs];
-                    nv = nt ? __popc(T.edges[cs] & T.owned[oriented][boundary_flags(x, y, z, N)]) : 0u;
+                    cs = cases[c];
                 }
-                if (nt) {
-                    W.set_vbase(c, (uint32_t)(run & kField22));
-                    const uint32_t ir = (uint32_t)((run >> kIndShift) & kField22);
-                    // the active-cell list (the split build's vertex work searches
-                    // it), and the triangle map or each active cell's first
-                    // index position
-                    const uint32_t ar = (uint32_t)(run >> kActShift);
-                    W.set_active(ar, c);
-                    if (direct) {
-                        uint16_t* tmap = reinterpret_cast<uint16_t*>(W.ibase) + ir / 3u;
-                        const unsigned xyz = (unsigned)x | ((unsigned)y << 4) | ((unsigned)z << 8);
-                        for (int k = 0; k < nt; ++k) tmap[k] = (uint16_t)(xyz | ((unsigned)k << 12));
-                    } else {
-                        W.set_ibase(ar, ir);
-                    }
-                    run += (unsigned long long)nv | ((unsigned long long)(3 * nt) << kIndShift) | (1ull << kActShift);
-                }
+                const int nt = T.ntri[cs];
+                if (nt) place(c, x, y, z, nt, __popc(T.edges[cs] & T.owned[oriented][boundary_flags(x, y, z, N)]));
                 if (++z == N) { z = 0; if (++y == N) { y = 0; ++x; } }
             }
         }

@@ -124,6 +124,7 @@ struct BuildArgs {
     uint32_t* split_queue;           // planned: kPlanRanks work queues of n entries
     uint32_t* split_ctr;             // kCtrWords counters, zero at launch (kCtr*)
     uint32_t split_planned;          // the planning kernel runs first and fills the queues
+    uint32_t mask_offset;            // nonzero: per-column below-iso masks at dyn smem + mask_offset
     // Optional streamed host output (batched form): device addresses of
     // page-locked host memory.  Pass 2 then runs inside the build kernel, and
     // each chunk's record, indices, vertices and normals go there as soon as

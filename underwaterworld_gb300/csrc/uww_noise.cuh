@@ -303,7 +303,8 @@ __device__ __forceinline__ void ztable_warps(const DevParams& p, const ZTable Z,
 template <int S>
 __device__ __forceinline__ int sample_columns_reg(const DevParams& p, const uint8_t* __restrict__ P,
                                                   const float4* __restrict__ gp, const ZTable Z,
-                                                  float* __restrict__ rho, int ox, int oy, int oz, int ncomp)
+                                                  float* __restrict__ rho, int ox, int oy, int oz, int ncomp,
+                                                  unsigned long long* masks = nullptr)
 {
     constexpr int SS = S * S;
     const int K = p.octaves;
@@ -349,12 +350,15 @@ __device__ __forceinline__ int sample_columns_reg(const DevParams& p, const uint
             }
         }
         float* out = rho + col * S;
+        unsigned below = 0;
 #pragma unroll
         for (int z = 0; z < S; ++z) {
             out[z] = acc[z];
             inside |= !(acc[z] > iso);
             outside |= !(acc[z] < iso);
+            below |= (unsigned)(acc[z] < iso) << z;
         }
+        if (masks) masks[col] = below;
     }
     return inside | (outside << 1);
 }
