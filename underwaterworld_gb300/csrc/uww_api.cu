@@ -150,7 +150,7 @@ struct LaunchCfg {
 };
 
 // split_ok: nothing of the launch needs the pipelined kernel (streamed host
-// output does)
+// output and per-vertex edge ids do)
 int plan_launch(uww_ctx* ctx, uint32_t n, uint32_t max_cells, bool queue, LaunchCfg* cfg, bool split_ok = true)
 {
     const size_t cap = ctx->smem_dyn_max;
@@ -233,7 +233,7 @@ int launch(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint32_t ma
            const HostOut* host = nullptr)
 {
     LaunchCfg cfg;
-    int st = plan_launch(ctx, n, max_cells, queue, &cfg, host == nullptr);
+    int st = plan_launch(ctx, n, max_cells, queue, &cfg, host == nullptr && edge_ids == nullptr);
     if (st) return st;
     // the work buffers a captured frame graph refers to: a reallocation
     // moves the context's generation on, and such a frame recaptures itself
@@ -315,17 +315,17 @@ int launch(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint32_t ma
             a.plan = ctx->d_plan;
         }
         if (cfg.split) {
-            // The counters, the tile sums, per chunk its counts word, the
-            // mesh list and the work queues -- laid out for the chunk count
-            // the buffer was sized for, so that they stay in place from one
-            // launch to the next -- then per chunk a workspace slot.  The
+            // The counters, the tile sums, per chunk its counts word and its
+            // staging place, and the work queues -- laid out for the chunk
+            // count the buffer was sized for, so that they stay in place from
+            // one launch to the next -- then per chunk a workspace slot.  The
             // counters and tile sums are zero at launch: cleared here on
             // (re)allocation and left zero by every launch's emission kernel.
             const size_t slot = align16(chunk_layout((int)max_cells).total);
             auto fixed_bytes = [](uint32_t m) {
                 const size_t ntiles = ((size_t)m + kTileChunks - 1) / kTileChunks;
-                return kCtrWords * 4 + ((ntiles * 8 + 15) & ~size_t(15)) + (((size_t)m * 8 + 15) & ~size_t(15)) +
-                       (((size_t)m * 4 + 15) & ~size_t(15)) + (((size_t)m * 4 * kPlanRanks + 15) & ~size_t(15));
+                return kCtrWords * 4 + ((ntiles * 8 + 15) & ~size_t(15)) + 2 * (((size_t)m * 8 + 15) & ~size_t(15)) +
+                       (((size_t)m * 4 * kPlanRanks + 15) & ~size_t(15));
             };
             const uint32_t m = std::max(n, ctx->split_n);
             if (!ctx->d_split || ctx->split_n < n || ctx->split_cap < fixed_bytes(m) + (size_t)n * slot) {
@@ -341,17 +341,39 @@ int launch(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint32_t ma
             const size_t ntiles = ((size_t)nc + kTileChunks - 1) / kTileChunks;
             uint8_t* b = ctx->d_split;
             a.split_ctr = reinterpret_cast<uint32_t*>(b);
+            a.stage_ctr = reinterpret_cast<unsigned long long*>(b + kCtrStage * 4);
             b += kCtrWords * 4;
             a.tile_sum = reinterpret_cast<unsigned long long*>(b);
             b += (ntiles * 8 + 15) & ~size_t(15);
             a.tinfo = reinterpret_cast<unsigned long long*>(b);
             b += ((size_t)nc * 8 + 15) & ~size_t(15);
-            a.mesh_list = reinterpret_cast<uint32_t*>(b);
-            b += ((size_t)nc * 4 + 15) & ~size_t(15);
+            a.stage_at = reinterpret_cast<unsigned long long*>(b);
+            b += ((size_t)nc * 8 + 15) & ~size_t(15);
             a.split_queue = reinterpret_cast<uint32_t*>(b);
             b += ((size_t)nc * 4 * kPlanRanks + 15) & ~size_t(15);
             a.slots = b;
             a.slot_bytes = slot;
+            // staging as large as the outputs (a batch whose output fits its
+            // capacities is always staged whole), and the emission units:
+            // at most one vertex block per kVertexBlock vertices plus one per
+            // chunk, one index block per kIndexBlock indices plus one per
+            // chunk, one whole chunk per chunk
+            const size_t vc = out->vert_capacity, ic = out->ind_capacity;
+            const size_t units = vc / kVertexBlock + ic / kIndexBlock + 3 * (size_t)nc;
+            const size_t sbytes = vc * 16 + ((ic * 4 + 15) & ~size_t(15)) + units * 8;
+            if (!ctx->d_stage || ctx->stage_cap < sbytes) {
+                st = grow(&ctx->d_stage, &ctx->stage_cap, sbytes);
+                if (st) return st;
+            }
+            uint8_t* sb = ctx->d_stage;
+            a.stage_pos = reinterpret_cast<float4*>(sb);
+            sb += vc * 16;
+            a.stage_inds = reinterpret_cast<uint32_t*>(sb);
+            sb += (ic * 4 + 15) & ~size_t(15);
+            a.units = reinterpret_cast<unsigned long long*>(sb);
+            a.unit_cap = (uint32_t)std::min<size_t>(units, 0xffffffffu);
+            a.stage_vcap = out->vert_capacity;
+            a.stage_icap = out->ind_capacity;
             a.split_planned = a.plan != nullptr;
             a.plan = nullptr;  // the split build plans into its own queues
         }
@@ -537,6 +559,7 @@ int uww_ctx_destroy(uww_ctx* ctx)
     cudaFree(ctx->d_lookback);
     cudaFree(ctx->d_plan);
     cudaFree(ctx->d_split);
+    cudaFree(ctx->d_stage);
     cudaFree(ctx->d_state);
     cudaFree(ctx->d_totals);
     cudaFree(ctx->d_scratch);

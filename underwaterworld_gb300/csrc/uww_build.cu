@@ -62,6 +62,14 @@ constexpr unsigned long long kField22 = (1ull << 22) - 1;
 // split build: a chunk's counts word (tinfo) is the packed counts and, in
 // bit 62, the early-blank flag
 constexpr unsigned long long kInfoEarlyBlank = 1ull << 62;
+// a meshed chunk the staging buffers had no room for
+constexpr unsigned long long kUnstaged = ~0ull;
+// emission units: kind in bits 60-63, part in 32-59, chunk in 0-31
+constexpr uint32_t kUnitVerts = 0, kUnitInds = 1, kUnitChunk = 2;
+__device__ __forceinline__ unsigned long long unit_entry(uint32_t c, uint32_t part, uint32_t kind)
+{
+    return (unsigned long long)c | ((unsigned long long)part << 32) | ((unsigned long long)kind << 60);
+}
 __device__ __forceinline__ uint32_t rec_off32(unsigned long long v) { return (uint32_t)(v > 0xffffffffull ? 0xffffffffull : v); }
 
 
@@ -684,6 +692,7 @@ struct EmitOut {
     uww_vert_color* verts;
     uint32_t* inds;
     uint32_t* edge_ids;
+    float4* pos;  // when set: position and corner b per vertex instead of verts (staged pass 1)
 };
 
 // Pass 1 for triangle t of a chunk's index stream: its cell from the
@@ -745,12 +754,16 @@ __device__ __forceinline__ void emit_triangle(const DevParams& p, const EmitOut&
             if (positions && ((fr >> i) & 1u)) {
                 const EdgeVertex ev = edge_vertex<O>(p, T, rho, S, x, y, z, e, s, ox, oy, oz);
                 if (a.edge_ids) a.edge_ids[voff + id] = ev.edge_id;
-                float2* v2 = reinterpret_cast<float2*>(a.verts + voff + id);
-                v2[0] = make_float2(ev.x, ev.y);
-                // colour slot 0 carries the owner's corner b (the value ramp's
-                // input, chunk.rs:215) to pass 2, which overwrites it
-                v2[1] = make_float2(ev.z, carry_corner ? (float)ev.cb : 0.f);
-                v2[2] = make_float2(0.f, 0.f);
+                if (a.pos) {
+                    a.pos[voff + id] = make_float4(ev.x, ev.y, ev.z, (float)ev.cb);
+                } else {
+                    float2* v2 = reinterpret_cast<float2*>(a.verts + voff + id);
+                    v2[0] = make_float2(ev.x, ev.y);
+                    // colour slot 0 carries the owner's corner b (the value
+                    // ramp's input, chunk.rs:215) to pass 2, which overwrites it
+                    v2[1] = make_float2(ev.z, carry_corner ? (float)ev.cb : 0.f);
+                    v2[2] = make_float2(0.f, 0.f);
+                }
             }
         } else {
             // the owner: the first cell in stream order holding this edge
@@ -1137,23 +1150,28 @@ __global__ void __launch_bounds__(kPlanThreads) plan_kernel(const DevParams p, c
 
 // ---------------------------------------------------------------------------
 // Split build, for batches whose chunks all work in shared memory: the front
-// half and the emission run as separate kernels instead of one pipelined one.
+// half with the chunk-local pass 1, the records, and the rest of the
+// emission, as separate kernels instead of one pipelined one.
 //   split_plan_kernel (planned batches): one pass, one thread per chunk -- a
 //     chunk the depth bias decides gets its counts word (zero, early-blank
 //     flag) at once; the others go to one of kPlanRanks work queues by cost
 //     rank (bias_decides_with), the likely costliest first.
 //   front_kernel: persistent, every thread a compute thread, one chunk per CTA
 //     at a time from the queues -- noise, votes, classification and block scan
-//     (chunk_front); a meshed chunk's workspace goes to its slot, its counts
-//     to tinfo and to its tile's sum, the chunk to the mesh list.  No
-//     look-back, no control warp, no hand-offs, no ordering between CTAs.
-//   emit_kernel, the front kernel's programmatic dependent (its CTAs load
-//     their tables as front CTAs finish): per CTA a meshed chunk, its slot
-//     copied to shared memory asynchronously (cp.async) while the CTA writes
-//     the records of a tile of chunks and sums its chunk's prefix from the
-//     tile sums; then one thread per triangle as in the pipelined back half,
-//     then the chunk's vertices' colours and normals (pass 2).  The last CTA
-//     writes the totals and leaves the counters zero.
+//     (chunk_front), then for a meshed chunk pass 1 from shared memory:
+//     chunk-local indices and vertex positions into staging buffers (room
+//     taken with one atomic per chunk), and the chunk's emission work as
+//     units: blocks of its vertices, blocks of its indices.  Its counts go
+//     to tinfo and to its tile's sum.  No look-back, no control warp, no
+//     hand-offs, no ordering between CTAs.
+//   records_kernel: one CTA per tile of chunks, the records and totals.
+//   emit_kernel: the units, taken from a counter -- a vertex block's colours
+//     and normals from its staged positions to the vertex's place, an index
+//     block copied to its place.  A chunk the staging buffers had no room
+//     for (the batch's output then exceeds the capacities) left its
+//     workspace in its slot and is emitted from there by one CTA.
+// The records and emission kernels are each the programmatic dependent of
+// the kernel before them.
 // The same device functions as the pipelined build: the same bits.  The work
 // order (queues, mesh list) varies from run to run; the outputs do not.
 
@@ -1255,20 +1273,21 @@ __global__ void __launch_bounds__(MAXT, MINB) front_kernel(const DevParams p, co
 {
     extern __shared__ __align__(16) uint8_t dyn_smem[];
     __shared__ SmemTables T;
-    __shared__ uint32_t rank;
+    __shared__ uint32_t rank, unit_a, unit_b;
+    __shared__ unsigned long long stage;
     const int tid = threadIdx.x, nthr = blockDim.x;
     load_tables(p, T, tid, nthr);
     // the planning kernel's queues (this kernel is its programmatic dependent)
     if (a.split_planned) asm volatile("griddepcontrol.wait;" ::: "memory");
-    // the emission kernel, launched after this one as its programmatic
-    // dependent, may take SMs as this kernel's CTAs finish (it loads its
-    // tables, then waits for the whole front kernel before reading any of it)
+    // the records kernel, launched after this one as its programmatic
+    // dependent (and the emission kernel after it), may take SMs as this
+    // kernel's CTAs finish; each waits for the kernel before it
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     if (tid == 0) {
         T.errflags = 0;
         T.nchunks = a.n_dev ? min(*a.n_dev, a.n) : a.n;
         rank = 0;
-        // the emission kernel adds the chunks that do not fit
+        // the records kernel adds the chunks that do not fit
         if (blockIdx.x == 0) a.totals[2] = 0ull;
     }
     __syncthreads();
@@ -1285,78 +1304,72 @@ __global__ void __launch_bounds__(MAXT, MINB) front_kernel(const DevParams p, co
         __syncthreads();
         const ChunkInfo ci = T.ci[0];
         const uint32_t nV = (uint32_t)(ci.total & kField22), nI = (uint32_t)((ci.total >> kIndShift) & kField22);
+        // the chunk's emission work: blocks of kVertexBlock vertices (colour,
+        // normal; list A) and of kIndexBlock indices (list B) when its pass 1
+        // is staged, else the whole chunk from its slot (list A)
+        const uint32_t vb = (nV + kVertexBlock - 1) / kVertexBlock, ib = (nI + kIndexBlock - 1) / kIndexBlock;
         if (tid == 0) {
             a.tinfo[c] = ci.total | ((ci.flags & UWW_CHUNK_EARLY_BLANK) ? kInfoEarlyBlank : 0ull);
             if (nV | nI) atomicAdd(&a.tile_sum[c / kTileChunks], (unsigned long long)nV | ((unsigned long long)nI << 32));
             if (nI) {
-                const uint32_t m = atomicAdd(&a.split_ctr[kCtrMeshed], 1u);
-                if (m < a.n) a.mesh_list[m] = c;
+                // room in the staging buffers (first come, first served; they
+                // hold the batch whenever its output fits its capacities)
+                const unsigned long long at =
+                    atomicAdd(a.stage_ctr, (unsigned long long)nV | ((unsigned long long)nI << 32));
+                const unsigned long long sv = at & 0xffffffffull, si = at >> 32;
+                const bool room = sv + nV <= a.stage_vcap && si + nI <= a.stage_icap;
+                stage = room ? at : kUnstaged;
+                a.stage_at[c] = stage;
+                unit_a = atomicAdd(&a.split_ctr[kCtrUnitsA], room ? vb : 1u);
+                unit_b = room ? atomicAdd(&a.split_ctr[kCtrUnitsB], ib) : 0u;
             }
         }
+        __syncthreads();
         if (nI) {
-            // the workspace (samples, cases, vertex bases, triangle map or
-            // active list) to the chunk's slot, in 16-byte words
-            const uint32_t words = chunk_layout(ci.N).total / 16u;
-            const uint4* src = reinterpret_cast<const uint4*>(dyn_smem);
-            uint4* dst = reinterpret_cast<uint4*>(a.slots + (size_t)c * a.slot_bytes);
-            for (uint32_t i = tid; i < words; i += nthr) dst[i] = src[i];
+            const unsigned long long st = stage;
+            if (st != kUnstaged) {
+                // pass 1 from the shared workspace: chunk-local indices and
+                // vertex positions (with the owner's corner b) into staging
+                const int N = ci.N;
+                const Workspace W = workspace(a, dyn_smem, 0, N);
+                const uint32_t sv = (uint32_t)st, si = (uint32_t)(st >> 32);
+                const uint32_t nT = nI / 3u, nA = (uint32_t)(ci.total >> kActShift);
+                const bool direct = direct_triangles(W, N, ci.total);
+                const float s = __fdiv_rn((float)p.chunk_size, (float)N);
+                const EmitOut eo{nullptr, a.stage_inds, nullptr, a.stage_pos};
+                for (uint32_t t = tid; t < nT; t += nthr)
+                    emit_triangle<O>(p, eo, T, W, N, nA, direct, t, sv, si, ci.ox, ci.oy, ci.oz, s, true);
+                for (uint32_t k = tid; k < vb; k += nthr)
+                    if (unit_a + k < a.unit_cap) a.units[unit_a + k] = unit_entry(c, k, kUnitVerts);
+                for (uint32_t k = tid; k < ib; k += nthr)
+                    if (unit_b + k < a.unit_cap) a.units[a.unit_cap - 1 - (unit_b + k)] = unit_entry(c, k, kUnitInds);
+            } else {
+                // no room: the workspace to the chunk's slot, in 16-byte
+                // words, for the emission kernel to emit the chunk from
+                const uint32_t words = chunk_layout(ci.N).total / 16u;
+                const uint4* src = reinterpret_cast<const uint4*>(dyn_smem);
+                uint4* dst = reinterpret_cast<uint4*>(a.slots + (size_t)c * a.slot_bytes);
+                for (uint32_t i = tid; i < words; i += nthr) dst[i] = src[i];
+                if (tid == 0 && unit_a < a.unit_cap) a.units[unit_a] = unit_entry(c, 0, kUnitChunk);
+            }
         }
         __syncthreads();  // the workspace and the staged ticket are reused
     }
     if (tid == 0 && T.errflags) atomicOr(&a.acc[1], (unsigned long long)T.errflags);
 }
 
-// Sum over the CTA of the counts of the chunks before chunk c: the tile sums
-// of the tiles before its tile, then the chunks of its tile before it.  Every
-// thread calls it; returns verts | inds << 32 (each saturated to 32 bits).
-__device__ __forceinline__ unsigned long long chunk_prefix(const BuildArgs& a, uint32_t c, SmemTables& T)
+// The split build's records: one CTA per tile of kTileChunks chunks, the
+// prefix of the tiles before it from the tile sums, then a scan over the
+// tile; CTA 0 writes the totals.  A programmatic dependent of the front
+// kernel, and the emission kernel one of this.
+__global__ void __launch_bounds__(kTileChunks) records_kernel(const BuildArgs a)
 {
-    const int tid = threadIdx.x, nthr = blockDim.x;
-    const uint32_t tile = c / kTileChunks, t0 = tile * kTileChunks;
-    unsigned long long v = 0ull, i = 0ull;
-    for (uint32_t k = tid; k < tile; k += nthr) {
-        const unsigned long long w = __ldcg(&a.tile_sum[k]);
-        v += w & 0xffffffffull;
-        i += w >> 32;
-    }
-    for (uint32_t j = t0 + tid; j < c; j += nthr) {
-        const unsigned long long w = __ldcg(&a.tinfo[j]);
-        v += w & kField22;
-        i += (w >> kIndShift) & kField22;
-    }
-    unsigned long long tv = 0ull, ti = 0ull;
-    block_scan2(v, i, &tv, &ti, T);
-    return rec_off32(tv) | ((unsigned long long)rec_off32(ti) << 32);
-}
-
-template <class O>
-__global__ void __launch_bounds__(256, 4) emit_kernel(const DevParams p, const BuildArgs a)
-{
-    extern __shared__ __align__(16) uint8_t dyn_smem[];
     __shared__ SmemTables T;
-    __shared__ int last;
-    const int tid = threadIdx.x, nthr = blockDim.x;
-    load_tables(p, T, tid, nthr);
-    // launched as a programmatic dependent of the front kernel: everything it
-    // wrote is read after this, and through L2 (no L1 line of it can be stale)
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     asm volatile("griddepcontrol.wait;" ::: "memory");
+    const int tid = threadIdx.x, nthr = blockDim.x;
     const uint32_t nchunks = a.n_dev ? min(*a.n_dev, a.n) : a.n;
-    const uint32_t nmesh = min(__ldcg(&a.split_ctr[kCtrMeshed]), a.n);
     const uint32_t ntiles = (nchunks + kTileChunks - 1) / kTileChunks;
-    // this CTA's first meshed chunk: its slot on its way to shared memory
-    // while the records are written and its prefix is summed
-    uint32_t c = blockIdx.x < nmesh ? __ldcg(&a.mesh_list[blockIdx.x]) : kNoChunk;
-    auto copy_slot = [&](uint32_t ch) {
-        const uint32_t words = chunk_layout((int)a.chunks[ch].cells).total / 16u;
-        const uint8_t* src = a.slots + (size_t)ch * a.slot_bytes;
-        for (uint32_t k = tid; k < words; k += nthr) {
-            const uint32_t dst = (uint32_t)__cvta_generic_to_shared(dyn_smem + 16u * k);
-            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src + 16u * k) : "memory");
-        }
-        asm volatile("cp.async.commit_group;" ::: "memory");
-    };
-    if (c != kNoChunk) copy_slot(c);
-    // the records, a tile of kTileChunks chunks per CTA (one per thread)
     unsigned long long over = 0;
     for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const uint32_t j = tile * kTileChunks + tid;
@@ -1391,42 +1404,128 @@ __global__ void __launch_bounds__(256, 4) emit_kernel(const DevParams p, const B
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) over += __shfl_xor_sync(0xffffffffu, over, o);
     if ((tid & 31) == 0 && over) atomicAdd(&a.totals[2], over);
-    // the meshed chunks, one per CTA at a time: pass 1 (one thread per
-    // triangle), then pass 2 over the chunk's vertices (colour and normal)
-    const bool want_color = (p.outputs & UWW_OUT_COLOR) != 0;
-    const bool want_normals = (p.outputs & UWW_OUT_NORMALS) != 0 && a.normals != nullptr;
-    for (uint32_t m = blockIdx.x; m < nmesh; m += gridDim.x) {
-        if (m != blockIdx.x) {
-            c = __ldcg(&a.mesh_list[m]);
-            __syncthreads();  // the previous chunk is done with the workspace
-            copy_slot(c);
+    if (blockIdx.x == 0) {
+        unsigned long long v = 0ull, i = 0ull, tv = 0ull, ti = 0ull;
+        for (uint32_t k = tid; k < ntiles; k += nthr) {
+            const unsigned long long s = __ldcg(&a.tile_sum[k]);
+            v += s & 0xffffffffull;
+            i += s >> 32;
         }
-        const unsigned long long pre = chunk_prefix(a, c, T);
-        const unsigned long long w = __ldcg(&a.tinfo[c]);
-        const uww_chunk_desc d = a.chunks[c];
-        asm volatile("cp.async.wait_all;" ::: "memory");
-        __syncthreads();
-        const uint32_t nV = (uint32_t)(w & kField22), nI = (uint32_t)((w >> kIndShift) & kField22);
-        const uint32_t voff = (uint32_t)pre, ioff = (uint32_t)(pre >> 32);
-        if ((unsigned long long)voff + nV > a.vert_capacity || (unsigned long long)ioff + nI > a.ind_capacity) continue;
-        const int N = (int)d.cells;
-        const Workspace W = workspace_at(dyn_smem, N);
-        const uint32_t nT = nI / 3u, nA = (uint32_t)((w >> kActShift) & 0x3ffffull);
-        const bool direct = direct_triangles(W, N, w & (kInfoEarlyBlank - 1));
-        const float s = __fdiv_rn((float)p.chunk_size, (float)N);
-        const EmitOut eo{a.verts, a.inds, a.edge_ids};
-        for (uint32_t tr = tid; tr < nT; tr += nthr)
-            emit_triangle<O>(p, eo, T, W, N, nA, direct, tr, voff, ioff, d.pos[0] * p.chunk_size,
-                             d.pos[1] * p.chunk_size, d.pos[2] * p.chunk_size, s, want_color || want_normals);
-        if (want_color || want_normals) {
-            __syncthreads();  // the chunk's vertex positions, written by this CTA
-            for (uint32_t v = tid; v < nV; v += nthr)
-                finish_vertex<O>(p, T.perm, T.gp, a.verts, a.normals, voff + v, want_color, want_normals);
+        block_scan2(v, i, &tv, &ti, T);
+        if (tid == 0) {
+            a.totals[0] = tv;
+            a.totals[1] = ti;
+            a.totals[3] = atomicExch(&a.acc[1], 0ull);
         }
     }
-    asm volatile("cp.async.wait_all;" ::: "memory");
-    // the last CTA: the totals, and the tile sums and counters left zero for
-    // the next launch
+}
+
+// a chunk's record, through L2 (written by the records kernel)
+__device__ __forceinline__ uww_chunk_record load_record(const uww_chunk_record* r)
+{
+    uww_chunk_record rec;
+    const uint4* r4 = reinterpret_cast<const uint4*>(r);
+    *reinterpret_cast<uint4*>(&rec) = __ldcg(r4);
+    *(reinterpret_cast<uint4*>(&rec) + 1) = __ldcg(r4 + 1);
+    return rec;
+}
+
+template <class O>
+__global__ void __launch_bounds__(256, 4) emit_kernel(const DevParams p, const BuildArgs a)
+{
+    extern __shared__ __align__(16) uint8_t dyn_smem[];  // one workspace (chunks emitted from their slot)
+    __shared__ SmemTables T;
+    __shared__ int last;
+    __shared__ uint32_t next_ticket;
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    load_tables(p, T, tid, nthr);
+    // launched as a programmatic dependent of the records kernel (itself one
+    // of the front kernel): what they wrote is read after this, through L2
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    const uint32_t nchunks = a.n_dev ? min(*a.n_dev, a.n) : a.n;
+    const uint32_t ntiles = (nchunks + kTileChunks - 1) / kTileChunks;
+    const uint32_t na = min(__ldcg(&a.split_ctr[kCtrUnitsA]), a.unit_cap);
+    const uint32_t nb = min(__ldcg(&a.split_ctr[kCtrUnitsB]), a.unit_cap - na);
+    const uint32_t nunits = na + nb;
+    const bool want_color = (p.outputs & UWW_OUT_COLOR) != 0;
+    const bool want_normals = (p.outputs & UWW_OUT_NORMALS) != 0 && a.normals != nullptr;
+    // ticket t: list A (vertex blocks, whole chunks) first, then list B
+    // (index blocks); tickets below gridDim.x are static, the rest counted
+    uint32_t t = blockIdx.x;
+    while (t < nunits) {
+        const unsigned long long ent = t < na ? __ldcg(&a.units[t]) : __ldcg(&a.units[a.unit_cap - 1 - (t - na)]);
+        const uint32_t c = (uint32_t)ent, part = (uint32_t)(ent >> 32) & 0x0fffffffu, kind = (uint32_t)(ent >> 60);
+        const uww_chunk_record rec = load_record(&a.records[c]);
+        __syncthreads();  // every thread has read the previous next_ticket
+        if (tid == 0) next_ticket = gridDim.x + atomicAdd(&a.split_ctr[kCtrUnitsTaken], 1u);
+        if (!(rec.flags & UWW_CHUNK_OVERFLOW)) {
+            if (kind == kUnitVerts) {
+                // colour and normal of a block of the chunk's vertices, from
+                // their staged positions
+                const uint32_t v = part * kVertexBlock + tid;
+                if (tid < (int)kVertexBlock && v < rec.num_verts) {
+                    const uint32_t sv = (uint32_t)__ldcg(&a.stage_at[c]);
+                    const float4 q = __ldcg(a.stage_pos + sv + v);
+                    float2 out[3];
+                    float g[3];
+                    vertex_values<O>(p, T.perm, T.gp, make_float2(q.x, q.y), make_float2(q.z, q.w), want_color,
+                                     want_normals, out, g);
+                    float2* v2 = reinterpret_cast<float2*>(a.verts + rec.vert_offset + v);
+                    v2[0] = out[0];
+                    v2[1] = out[1];
+                    v2[2] = out[2];
+                    if (want_normals) {
+                        float* nn = a.normals + 3 * (size_t)(rec.vert_offset + v);
+                        nn[0] = g[0]; nn[1] = g[1]; nn[2] = g[2];
+                    }
+                }
+            } else if (kind == kUnitInds) {
+                // a block of the chunk's indices to their place
+                const uint32_t si = (uint32_t)(__ldcg(&a.stage_at[c]) >> 32);
+                const uint32_t k0 = part * kIndexBlock, k1 = min(k0 + kIndexBlock, rec.num_inds);
+                const uint32_t* src = a.stage_inds + si;
+                uint32_t* dst = a.inds + rec.ind_offset;
+                uint32_t w[kIndexBlock / 256];
+#pragma unroll
+                for (int r = 0; r < (int)(kIndexBlock / 256); ++r) {
+                    const uint32_t k = k0 + (uint32_t)r * 256u + tid;
+                    w[r] = k < k1 ? __ldcg(src + k) : 0u;
+                }
+#pragma unroll
+                for (int r = 0; r < (int)(kIndexBlock / 256); ++r) {
+                    const uint32_t k = k0 + (uint32_t)r * 256u + tid;
+                    if (k < k1) dst[k] = w[r];
+                }
+            } else {
+                // a chunk without staging room: pass 1 and pass 2 from its slot
+                const uww_chunk_desc d = a.chunks[c];
+                const int N = (int)d.cells;
+                const uint32_t words = chunk_layout(N).total / 16u;
+                const uint4* src = reinterpret_cast<const uint4*>(a.slots + (size_t)c * a.slot_bytes);
+                uint4* dst = reinterpret_cast<uint4*>(dyn_smem);
+                for (uint32_t i = tid; i < words; i += nthr) dst[i] = __ldcg(src + i);
+                __syncthreads();
+                const Workspace W = workspace_at(dyn_smem, N);
+                const unsigned long long w = __ldcg(&a.tinfo[c]);
+                const bool direct = direct_triangles(W, N, w & (kInfoEarlyBlank - 1));
+                const float s = __fdiv_rn((float)p.chunk_size, (float)N);
+                const EmitOut eo{a.verts, a.inds, a.edge_ids, nullptr};
+                for (uint32_t tr = tid; tr < rec.num_inds / 3u; tr += nthr)
+                    emit_triangle<O>(p, eo, T, W, N, rec.num_active_cells, direct, tr, rec.vert_offset,
+                                     rec.ind_offset, d.pos[0] * p.chunk_size, d.pos[1] * p.chunk_size,
+                                     d.pos[2] * p.chunk_size, s, want_color || want_normals);
+                if (want_color || want_normals) {
+                    __syncthreads();  // the chunk's vertex positions, written by this CTA
+                    for (uint32_t v = tid; v < rec.num_verts; v += nthr)
+                        finish_vertex<O>(p, T.perm, T.gp, a.verts, a.normals, rec.vert_offset + v, want_color,
+                                         want_normals);
+                }
+            }
+        }
+        __syncthreads();  // next_ticket written; the workspace is free
+        t = next_ticket;
+    }
+    // the last CTA: the tile sums and counters left zero for the next launch
     __syncthreads();
     if (tid == 0) {
         __threadfence();
@@ -1435,19 +1534,7 @@ __global__ void __launch_bounds__(256, 4) emit_kernel(const DevParams p, const B
     __syncthreads();
     if (!last) return;
     __threadfence();
-    unsigned long long v = 0ull, i = 0ull, tv = 0ull, ti = 0ull;
-    for (uint32_t k = tid; k < ntiles; k += nthr) {
-        const unsigned long long s = __ldcg(&a.tile_sum[k]);
-        v += s & 0xffffffffull;
-        i += s >> 32;
-    }
-    block_scan2(v, i, &tv, &ti, T);
     for (uint32_t k = tid; k < ntiles; k += nthr) a.tile_sum[k] = 0ull;
-    if (tid == 0) {
-        a.totals[0] = tv;
-        a.totals[1] = ti;
-        a.totals[3] = atomicExch(&a.acc[1], 0ull);
-    }
     if (tid < kCtrWords) a.split_ctr[tid] = 0u;
 }
 
@@ -1609,8 +1696,20 @@ cudaError_t launch_build(const DevParams& p, const BuildArgs& a, bool queue, int
         cfg.attrs = attr;
         cfg.numAttrs = a.split_planned ? 1 : 0;
         if ((e = cudaLaunchKernelEx(&cfg, front_for(exact, threads), p, a)) != cudaSuccess) return e;
-        // the emission (with pass 2) as the front kernel's programmatic
-        // dependent: its CTAs load their tables as front CTAs finish
+        // the records, then the emission, each the programmatic dependent
+        // of the kernel before it: their CTAs start as the front kernel's
+        // CTAs finish
+        cudaLaunchAttribute pdl[1];
+        pdl[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        pdl[0].val.programmaticStreamSerializationAllowed = 1;
+        const uint32_t nt = std::max(1u, (a.n + kTileChunks - 1) / kTileChunks);
+        cudaLaunchConfig_t rcfg = {};
+        rcfg.gridDim = dim3(std::min(nt, 1024u));
+        rcfg.blockDim = dim3(kTileChunks);
+        rcfg.stream = s;
+        rcfg.attrs = pdl;
+        rcfg.numAttrs = 1;
+        if ((e = cudaLaunchKernelEx(&rcfg, records_kernel, a)) != cudaSuccess) return e;
         int dev = 0, sms = 0, ebps = 0;
         const FrontFn efn = emit_for(exact);
         e = cudaGetDevice(&dev);
@@ -1622,9 +1721,6 @@ cudaError_t launch_build(const DevParams& p, const BuildArgs& a, bool queue, int
         ecfg.blockDim = dim3(256);
         ecfg.dynamicSmemBytes = a.slot_bytes;
         ecfg.stream = s;
-        cudaLaunchAttribute pdl[1];
-        pdl[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-        pdl[0].val.programmaticStreamSerializationAllowed = 1;
         ecfg.attrs = pdl;
         ecfg.numAttrs = 1;
         return cudaLaunchKernelEx(&ecfg, efn, p, a);

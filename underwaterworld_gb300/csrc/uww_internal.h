@@ -59,15 +59,19 @@ constexpr uint32_t kPlanDone = 0, kPlanCount = 1, kPlanList = 2;
 __host__ __device__ inline size_t plan_kinds_offset(uint32_t n) { return ((size_t)n + kPlanList) * sizeof(uint32_t); }
 __host__ __device__ inline size_t plan_buffer_bytes(uint32_t n) { return plan_kinds_offset(n) + n; }
 
-// Split build (uww_build.cu): chunks per tile of the tile sums (the emission
-// kernel writes a tile's records with one thread per chunk), cost ranks of
-// the planning kernel's work queues, and the words of the counter block:
-// [kCtrQueued + r] chunks queued at rank r, [kCtrTaken + r] taken from queue
-// r, the meshed chunks, the emission CTAs finished.  All zero between
-// launches.
+// Split build (uww_build.cu): chunks per tile of the tile sums (the records
+// kernel scans a tile with one thread per chunk), vertices and indices per
+// emission unit, cost ranks of the planning kernel's work queues, and the
+// words of the counter block: [kCtrQueued + r] chunks queued at rank r,
+// [kCtrTaken + r] taken from queue r, the units in list A (vertex blocks,
+// whole chunks) and list B (index blocks), the units taken, the emission
+// CTAs finished, and (u64 at word kCtrStage) the staging buffers' fill,
+// vertices | indices << 32.  All zero between launches.
 constexpr uint32_t kTileChunks = 256;
+constexpr uint32_t kVertexBlock = 256, kIndexBlock = 2048;
 constexpr int kPlanRanks = 8;
-constexpr uint32_t kCtrQueued = 0, kCtrTaken = 8, kCtrMeshed = 16, kCtrDone = 17, kCtrWords = 32;
+constexpr uint32_t kCtrQueued = 0, kCtrTaken = 8, kCtrUnitsA = 16, kCtrUnitsB = 17, kCtrUnitsTaken = 18,
+                   kCtrDone = 19, kCtrStage = 20, kCtrWords = 32;
 
 // Lookback word: [63:62] status, [61:30] indices, [29:0] vertices.
 constexpr unsigned long long kLbAggregate = 1ull << 62;
@@ -114,13 +118,21 @@ struct BuildArgs {
     uint32_t* plan;                  // planned batch: finish counter, count, list (plan_kernel; kPlan*)
     // Split build (every chunk in shared memory, no streamed host output).
     // Per chunk c: its counts word tinfo[c] (packed counts, early-blank flag
-    // in bit 62) and, when meshed, its workspace in slot c; per tile of
-    // kTileChunks chunks the sum of its counts (verts | inds << 32).
+    // in bit 62) and, when meshed, where its staged pass 1 sits (stage_at[c]:
+    // vertices | indices << 32; all ones when the staging buffers had no
+    // room -- its workspace is then in slot c); per tile of kTileChunks
+    // chunks the sum of its counts (verts | inds << 32).
     uint8_t* slots;                  // chunks x slot_bytes, 16-byte aligned
     size_t slot_bytes;
     unsigned long long* tinfo;
     unsigned long long* tile_sum;    // zero at launch; re-zeroed by the emission kernel's last CTA
-    uint32_t* mesh_list;             // the meshed chunks, in the order the front kernel finished them
+    unsigned long long* stage_at;
+    float4* stage_pos;               // staging: per vertex position and corner b
+    uint32_t* stage_inds;            // staging: chunk-local indices
+    uint32_t stage_vcap, stage_icap;
+    unsigned long long* stage_ctr;   // the staging fill (counter block word kCtrStage)
+    unsigned long long* units;       // emission units (unit_entry): list A from the front, list B from the back
+    uint32_t unit_cap;
     uint32_t* split_queue;           // planned: kPlanRanks work queues of n entries
     uint32_t* split_ctr;             // kCtrWords counters, zero at launch (kCtr*)
     uint32_t split_planned;          // the planning kernel runs first and fills the queues
@@ -226,6 +238,8 @@ struct uww_ctx {
     uint32_t* d_plan = nullptr;   // planned batch: chunk count + list
     size_t plan_cap = 0;
     uint8_t* d_split = nullptr;   // split build: counters, tile sums, counts, queues, slots
+    uint8_t* d_stage = nullptr;   // split build: staging buffers and emission units
+    size_t stage_cap = 0;
     size_t split_cap = 0;
     uint32_t split_n = 0;         // the chunk count its layout is made for
     unsigned long long* d_state = nullptr;
