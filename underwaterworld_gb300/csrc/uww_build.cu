@@ -1164,14 +1164,13 @@ __global__ void __launch_bounds__(kPlanThreads) plan_kernel(const DevParams p, c
 //     units: blocks of its vertices, blocks of its indices.  Its counts go
 //     to tinfo and to its tile's sum.  No look-back, no control warp, no
 //     hand-offs, no ordering between CTAs.
-//   records_kernel: one CTA per tile of chunks, the records and totals.
-//   emit_kernel: the units, taken from a counter -- a vertex block's colours
-//     and normals from its staged positions to the vertex's place, an index
-//     block copied to its place.  A chunk the staging buffers had no room
+//   emit_kernel, the front kernel's programmatic dependent: its first CTAs
+//     write the records and totals, a tile of chunks each; then every CTA
+//     takes units from a counter -- a vertex block's colours and normals
+//     from its staged positions, an index block -- and, once the records
+//     are written, stores them in place.  A chunk the staging buffers had no room
 //     for (the batch's output then exceeds the capacities) left its
 //     workspace in its slot and is emitted from there by one CTA.
-// The records and emission kernels are each the programmatic dependent of
-// the kernel before them.
 // The same device functions as the pipelined build: the same bits.  The work
 // order (queues, mesh list) varies from run to run; the outputs do not.
 
@@ -1358,69 +1357,34 @@ __global__ void __launch_bounds__(MAXT, MINB) front_kernel(const DevParams p, co
     if (tid == 0 && T.errflags) atomicOr(&a.acc[1], (unsigned long long)T.errflags);
 }
 
-// The split build's records: one CTA per tile of kTileChunks chunks, the
-// prefix of the tiles before it from the tile sums, then a scan over the
-// tile; CTA 0 writes the totals.  A programmatic dependent of the front
-// kernel, and the emission kernel one of this.
-__global__ void __launch_bounds__(kTileChunks) records_kernel(const BuildArgs a)
+// Acquire load at gpu scope: the emission kernel's CTAs learn through it
+// that the records of every tile are written.
+__device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t* p)
 {
-    __shared__ SmemTables T;
-    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-    asm volatile("griddepcontrol.wait;" ::: "memory");
-    const int tid = threadIdx.x, nthr = blockDim.x;
-    const uint32_t nchunks = a.n_dev ? min(*a.n_dev, a.n) : a.n;
-    const uint32_t ntiles = (nchunks + kTileChunks - 1) / kTileChunks;
-    unsigned long long over = 0;
-    for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const uint32_t j = tile * kTileChunks + tid;
-        const unsigned long long w = j < nchunks ? __ldcg(&a.tinfo[j]) : 0ull;
-        const uint32_t nV = (uint32_t)(w & kField22), nI = (uint32_t)((w >> kIndShift) & kField22);
-        unsigned long long tv = 0ull, ti = 0ull, pv = 0ull, pi = 0ull;
-        for (uint32_t k = tid; k < tile; k += nthr) {
-            const unsigned long long s = __ldcg(&a.tile_sum[k]);
-            pv += s & 0xffffffffull;
-            pi += s >> 32;
-        }
-        block_scan2(pv, pi, &tv, &ti, T);  // tv, ti: the tiles before this one
-        unsigned long long ev = nV, ei = nI, sv = 0ull, si = 0ull;
-        block_scan2(ev, ei, &sv, &si, T);
-        ev += tv;
-        ei += ti;
-        if (j < nchunks) {
-            const bool fits = ev + nV <= a.vert_capacity && ei + nI <= a.ind_capacity;
-            uww_chunk_record rec;
-            rec.num_verts = nV;
-            rec.num_inds = nI;
-            rec.vert_offset = rec_off32(ev);
-            rec.ind_offset = rec_off32(ei);
-            rec.flags = ((w & kInfoEarlyBlank) ? UWW_CHUNK_EARLY_BLANK : 0u) | (nI ? UWW_CHUNK_HAS_MESH : 0u) |
-                        (fits ? 0u : UWW_CHUNK_OVERFLOW);
-            rec.num_active_cells = (uint32_t)((w >> kActShift) & 0x3ffffull);
-            rec.reserved[0] = rec.reserved[1] = 0;
-            a.records[j] = rec;
-            over += fits ? 0u : 1u;
-        }
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) over += __shfl_xor_sync(0xffffffffu, over, o);
-    if ((tid & 31) == 0 && over) atomicAdd(&a.totals[2], over);
-    if (blockIdx.x == 0) {
-        unsigned long long v = 0ull, i = 0ull, tv = 0ull, ti = 0ull;
-        for (uint32_t k = tid; k < ntiles; k += nthr) {
-            const unsigned long long s = __ldcg(&a.tile_sum[k]);
-            v += s & 0xffffffffull;
-            i += s >> 32;
-        }
-        block_scan2(v, i, &tv, &ti, T);
-        if (tid == 0) {
-            a.totals[0] = tv;
-            a.totals[1] = ti;
-            a.totals[3] = atomicExch(&a.acc[1], 0ull);
-        }
-    }
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
 }
 
-// a chunk's record, through L2 (written by the records kernel)
+// Thread 0 of a CTA: wait (bounded, backing off) until cond() holds; on
+// timeout raise the error flag and return false.
+template <class F>
+__device__ __forceinline__ bool wait_until(const BuildArgs& a, F cond)
+{
+    const long long t0 = clock64();
+    unsigned ns = 32;
+    while (!cond()) {
+        if (clock64() - t0 > a.spin_limit_cycles) {
+            atomicOr(&a.acc[1], (unsigned long long)kErrTimeout);
+            return false;
+        }
+        __nanosleep(ns);
+        ns = min(2u * ns, 256u);
+    }
+    return true;
+}
+
+// a chunk's record, through L2 (written by another CTA of the emission kernel)
 __device__ __forceinline__ uww_chunk_record load_record(const uww_chunk_record* r)
 {
     uww_chunk_record rec;
@@ -1439,8 +1403,8 @@ __global__ void __launch_bounds__(256, 4) emit_kernel(const DevParams p, const B
     __shared__ uint32_t next_ticket;
     const int tid = threadIdx.x, nthr = blockDim.x;
     load_tables(p, T, tid, nthr);
-    // launched as a programmatic dependent of the records kernel (itself one
-    // of the front kernel): what they wrote is read after this, through L2
+    // launched as a programmatic dependent of the front kernel: what it
+    // wrote is read after this, through L2
     asm volatile("griddepcontrol.wait;" ::: "memory");
     const uint32_t nchunks = a.n_dev ? min(*a.n_dev, a.n) : a.n;
     const uint32_t ntiles = (nchunks + kTileChunks - 1) / kTileChunks;
@@ -1449,27 +1413,100 @@ __global__ void __launch_bounds__(256, 4) emit_kernel(const DevParams p, const B
     const uint32_t nunits = na + nb;
     const bool want_color = (p.outputs & UWW_OUT_COLOR) != 0;
     const bool want_normals = (p.outputs & UWW_OUT_NORMALS) != 0 && a.normals != nullptr;
+    // ---- the records: the first CTAs, a tile of kTileChunks chunks each
+    // (one per thread), the tiles before it from the tile sums ----
+    if (blockIdx.x < ntiles) {
+        unsigned long long over = 0;
+        uint32_t tiles = 0;
+        for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++tiles) {
+            const uint32_t j = tile * kTileChunks + tid;
+            const unsigned long long w = j < nchunks ? __ldcg(&a.tinfo[j]) : 0ull;
+            const uint32_t nV = (uint32_t)(w & kField22), nI = (uint32_t)((w >> kIndShift) & kField22);
+            unsigned long long tv = 0ull, ti = 0ull, pv = 0ull, pi = 0ull;
+            for (uint32_t k = tid; k < tile; k += nthr) {
+                const unsigned long long sm = __ldcg(&a.tile_sum[k]);
+                pv += sm & 0xffffffffull;
+                pi += sm >> 32;
+            }
+            block_scan2(pv, pi, &tv, &ti, T);  // tv, ti: the tiles before this one
+            unsigned long long ev = nV, ei = nI, sv = 0ull, si = 0ull;
+            block_scan2(ev, ei, &sv, &si, T);
+            ev += tv;
+            ei += ti;
+            if (j < nchunks) {
+                const bool fits = ev + nV <= a.vert_capacity && ei + nI <= a.ind_capacity;
+                uww_chunk_record rec;
+                rec.num_verts = nV;
+                rec.num_inds = nI;
+                rec.vert_offset = rec_off32(ev);
+                rec.ind_offset = rec_off32(ei);
+                rec.flags = ((w & kInfoEarlyBlank) ? UWW_CHUNK_EARLY_BLANK : 0u) | (nI ? UWW_CHUNK_HAS_MESH : 0u) |
+                            (fits ? 0u : UWW_CHUNK_OVERFLOW);
+                rec.num_active_cells = (uint32_t)((w >> kActShift) & 0x3ffffull);
+                rec.reserved[0] = rec.reserved[1] = 0;
+                a.records[j] = rec;
+                over += fits ? 0u : 1u;
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) over += __shfl_xor_sync(0xffffffffu, over, o);
+        if ((tid & 31) == 0 && over) atomicAdd(&a.totals[2], over);
+        if (blockIdx.x == 0) {
+            unsigned long long v = 0ull, i = 0ull, tv = 0ull, ti = 0ull;
+            for (uint32_t k = tid; k < ntiles; k += nthr) {
+                const unsigned long long sm = __ldcg(&a.tile_sum[k]);
+                v += sm & 0xffffffffull;
+                i += sm >> 32;
+            }
+            block_scan2(v, i, &tv, &ti, T);
+            if (tid == 0) {
+                a.totals[0] = tv;
+                a.totals[1] = ti;
+                a.totals[3] = atomicExch(&a.acc[1], 0ull);
+            }
+        }
+        // published: the tiles' records, for every CTA's units
+        __threadfence();
+        __syncthreads();
+        if (tid == 0) atomicAdd(&a.split_ctr[kCtrRecDone], tiles);
+    }
+    // the records every unit needs are waited for only once its own work
+    // is done, just before its first store (a CTA's first unit overlaps
+    // the records' writing)
+    bool recs = false;
+    auto await_records = [&]() {
+        if (recs) return;
+        if (tid == 0) wait_until(a, [&]() { return ld_acquire_u32(&a.split_ctr[kCtrRecDone]) >= ntiles; });
+        __syncthreads();
+        recs = true;
+    };
     // ticket t: list A (vertex blocks, whole chunks) first, then list B
     // (index blocks); tickets below gridDim.x are static, the rest counted
     uint32_t t = blockIdx.x;
     while (t < nunits) {
         const unsigned long long ent = t < na ? __ldcg(&a.units[t]) : __ldcg(&a.units[a.unit_cap - 1 - (t - na)]);
         const uint32_t c = (uint32_t)ent, part = (uint32_t)(ent >> 32) & 0x0fffffffu, kind = (uint32_t)(ent >> 60);
-        const uww_chunk_record rec = load_record(&a.records[c]);
+        const unsigned long long w = __ldcg(&a.tinfo[c]);
+        const uint32_t cnV = (uint32_t)(w & kField22), cnI = (uint32_t)((w >> kIndShift) & kField22);
         __syncthreads();  // every thread has read the previous next_ticket
         if (tid == 0) next_ticket = gridDim.x + atomicAdd(&a.split_ctr[kCtrUnitsTaken], 1u);
-        if (!(rec.flags & UWW_CHUNK_OVERFLOW)) {
+        {
             if (kind == kUnitVerts) {
                 // colour and normal of a block of the chunk's vertices, from
-                // their staged positions
+                // their staged positions, then (the record known) to their place
                 const uint32_t v = part * kVertexBlock + tid;
-                if (tid < (int)kVertexBlock && v < rec.num_verts) {
+                const bool mine = tid < (int)kVertexBlock && v < cnV;
+                float2 out[3];
+                float g[3];
+                if (mine) {
                     const uint32_t sv = (uint32_t)__ldcg(&a.stage_at[c]);
                     const float4 q = __ldcg(a.stage_pos + sv + v);
-                    float2 out[3];
-                    float g[3];
                     vertex_values<O>(p, T.perm, T.gp, make_float2(q.x, q.y), make_float2(q.z, q.w), want_color,
                                      want_normals, out, g);
+                }
+                await_records();
+                const uww_chunk_record rec = load_record(&a.records[c]);
+                if (mine && !(rec.flags & UWW_CHUNK_OVERFLOW)) {
                     float2* v2 = reinterpret_cast<float2*>(a.verts + rec.vert_offset + v);
                     v2[0] = out[0];
                     v2[1] = out[1];
@@ -1480,24 +1517,31 @@ __global__ void __launch_bounds__(256, 4) emit_kernel(const DevParams p, const B
                     }
                 }
             } else if (kind == kUnitInds) {
-                // a block of the chunk's indices to their place
+                // a block of the chunk's indices (loaded), then to their place
                 const uint32_t si = (uint32_t)(__ldcg(&a.stage_at[c]) >> 32);
-                const uint32_t k0 = part * kIndexBlock, k1 = min(k0 + kIndexBlock, rec.num_inds);
+                const uint32_t k0 = part * kIndexBlock, k1 = min(k0 + kIndexBlock, cnI);
                 const uint32_t* src = a.stage_inds + si;
-                uint32_t* dst = a.inds + rec.ind_offset;
-                uint32_t w[kIndexBlock / 256];
+                uint32_t iw[kIndexBlock / 256];
 #pragma unroll
                 for (int r = 0; r < (int)(kIndexBlock / 256); ++r) {
                     const uint32_t k = k0 + (uint32_t)r * 256u + tid;
-                    w[r] = k < k1 ? __ldcg(src + k) : 0u;
+                    iw[r] = k < k1 ? __ldcg(src + k) : 0u;
                 }
+                await_records();
+                const uww_chunk_record rec = load_record(&a.records[c]);
+                if (!(rec.flags & UWW_CHUNK_OVERFLOW)) {
+                    uint32_t* dst = a.inds + rec.ind_offset;
 #pragma unroll
-                for (int r = 0; r < (int)(kIndexBlock / 256); ++r) {
-                    const uint32_t k = k0 + (uint32_t)r * 256u + tid;
-                    if (k < k1) dst[k] = w[r];
+                    for (int r = 0; r < (int)(kIndexBlock / 256); ++r) {
+                        const uint32_t k = k0 + (uint32_t)r * 256u + tid;
+                        if (k < k1) dst[k] = iw[r];
+                    }
                 }
             } else {
                 // a chunk without staging room: pass 1 and pass 2 from its slot
+                await_records();
+                const uww_chunk_record rec = load_record(&a.records[c]);
+                if (rec.flags & UWW_CHUNK_OVERFLOW) goto unit_done;
                 const uww_chunk_desc d = a.chunks[c];
                 const int N = (int)d.cells;
                 const uint32_t words = chunk_layout(N).total / 16u;
@@ -1506,7 +1550,6 @@ __global__ void __launch_bounds__(256, 4) emit_kernel(const DevParams p, const B
                 for (uint32_t i = tid; i < words; i += nthr) dst[i] = __ldcg(src + i);
                 __syncthreads();
                 const Workspace W = workspace_at(dyn_smem, N);
-                const unsigned long long w = __ldcg(&a.tinfo[c]);
                 const bool direct = direct_triangles(W, N, w & (kInfoEarlyBlank - 1));
                 const float s = __fdiv_rn((float)p.chunk_size, (float)N);
                 const EmitOut eo{a.verts, a.inds, a.edge_ids, nullptr};
@@ -1522,6 +1565,7 @@ __global__ void __launch_bounds__(256, 4) emit_kernel(const DevParams p, const B
                 }
             }
         }
+    unit_done:
         __syncthreads();  // next_ticket written; the workspace is free
         t = next_ticket;
     }
@@ -1696,20 +1740,11 @@ cudaError_t launch_build(const DevParams& p, const BuildArgs& a, bool queue, int
         cfg.attrs = attr;
         cfg.numAttrs = a.split_planned ? 1 : 0;
         if ((e = cudaLaunchKernelEx(&cfg, front_for(exact, threads), p, a)) != cudaSuccess) return e;
-        // the records, then the emission, each the programmatic dependent
-        // of the kernel before it: their CTAs start as the front kernel's
-        // CTAs finish
+        // the emission (with the records) as the front kernel's programmatic
+        // dependent: its CTAs load their tables as front CTAs finish
         cudaLaunchAttribute pdl[1];
         pdl[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
         pdl[0].val.programmaticStreamSerializationAllowed = 1;
-        const uint32_t nt = std::max(1u, (a.n + kTileChunks - 1) / kTileChunks);
-        cudaLaunchConfig_t rcfg = {};
-        rcfg.gridDim = dim3(std::min(nt, 1024u));
-        rcfg.blockDim = dim3(kTileChunks);
-        rcfg.stream = s;
-        rcfg.attrs = pdl;
-        rcfg.numAttrs = 1;
-        if ((e = cudaLaunchKernelEx(&rcfg, records_kernel, a)) != cudaSuccess) return e;
         int dev = 0, sms = 0, ebps = 0;
         const FrontFn efn = emit_for(exact);
         e = cudaGetDevice(&dev);

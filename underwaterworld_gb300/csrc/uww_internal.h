@@ -65,13 +65,14 @@ __host__ __device__ inline size_t plan_buffer_bytes(uint32_t n) { return plan_ki
 // words of the counter block: [kCtrQueued + r] chunks queued at rank r,
 // [kCtrTaken + r] taken from queue r, the units in list A (vertex blocks,
 // whole chunks) and list B (index blocks), the units taken, the emission
-// CTAs finished, and (u64 at word kCtrStage) the staging buffers' fill,
-// vertices | indices << 32.  All zero between launches.
+// CTAs finished, (u64 at word kCtrStage) the staging buffers' fill,
+// vertices | indices << 32, and the record tiles written.  All zero between
+// launches.
 constexpr uint32_t kTileChunks = 256;
 constexpr uint32_t kVertexBlock = 256, kIndexBlock = 2048;
 constexpr int kPlanRanks = 8;
 constexpr uint32_t kCtrQueued = 0, kCtrTaken = 8, kCtrUnitsA = 16, kCtrUnitsB = 17, kCtrUnitsTaken = 18,
-                   kCtrDone = 19, kCtrStage = 20, kCtrWords = 32;
+                   kCtrDone = 19, kCtrStage = 20, kCtrRecDone = 22, kCtrWords = 32;
 
 // Lookback word: [63:62] status, [61:30] indices, [29:0] vertices.
 constexpr unsigned long long kLbAggregate = 1ull << 62;
