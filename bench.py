@@ -53,15 +53,15 @@ FLOPS_PER_SAMPLE_EXTRA = 16    # world coordinates, normalisation, linear bias
 FLOPS_PER_OCTAVE_GRAD = 254    # Perlin value + analytic gradient + accumulate (normals)
 FLOPS_PER_VERTEX_EXTRA = 60    # interpolation, colour ramp, normalisation
 
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one build_kernel
-# launch on this workload, from a single-kernel ncu capture of this script's
-# own step (-k regex:build_kernel -s 12 -c 1 of
-# `bench.py --steps 5 --warmup 3 --quick --no-cpu --clock-window 0`, caches
-# flushed before the launch): 889.3 KB read + 16.4 KB written.  The outputs
-# stay in L2 (write-back) when the kernel ends, so this is below the
-# algorithmic output bytes.
-NCU_DRAM_BYTES_PER_LAUNCH = 905_728
-NCU_TRAFFIC_SOURCE = ("ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum -k regex:build_kernel -s 12 -c 1, "
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of
+# the step's dominant kernel, front_kernel, on this workload, from a
+# single-kernel ncu capture of this script's own step (-k regex:front_kernel
+# -s 12 -c 1 of `bench.py --steps 5 --warmup 3 --quick --no-cpu
+# --clock-window 0`, caches flushed before the launch): 182.8 KB read, 0
+# written.  Its staged output stays in L2 for the emission kernel, so this is
+# far below the algorithmic output bytes.
+NCU_DRAM_BYTES_PER_LAUNCH = 182_784
+NCU_TRAFFIC_SOURCE = ("ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum -k regex:front_kernel -s 12 -c 1, "
                       "python bench.py --steps 5 --warmup 3 --quick --no-cpu --clock-window 0")
 # FP32 flops the noise-stage kernel executes per launch of this workload
 # (2 x FFMA + FADD + FMUL thread instructions, ncu sm__sass_thread_inst_executed_op_*_pred_on.sum,
@@ -924,13 +924,15 @@ def main():
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded chunk grid; seeds 0-9 cycle per step)",
         "config": config_dict(n),
-        "build": "fast (FMA), persistent grid + device work queue + decoupled look-back, chunks the depth bias "
-                 "decides settled without their noise, then the per-vertex colour/normal pass",
+        "build": "fast (FMA), split build: depth-bias planning into cost-ranked work queues (chunks it decides "
+                 "settled without their noise), persistent front kernel (noise, classification, chunk-local "
+                 "pass 1 staged), emission kernel as its programmatic dependent (records, colour/normal "
+                 "blocks, index blocks)",
         "mean_verts_per_step": mean_v, "mean_inds_per_step": mean_i, "chunks_decided_by_depth_bias": decided,
         "mvoxels_per_s": value * 12 ** 3 / 1e6,
         "msamples_per_s": value * 13 ** 3 / 1e6,
-        # per step: the planning kernel, the build, the colour/normal pass
-        "gpu_launches": args.steps * (2 + (1 if params[0].outputs & (abi.UWW_OUT_COLOR | abi.UWW_OUT_NORMALS) else 0)),
+        # per step: the planning kernel, the front kernel, the emission kernel
+        "gpu_launches": args.steps * 3,
         "clocks": clk,
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": achieved / fp32_peak, "traffic": NCU_DRAM_BYTES_PER_LAUNCH,
@@ -938,6 +940,8 @@ def main():
                                     f"{peak['sm_mhz_median']} MHz (SMs x 128 x 2 x clock = "
                                     f"{peak['clock_peak_tflops']} TFLOP/s); the measured-peaks file has no FP32 entry",
                      "traffic_source": NCU_TRAFFIC_SOURCE,
+                     "kernel": "front_kernel (the noise of the evaluated chunks); achieved over the whole step "
+                               "(planning + front + emission), a lower bound on the front kernel's own rate",
                      "flops_per_step": flops,
                      "emission": {"bound": "hbm", "achieved": out_bytes / (t_total / args.steps) / 1e9,
                                   "peak": hbm_peak, "unit": "GB/s",
