@@ -707,10 +707,22 @@ int uww_build_chunks_host(uww_ctx* ctx, const uww_chunk_desc* h_chunks, uint32_t
     const bool mapped = dv && di && dr && (!want_normals || dn) && (!want_cases || dc) && (!want_samples || ds);
     LaunchCfg probe;
     if (mapped && plan_launch(ctx, n, max_cells, true, &probe) == UWW_OK && probe.split) {
-        // The split build on the device, then one copy kernel that moves
-        // every output to the host buffers, the vertex, normal and index
-        // spans sized from the device totals: no host round trip in between.
-        if ((st = launch(ctx, ctx->d_chunks, n, max_cells, &d_out, true))) return st;
+        // The split build.  Its emission kernel is the only one that writes
+        // vertices, normals and indices, each once and in place: with host
+        // buffers aligned for its stores (8 bytes for vertices) it stores
+        // them straight into them, so the host link carries the output
+        // while the emission runs.  Then one copy kernel moves the rest
+        // (records, totals; otherwise every output, the vertex, normal and
+        // index spans sized from the device totals): no host round trip in
+        // between.
+        const bool direct = aligned_to(dv, 8) && aligned_to(dn, 4) && aligned_to(di, 4);
+        uww_mesh_out o = d_out;
+        if (direct) {
+            o.verts = static_cast<uww_vert_color*>(dv);
+            o.normals = want_normals ? static_cast<float*>(dn) : nullptr;
+            o.inds = static_cast<uint32_t*>(di);
+        }
+        if ((st = launch(ctx, ctx->d_chunks, n, max_cells, &o, true))) return st;
         CopyOut c;
         std::memset(&c, 0, sizeof(c));
         auto seg = [&](const void* src, void* dst, unsigned long long fixed, int count_idx, uint32_t elem,
@@ -724,9 +736,11 @@ int uww_build_chunks_host(uww_ctx* ctx, const uww_chunk_desc* h_chunks, uint32_t
             g.cap_elems = cap;
         };
         seg(ctx->d_records, dr, (unsigned long long)n * sizeof(uww_chunk_record), -1, 0, 0);
-        seg(ctx->d_verts, dv, 0, 0, (uint32_t)sizeof(uww_vert_color), h_out->vert_capacity);
-        if (want_normals) seg(ctx->d_normals, dn, 0, 0, 12u, h_out->vert_capacity);
-        seg(ctx->d_inds, di, 0, 1, 4u, h_out->ind_capacity);
+        if (!direct) {
+            seg(ctx->d_verts, dv, 0, 0, (uint32_t)sizeof(uww_vert_color), h_out->vert_capacity);
+            if (want_normals) seg(ctx->d_normals, dn, 0, 0, 12u, h_out->vert_capacity);
+            seg(ctx->d_inds, di, 0, 1, 4u, h_out->ind_capacity);
+        }
         if (want_cases && case_bytes) seg(ctx->d_cases, dc, case_bytes, -1, 0, 0);
         if (want_samples && sample_count) seg(ctx->d_samples, ds, sample_count * 4, -1, 0, 0);
         void* dt = device_view(ctx->h_totals);

@@ -1397,7 +1397,8 @@ __device__ __forceinline__ uww_chunk_record load_record(const uww_chunk_record* 
 template <class O>
 __global__ void __launch_bounds__(256, 4) emit_kernel(const DevParams p, const BuildArgs a)
 {
-    extern __shared__ __align__(16) uint8_t dyn_smem[];  // one workspace (chunks emitted from their slot)
+    // one workspace (chunks emitted from their slot) or a gathered vertex block
+    extern __shared__ __align__(16) uint8_t dyn_smem[];
     __shared__ SmemTables T;
     __shared__ int last;
     __shared__ uint32_t next_ticket;
@@ -1493,27 +1494,34 @@ __global__ void __launch_bounds__(256, 4) emit_kernel(const DevParams p, const B
         {
             if (kind == kUnitVerts) {
                 // colour and normal of a block of the chunk's vertices, from
-                // their staged positions, then (the record known) to their place
-                const uint32_t v = part * kVertexBlock + tid;
-                const bool mine = tid < (int)kVertexBlock && v < cnV;
-                float2 out[3];
-                float g[3];
-                if (mine) {
+                // their staged positions, gathered in shared memory; then (the
+                // record known) the block's vertices and normals to their
+                // place as consecutive 4-byte words, whole sectors per warp
+                // (the outputs may be page-locked host memory)
+                const uint32_t v0 = part * kVertexBlock, v = v0 + tid;
+                const uint32_t nv = cnV > v0 ? min(kVertexBlock, cnV - v0) : 0u;
+                float* sw = reinterpret_cast<float*>(dyn_smem);  // 6 words a vertex, then 3 a normal
+                if (tid < (int)nv) {
                     const uint32_t sv = (uint32_t)__ldcg(&a.stage_at[c]);
                     const float4 q = __ldcg(a.stage_pos + sv + v);
+                    float2 out[3];
+                    float g[3];
                     vertex_values<O>(p, T.perm, T.gp, make_float2(q.x, q.y), make_float2(q.z, q.w), want_color,
                                      want_normals, out, g);
+                    float* o = sw + 6 * tid;
+                    o[0] = out[0].x; o[1] = out[0].y; o[2] = out[1].x; o[3] = out[1].y; o[4] = out[2].x; o[5] = out[2].y;
+                    float* nn = sw + 6 * kVertexBlock + 3 * tid;
+                    nn[0] = g[0]; nn[1] = g[1]; nn[2] = g[2];
                 }
                 await_records();
+                __syncthreads();  // the block is gathered
                 const uww_chunk_record rec = load_record(&a.records[c]);
-                if (mine && !(rec.flags & UWW_CHUNK_OVERFLOW)) {
-                    float2* v2 = reinterpret_cast<float2*>(a.verts + rec.vert_offset + v);
-                    v2[0] = out[0];
-                    v2[1] = out[1];
-                    v2[2] = out[2];
+                if (!(rec.flags & UWW_CHUNK_OVERFLOW)) {
+                    float* dv = reinterpret_cast<float*>(a.verts + rec.vert_offset + v0);
+                    for (uint32_t k = tid; k < 6 * nv; k += nthr) dv[k] = sw[k];
                     if (want_normals) {
-                        float* nn = a.normals + 3 * (size_t)(rec.vert_offset + v);
-                        nn[0] = g[0]; nn[1] = g[1]; nn[2] = g[2];
+                        float* dn = a.normals + 3 * (size_t)(rec.vert_offset + v0);
+                        for (uint32_t k = tid; k < 3 * nv; k += nthr) dn[k] = sw[6 * kVertexBlock + k];
                     }
                 }
             } else if (kind == kUnitInds) {
@@ -1749,12 +1757,15 @@ cudaError_t launch_build(const DevParams& p, const BuildArgs& a, bool queue, int
         const FrontFn efn = emit_for(exact);
         e = cudaGetDevice(&dev);
         if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ebps, efn, 256, a.slot_bytes);
+        // dynamic shared memory: a chunk's workspace (chunks without staging
+        // room) or a gathered vertex block (9 words a vertex), the larger
+        const size_t edyn = std::max(a.slot_bytes, (size_t)kVertexBlock * 9 * sizeof(float));
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ebps, efn, 256, edyn);
         if (e != cudaSuccess) return e;
         cudaLaunchConfig_t ecfg = {};
         ecfg.gridDim = dim3((unsigned)std::max(1, sms * std::max(1, ebps)));
         ecfg.blockDim = dim3(256);
-        ecfg.dynamicSmemBytes = a.slot_bytes;
+        ecfg.dynamicSmemBytes = edyn;
         ecfg.stream = s;
         ecfg.attrs = pdl;
         ecfg.numAttrs = 1;
