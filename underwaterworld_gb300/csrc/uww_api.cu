@@ -272,6 +272,7 @@ int launch(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint32_t ma
     a.smem_buf_bytes = cfg.smem_buf;
     a.ztable_offset = cfg.ztable_offset;
     a.mask_offset = cfg.mask_offset;
+    a.tables = static_cast<const uint2*>(ctx->d_tables);
     a.smem_cells = cfg.smem_cells;
     a.spin_limit_cycles = ctx->spin_limit > 0 ? ctx->spin_limit : kSpinLimitCycles;
     a.withhold_first = (ctx->test_flags & UWW_TEST_WITHHOLD_FIRST) ? 1u : 0u;
@@ -542,6 +543,8 @@ int uww_ctx_create(const uww_params* p, void* stream, uww_ctx** out)
         ctx->d_acc = ctx->d_state + 1;
     }
     if (e == cudaSuccess) e = cudaMalloc((void**)&ctx->d_totals, 4 * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->d_tables, table_image_bytes());
+    if (e == cudaSuccess) { where = "table image"; e = launch_table_image(ctx->dev, ctx->d_tables, ctx->stream); }
     if (e == cudaSuccess) { where = "cudaMallocHost"; e = cudaMallocHost((void**)&ctx->h_totals, 4 * sizeof(unsigned long long)); }
     if (e != cudaSuccess) {
         const int st2 = cuda_status(e, where);
@@ -558,6 +561,7 @@ int uww_ctx_destroy(uww_ctx* ctx)
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     cudaFree(ctx->d_lookback);
     cudaFree(ctx->d_plan);
+    cudaFree(ctx->d_tables);
     cudaFree(ctx->d_split);
     cudaFree(ctx->d_stage);
     cudaFree(ctx->d_state);
@@ -586,7 +590,9 @@ int uww_ctx_set_params(uww_ctx* ctx, const uww_params* p)
     if (st) return st;
     ctx->params = *p;
     make_dev_params(p, &ctx->dev);
-    return UWW_OK;
+    // the kernels' table image follows the parameters (in stream order:
+    // builds already queued use the previous image)
+    return cuda_status(launch_table_image(ctx->dev, ctx->d_tables, ctx->stream), "table image");
 }
 
 int uww_ctx_get_params(const uww_ctx* ctx, uww_params* p)

@@ -944,6 +944,33 @@ __device__ __forceinline__ void load_tables(const DevParams& p, SmemTables& T, i
     }
 }
 
+// The tables part of SmemTables (everything before the scan words) as one
+// image: built once per parameter set by table_image_kernel into a context
+// buffer, then copied by each CTA in 8-byte words -- one round of coalesced
+// loads instead of the table loads and their derivation.
+constexpr size_t kTableImageBytes = offsetof(SmemTables, warp_sums);
+static_assert(kTableImageBytes % 8 == 0, "the table image is copied in 8-byte words");
+
+__device__ __forceinline__ void load_tables_image(const DevParams& p, const BuildArgs& a, SmemTables& T, int tid,
+                                                  int nthr)
+{
+    if (!a.tables) {
+        load_tables(p, T, tid, nthr);
+        return;
+    }
+    uint2* dst = reinterpret_cast<uint2*>(&T);
+    for (int i = tid; i < (int)(kTableImageBytes / 8); i += nthr) dst[i] = __ldg(a.tables + i);
+}
+
+__global__ void __launch_bounds__(256) table_image_kernel(const DevParams p, uint2* out)
+{
+    __shared__ SmemTables T;
+    load_tables(p, T, threadIdx.x, blockDim.x);
+    __syncthreads();
+    const uint2* src = reinterpret_cast<const uint2*>(&T);
+    for (int i = threadIdx.x; i < (int)(kTableImageBytes / 8); i += blockDim.x) out[i] = src[i];
+}
+
 // MAXT/MINB: the launch bounds of an instantiation.  Chunks of up to 16 cells
 // per edge run with <= 224 threads (192 compute + the control warp) and at
 // least 4 CTAs per SM (<= 72
@@ -957,7 +984,7 @@ __global__ void __launch_bounds__(MAXT, MINB) build_kernel(const DevParams p, co
     // batched form: the last warp is the control warp
     const int ncomp = QUEUE ? nthr - 32 : nthr;
 
-    load_tables(p, T, tid, nthr);
+    load_tables_image(p, a, T, tid, nthr);
     // a planned batch reads the chunk list of the planning kernel launched
     // just before it (as a programmatic dependent: the table setup above
     // overlaps the planning)
@@ -1275,7 +1302,7 @@ __global__ void __launch_bounds__(MAXT, MINB) front_kernel(const DevParams p, co
     __shared__ uint32_t rank, unit_a, unit_b;
     __shared__ unsigned long long stage;
     const int tid = threadIdx.x, nthr = blockDim.x;
-    load_tables(p, T, tid, nthr);
+    load_tables_image(p, a, T, tid, nthr);
     // the planning kernel's queues (this kernel is its programmatic dependent)
     if (a.split_planned) asm volatile("griddepcontrol.wait;" ::: "memory");
     // the records kernel, launched after this one as its programmatic
@@ -1403,7 +1430,7 @@ __global__ void __launch_bounds__(256, 4) emit_kernel(const DevParams p, const B
     __shared__ int last;
     __shared__ uint32_t next_ticket;
     const int tid = threadIdx.x, nthr = blockDim.x;
-    load_tables(p, T, tid, nthr);
+    load_tables_image(p, a, T, tid, nthr);
     // launched as a programmatic dependent of the front kernel: what it
     // wrote is read after this, through L2
     asm volatile("griddepcontrol.wait;" ::: "memory");
@@ -1814,6 +1841,14 @@ cudaError_t launch_build(const DevParams& p, const BuildArgs& a, bool queue, int
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     return cudaLaunchKernelEx(&cfg, vfn, p, a.verts, a.normals, (const unsigned long long*)a.totals, a.vert_capacity);
+}
+
+size_t table_image_bytes() { return kTableImageBytes; }
+
+cudaError_t launch_table_image(const DevParams& p, void* out, cudaStream_t s)
+{
+    table_image_kernel<<<1, 256, 0, s>>>(p, static_cast<uint2*>(out));
+    return cudaGetLastError();
 }
 
 cudaError_t launch_copy_out(const CopyOut& c, const unsigned long long* totals, int blocks_x, cudaStream_t s)
