@@ -110,8 +110,6 @@ struct SmemTables {
     uint16_t first_ref[256];      // per case: row positions that are their edge's first reference
     unsigned long long warp_sums[32];
     unsigned long long chunk_total;
-    unsigned long long warp_sums2[32];  // split build: second component of its scans
-    unsigned long long chunk_total2;
     ChunkInfo ci[2];              // the chunks in flight (front / back)
     Ticket tk[2];                 // tickets handed from the control warp
     Offsets off[2];               // offsets handed from the control warp
@@ -1243,39 +1241,6 @@ __global__ void __launch_bounds__(kPlanThreads) split_plan_kernel(const DevParam
     }
 }
 
-// Exclusive scan of two u64 components over the CTA in thread order; the
-// totals go to *ta, *tb.  Every thread calls it.
-__device__ __forceinline__ void block_scan2(unsigned long long& a, unsigned long long& b, unsigned long long* ta,
-                                            unsigned long long* tb, SmemTables& T)
-{
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    unsigned long long ia = a, ib = b;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const unsigned long long xa = __shfl_up_sync(0xffffffffu, ia, o), xb = __shfl_up_sync(0xffffffffu, ib, o);
-        if (lane >= o) { ia += xa; ib += xb; }
-    }
-    if (lane == 31) { T.warp_sums[warp] = ia; T.warp_sums2[warp] = ib; }
-    __syncthreads();
-    if (warp == 0) {
-        const unsigned long long wa = lane < nw ? T.warp_sums[lane] : 0ull, wb = lane < nw ? T.warp_sums2[lane] : 0ull;
-        unsigned long long sa = wa, sb = wb;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const unsigned long long xa = __shfl_up_sync(0xffffffffu, sa, o), xb = __shfl_up_sync(0xffffffffu, sb, o);
-            if (lane >= o) { sa += xa; sb += xb; }
-        }
-        if (lane < nw) { T.warp_sums[lane] = sa - wa; T.warp_sums2[lane] = sb - wb; }
-        if (lane == nw - 1) { T.chunk_total = sa; T.chunk_total2 = sb; }
-    }
-    __syncthreads();
-    a = T.warp_sums[warp] + ia - a;
-    b = T.warp_sums2[warp] + ib - b;
-    *ta = T.chunk_total;
-    *tb = T.chunk_total2;
-    __syncthreads();  // the shared words are free for the next call
-}
-
 // The split build's next piece of work for this CTA (thread 0): a chunk from
 // the first queue with work left (planned), else the next chunk in order;
 // kNoChunk when there is none.
@@ -1441,26 +1406,36 @@ __global__ void __launch_bounds__(256, 4) emit_kernel(const DevParams p, const B
     const uint32_t nunits = na + nb;
     const bool want_color = (p.outputs & UWW_OUT_COLOR) != 0;
     const bool want_normals = (p.outputs & UWW_OUT_NORMALS) != 0 && a.normals != nullptr;
-    // ---- the records: the first CTAs, a tile of kTileChunks chunks each
-    // (one per thread), the tiles before it from the tile sums ----
-    if (blockIdx.x < ntiles) {
-        unsigned long long over = 0;
+    // ---- the records: one warp per tile of kTileChunks (32) chunks, one
+    // lane per chunk -- the tiles before it summed from the tile sums, then
+    // a warp scan; no CTA barrier ----
+    {
+        const int lane = tid & 31, warp = tid >> 5, nw = nthr >> 5;
         uint32_t tiles = 0;
-        for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++tiles) {
-            const uint32_t j = tile * kTileChunks + tid;
-            const unsigned long long w = j < nchunks ? __ldcg(&a.tinfo[j]) : 0ull;
-            const uint32_t nV = (uint32_t)(w & kField22), nI = (uint32_t)((w >> kIndShift) & kField22);
-            unsigned long long tv = 0ull, ti = 0ull, pv = 0ull, pi = 0ull;
-            for (uint32_t k = tid; k < tile; k += nthr) {
+        unsigned long long over = 0;
+        for (uint32_t tile = blockIdx.x * nw + warp; tile < ntiles; tile += gridDim.x * nw, ++tiles) {
+            unsigned long long pv = 0ull, pi = 0ull;
+            for (uint32_t k = lane; k < tile; k += 32) {
                 const unsigned long long sm = __ldcg(&a.tile_sum[k]);
                 pv += sm & 0xffffffffull;
                 pi += sm >> 32;
             }
-            block_scan2(pv, pi, &tv, &ti, T);  // tv, ti: the tiles before this one
-            unsigned long long ev = nV, ei = nI, sv = 0ull, si = 0ull;
-            block_scan2(ev, ei, &sv, &si, T);
-            ev += tv;
-            ei += ti;
+            const uint32_t j = tile * kTileChunks + lane;
+            const unsigned long long w = j < nchunks ? __ldcg(&a.tinfo[j]) : 0ull;
+            const uint32_t nV = (uint32_t)(w & kField22), nI = (uint32_t)((w >> kIndShift) & kField22);
+            unsigned long long ev = nV, ei = nI;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                pv += __shfl_xor_sync(0xffffffffu, pv, o);
+                pi += __shfl_xor_sync(0xffffffffu, pi, o);
+            }
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const unsigned long long xv = __shfl_up_sync(0xffffffffu, ev, o), xi = __shfl_up_sync(0xffffffffu, ei, o);
+                if (lane >= o) { ev += xv; ei += xi; }
+            }
+            ev += pv - nV;  // exclusive prefix of chunk j
+            ei += pi - nI;
             if (j < nchunks) {
                 const bool fits = ev + nV <= a.vert_capacity && ei + nI <= a.ind_capacity;
                 uww_chunk_record rec;
@@ -1476,27 +1451,36 @@ __global__ void __launch_bounds__(256, 4) emit_kernel(const DevParams p, const B
                 over += fits ? 0u : 1u;
             }
         }
+        if (tiles) {
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) over += __shfl_xor_sync(0xffffffffu, over, o);
-        if ((tid & 31) == 0 && over) atomicAdd(&a.totals[2], over);
-        if (blockIdx.x == 0) {
-            unsigned long long v = 0ull, i = 0ull, tv = 0ull, ti = 0ull;
-            for (uint32_t k = tid; k < ntiles; k += nthr) {
+            for (int o = 16; o > 0; o >>= 1) over += __shfl_xor_sync(0xffffffffu, over, o);
+            // published: this warp's tiles, for every CTA's units
+            __threadfence();
+            __syncwarp();
+            if (lane == 0) {
+                if (over) atomicAdd(&a.totals[2], over);
+                atomicAdd(&a.split_ctr[kCtrRecDone], tiles);
+            }
+        }
+        if (blockIdx.x == 0 && warp == 0) {
+            // the totals, from every tile's sum
+            unsigned long long v = 0ull, i = 0ull;
+            for (uint32_t k = lane; k < ntiles; k += 32) {
                 const unsigned long long sm = __ldcg(&a.tile_sum[k]);
                 v += sm & 0xffffffffull;
                 i += sm >> 32;
             }
-            block_scan2(v, i, &tv, &ti, T);
-            if (tid == 0) {
-                a.totals[0] = tv;
-                a.totals[1] = ti;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                v += __shfl_xor_sync(0xffffffffu, v, o);
+                i += __shfl_xor_sync(0xffffffffu, i, o);
+            }
+            if (lane == 0) {
+                a.totals[0] = v;
+                a.totals[1] = i;
                 a.totals[3] = atomicExch(&a.acc[1], 0ull);
             }
         }
-        // published: the tiles' records, for every CTA's units
-        __threadfence();
-        __syncthreads();
-        if (tid == 0) atomicAdd(&a.split_ctr[kCtrRecDone], tiles);
     }
     // the records every unit needs are waited for only once its own work
     // is done, just before its first store (a CTA's first unit overlaps

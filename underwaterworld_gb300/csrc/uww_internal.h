@@ -59,8 +59,8 @@ constexpr uint32_t kPlanDone = 0, kPlanCount = 1, kPlanList = 2;
 __host__ __device__ inline size_t plan_kinds_offset(uint32_t n) { return ((size_t)n + kPlanList) * sizeof(uint32_t); }
 __host__ __device__ inline size_t plan_buffer_bytes(uint32_t n) { return plan_kinds_offset(n) + n; }
 
-// Split build (uww_build.cu): chunks per tile of the tile sums (the records
-// kernel scans a tile with one thread per chunk), vertices and indices per
+// Split build (uww_build.cu): chunks per tile of the tile sums (the emission
+// kernel scans a tile with one warp, a lane per chunk), vertices and indices per
 // emission unit, cost ranks of the planning kernel's work queues, and the
 // words of the counter block: [kCtrQueued + r] chunks queued at rank r,
 // [kCtrTaken + r] taken from queue r, the units in list A (vertex blocks,
@@ -68,7 +68,7 @@ __host__ __device__ inline size_t plan_buffer_bytes(uint32_t n) { return plan_ki
 // CTAs finished, (u64 at word kCtrStage) the staging buffers' fill,
 // vertices | indices << 32, and the record tiles written.  All zero between
 // launches.
-constexpr uint32_t kTileChunks = 256;
+constexpr uint32_t kTileChunks = 32;
 constexpr uint32_t kVertexBlock = 256, kIndexBlock = 2048;
 constexpr int kPlanRanks = 8;
 constexpr uint32_t kCtrQueued = 0, kCtrTaken = 8, kCtrUnitsA = 16, kCtrUnitsB = 17, kCtrUnitsTaken = 18,
