@@ -335,6 +335,18 @@ __device__ __forceinline__ void safe_normalize(float g[3])
 }
 
 // Per-vertex colour: chunk.rs:208-219 -> util.rs:93-95, 122-153, 106-112.
+// fmodf(x, y) for y > 0, bit for bit: x itself when |x| < y, and x - y or
+// x - 2y when x lies in [y, 3y) -- fmod's result is exact, and so are these
+// differences (Sterbenz's lemma) -- else fmodf.  The colour ramp's arguments
+// stay in those ranges, where fmodf's general path is the slow part.
+__device__ __forceinline__ float fmod_pos(float x, float y)
+{
+    if (fabsf(x) < y) return x;
+    if (x >= y && x < 2.0f * y) return __fsub_rn(x, y);
+    if (x >= 2.0f * y && x < 3.0f * y) return __fsub_rn(x, 2.0f * y);
+    return fmodf(x, y);
+}
+
 template <class O>
 __device__ __forceinline__ void vertex_color(const DevParams& p, float world_z, int corner_b, float out[3])
 {
@@ -344,11 +356,11 @@ __device__ __forceinline__ void vertex_color(const DevParams& p, float world_z, 
     const float vi = O::div((float)(corner_b % 3), 9.0f);
     const float hue0 = O::add(-150.0f, O::mul(210.0f, mix));  // MIN_HUE + (MAX_HUE - MIN_HUE) * mix
     const float value = O::add(0.4f, vi);                      // BASE_VALUE + value_intensity
-    const float r0 = fmodf(hue0, 360.0f);
+    const float r0 = fmod_pos(hue0, 360.0f);
     const float hue = r0 < 0.f ? O::add(r0, 360.0f) : r0;      // rem_euclid
     const float c = O::mul(value, 0.6f);                       // SATURATION
     const float h = O::div(hue, 60.0f);
-    const float x = O::mul(c, O::sub(1.0f, fabsf(O::sub(fmodf(h, 2.0f), 1.0f))));
+    const float x = O::mul(c, O::sub(1.0f, fabsf(O::sub(fmod_pos(h, 2.0f), 1.0f))));
     const float m = O::sub(value, c);
     float r, gg, b;
     if (0.f <= h && h < 1.f)      { r = c; gg = x; b = 0.f; }
