@@ -265,6 +265,13 @@ typedef struct uww_tuning {
  * UWW_CHUNK_OVERFLOW and nothing written outside the output capacities.  It
  * lets a test check the timeout path without a fault or a hang. */
 #define UWW_TEST_WITHHOLD_FIRST 1u
+/* WITHHOLD_RECORDS: in the split build, the records of the batch's first
+ * tile of chunks are written but never announced, so every emission unit's
+ * wait for the records runs out (after spin_limit cycles): the build returns
+ * with UWW_ERRFLAG_TIMEOUT, stores no vertex, normal or index, and writes
+ * nothing outside the output capacities.  (The pipelined build, which the
+ * look-back flag selects, ignores it.) */
+#define UWW_TEST_WITHHOLD_RECORDS 2u
 /* The autotuner sets threads, blocks_per_sm and smem_cells and keeps the
  * context's spin_limit and test_flags. */
 int uww_ctx_set_tuning(uww_ctx* ctx, const uww_tuning* t);

@@ -1,4 +1,4 @@
-"""The batched build's bounded look-back wait, made to run out on purpose.
+"""The batched builds' bounded waits, made to run out on purpose.
 
 The device-wide prefix sum of the batched build (a decoupled look-back over
 the work-queue order) makes each chunk wait for the words its predecessors
@@ -13,6 +13,12 @@ by itself, the call reports UWW_ERR_TIMEOUT, no byte outside the output
 capacities changes, and the same context then builds the batch correctly at
 the default limit.  (The reference has no such path: a failed chunk build
 panics, state.rs:106.)
+
+The split build waits in one place: each emission CTA, before its first
+store, for the records of every tile.  UWW_TEST_WITHHOLD_RECORDS makes the
+first tile's records never be announced; the waits run out, the build
+reports UWW_ERR_TIMEOUT and stores no vertex, normal or index, and again the
+context recovers.
 """
 import ctypes as C
 
@@ -103,10 +109,54 @@ def test_spin_limit_and_test_flags_are_validated(ctx_factory):
     C.pointer(bad)[0] = t
     bad.spin_limit = -1
     assert abi.lib().uww_ctx_set_tuning(ctx.h, C.byref(bad)) == abi.UWW_ERR_INVALID_ARG
-    bad.spin_limit, bad.test_flags = 0, 2
+    bad.spin_limit, bad.test_flags = 0, 4
     assert abi.lib().uww_ctx_set_tuning(ctx.h, C.byref(bad)) == abi.UWW_ERR_INVALID_ARG
     ctx.set_tuning(threads=128)  # the launch-shape setter keeps the spin limit
     set_tuning(ctx, 5000, 0)
     ctx.set_tuning(threads=160)
     abi.check(abi.lib().uww_ctx_get_tuning(ctx.h, C.byref(t)))
     assert (t.threads, t.spin_limit, t.test_flags) == (160, 5000, 0)
+
+
+def test_withheld_records_time_out_and_the_context_recovers(ctx_factory, oracle):
+    p, d = workloads.uniform_grid(seed=4, outputs=abi.UWW_OUT_COLOR | abi.UWW_OUT_NORMALS)
+    p.math_mode = abi.UWW_MATH_FAST
+    n = len(d)
+    ref = oracle.build_chunks(p, d, precision=oracle.F32, threads=8)
+    vcap, icap = int(ref.totals[0]) + 64, int(ref.totals[1]) + 64
+    ctx = ctx_factory(p)
+    clean = ctx.build_chunks_device(d, vcap, icap)  # the same fast build, nothing withheld
+    assert clean.status == abi.UWW_OK
+    d_desc = ctx.upload(d)
+    sizes = {"verts": vcap * 24, "normals": vcap * 12, "inds": icap * 4, "records": n * 32, "totals": 32}
+    bufs = {k: DeviceArray(v + GUARD) for k, v in sizes.items()}
+    guard = np.full(max(sizes.values()) + GUARD, 0xAB, np.uint8)
+    for k, b in bufs.items():
+        abi.check(abi.lib().uww_memcpy(ctx.h, C.c_void_p(b.ptr), guard.ctypes.data_as(C.c_void_p), b.nbytes, abi.H2D))
+    out = abi.MeshOut(bufs["verts"].ptr, bufs["normals"].ptr, bufs["inds"].ptr, None, None, bufs["records"].ptr,
+                      bufs["totals"].ptr, vcap, icap, 0, 0)
+
+    set_tuning(ctx, SHORT_SPIN, abi.UWW_TEST_WITHHOLD_RECORDS)
+    abi.check(abi.lib().uww_build_chunks(ctx.h, C.c_void_p(d_desc.ptr), n, 12, C.byref(out)), "launch")
+    ctx.sync()  # the launch ended by itself
+    tot = ctx.download(bufs["totals"], (4,), np.uint64)
+    assert totals_status(tot) == abi.UWW_ERR_TIMEOUT, tot
+    # the records were written (only not announced) and the totals are right
+    np.testing.assert_array_equal(tot[:2], clean.totals[:2])
+    rec = ctx.download(bufs["records"], (n,), abi.CHUNK_RECORD_DTYPE)
+    np.testing.assert_array_equal(rec, clean.records)
+    # no vertex, normal or index stored, nothing past any capacity
+    for name in ("verts", "normals", "inds"):
+        back = ctx.download(bufs[name], (bufs[name].nbytes,), np.uint8)
+        assert np.all(back == 0xAB), f"{name}: stored although the records were never announced"
+    back = ctx.download(bufs["records"], (bufs["records"].nbytes,), np.uint8)
+    assert np.all(back[sizes["records"]:] == 0xAB)
+
+    # the same context, default limit, no injection: the batch builds correctly
+    set_tuning(ctx, 0, 0)
+    q = p.copy()
+    q.math_mode = abi.UWW_MATH_EXACT
+    ctx.set_params(q)
+    got = ctx.build_chunks_device(d, vcap, icap)
+    assert got.status == abi.UWW_OK
+    assert_batches_equal(got, ref)

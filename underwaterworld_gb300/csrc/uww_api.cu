@@ -276,6 +276,7 @@ int launch(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint32_t ma
     a.smem_cells = cfg.smem_cells;
     a.spin_limit_cycles = ctx->spin_limit > 0 ? ctx->spin_limit : kSpinLimitCycles;
     a.withhold_first = (ctx->test_flags & UWW_TEST_WITHHOLD_FIRST) ? 1u : 0u;
+    a.withhold_records = (ctx->test_flags & UWW_TEST_WITHHOLD_RECORDS) ? 1u : 0u;
     a.no_depth_shortcut = (ctx->options & UWW_TUNE_NO_DEPTH_SHORTCUT) ? 1u : 0u;
     a.edge_ids = edge_ids;
     a.n_dev = n_dev;
@@ -830,7 +831,8 @@ int uww_ctx_set_tuning(uww_ctx* ctx, const uww_tuning* t)
     if (t->threads > 192 && t->threads < 224) return UWW_ERR_INVALID_ARG;  // between the two kernel shapes
     if (t->blocks_per_sm < 0 || t->blocks_per_sm > 32) return UWW_ERR_INVALID_ARG;
     if (t->smem_cells < 0 || t->smem_cells > UWW_MAX_CELLS) return UWW_ERR_INVALID_ARG;
-    if (t->spin_limit < 0 || (t->test_flags & ~UWW_TEST_WITHHOLD_FIRST)) return UWW_ERR_INVALID_ARG;
+    if (t->spin_limit < 0 || (t->test_flags & ~(UWW_TEST_WITHHOLD_FIRST | UWW_TEST_WITHHOLD_RECORDS)))
+        return UWW_ERR_INVALID_ARG;
     if (t->options & ~(UWW_TUNE_NO_DEPTH_SHORTCUT | UWW_TUNE_PIPELINED)) return UWW_ERR_INVALID_ARG;
     ctx->threads = t->threads;
     ctx->blocks_per_sm = t->blocks_per_sm;

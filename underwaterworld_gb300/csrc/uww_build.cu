@@ -1394,6 +1394,7 @@ __global__ void __launch_bounds__(256, 4) emit_kernel(const DevParams p, const B
     __shared__ SmemTables T;
     __shared__ int last;
     __shared__ uint32_t next_ticket;
+    __shared__ int rec_wait;
     const int tid = threadIdx.x, nthr = blockDim.x;
     load_tables_image(p, a, T, tid, nthr);
     // launched as a programmatic dependent of the front kernel: what it
@@ -1459,7 +1460,9 @@ __global__ void __launch_bounds__(256, 4) emit_kernel(const DevParams p, const B
             __syncwarp();
             if (lane == 0) {
                 if (over) atomicAdd(&a.totals[2], over);
-                atomicAdd(&a.split_ctr[kCtrRecDone], tiles);
+                // (failure injection: tile 0, this warp's first, never announced)
+                const uint32_t told = tiles - ((a.withhold_records && blockIdx.x == 0 && warp == 0) ? 1u : 0u);
+                if (told) atomicAdd(&a.split_ctr[kCtrRecDone], told);
             }
         }
         if (blockIdx.x == 0 && warp == 0) {
@@ -1478,19 +1481,22 @@ __global__ void __launch_bounds__(256, 4) emit_kernel(const DevParams p, const B
             if (lane == 0) {
                 a.totals[0] = v;
                 a.totals[1] = i;
-                a.totals[3] = atomicExch(&a.acc[1], 0ull);
             }
         }
     }
     // the records every unit needs are waited for only once its own work
     // is done, just before its first store (a CTA's first unit overlaps
-    // the records' writing)
-    bool recs = false;
-    auto await_records = [&]() {
-        if (recs) return;
-        if (tid == 0) wait_until(a, [&]() { return ld_acquire_u32(&a.split_ctr[kCtrRecDone]) >= ntiles; });
-        __syncthreads();
-        recs = true;
+    // the records' writing); if the wait runs out, the CTA stores nothing
+    bool recs = false, recs_ok = false;
+    auto await_records = [&]() -> bool {
+        if (!recs) {
+            if (tid == 0)
+                rec_wait = wait_until(a, [&]() { return ld_acquire_u32(&a.split_ctr[kCtrRecDone]) >= ntiles; }) ? 1 : 0;
+            __syncthreads();
+            recs_ok = rec_wait != 0;
+            recs = true;
+        }
+        return recs_ok;
     };
     // ticket t: list A (vertex blocks, whole chunks) first, then list B
     // (index blocks); tickets below gridDim.x are static, the rest counted
@@ -1524,10 +1530,10 @@ __global__ void __launch_bounds__(256, 4) emit_kernel(const DevParams p, const B
                     float* nn = sw + 6 * kVertexBlock + 3 * tid;
                     nn[0] = g[0]; nn[1] = g[1]; nn[2] = g[2];
                 }
-                await_records();
+                const bool ok = await_records();
                 __syncthreads();  // the block is gathered
                 const uww_chunk_record rec = load_record(&a.records[c]);
-                if (!(rec.flags & UWW_CHUNK_OVERFLOW)) {
+                if (ok && !(rec.flags & UWW_CHUNK_OVERFLOW)) {
                     float* dv = reinterpret_cast<float*>(a.verts + rec.vert_offset + v0);
                     for (uint32_t k = tid; k < 6 * nv; k += nthr) dv[k] = sw[k];
                     if (want_normals) {
@@ -1546,9 +1552,9 @@ __global__ void __launch_bounds__(256, 4) emit_kernel(const DevParams p, const B
                     const uint32_t k = k0 + (uint32_t)r * 256u + tid;
                     iw[r] = k < k1 ? __ldcg(src + k) : 0u;
                 }
-                await_records();
+                const bool ok = await_records();
                 const uww_chunk_record rec = load_record(&a.records[c]);
-                if (!(rec.flags & UWW_CHUNK_OVERFLOW)) {
+                if (ok && !(rec.flags & UWW_CHUNK_OVERFLOW)) {
                     uint32_t* dst = a.inds + rec.ind_offset;
 #pragma unroll
                     for (int r = 0; r < (int)(kIndexBlock / 256); ++r) {
@@ -1558,7 +1564,7 @@ __global__ void __launch_bounds__(256, 4) emit_kernel(const DevParams p, const B
                 }
             } else {
                 // a chunk without staging room: pass 1 and pass 2 from its slot
-                await_records();
+                if (!await_records()) goto unit_done;
                 const uww_chunk_record rec = load_record(&a.records[c]);
                 if (rec.flags & UWW_CHUNK_OVERFLOW) goto unit_done;
                 const uww_chunk_desc d = a.chunks[c];
@@ -1599,6 +1605,9 @@ __global__ void __launch_bounds__(256, 4) emit_kernel(const DevParams p, const B
     __threadfence();
     for (uint32_t k = tid; k < ntiles; k += nthr) a.tile_sum[k] = 0ull;
     if (tid < kCtrWords) a.split_ctr[tid] = 0u;
+    // every error flag of the build: the front kernel's, and a wait of this
+    // one that ran out
+    if (tid == 0) a.totals[3] = atomicExch(&a.acc[1], 0ull);
 }
 
 // Pass 2 of the batched build over every vertex of the batch: vertex counts

@@ -113,6 +113,7 @@ struct BuildArgs {
     uint32_t smem_cells;             // chunks with cells <= smem_cells work in shared memory
     long long spin_limit_cycles;     // bound on every device-side wait
     uint32_t withhold_first;         // UWW_TEST_WITHHOLD_FIRST: ticket 0 never publishes its prefix
+    uint32_t withhold_records;       // UWW_TEST_WITHHOLD_RECORDS: tile 0's records are never announced
     uint32_t no_depth_shortcut;      // UWW_TUNE_NO_DEPTH_SHORTCUT: every chunk evaluates its noise
     uint32_t* edge_ids;              // optional, per output vertex: (first corner sample << 3) | direction
     const uint32_t* n_dev;           // optional device chunk count; the launch builds min(*n_dev, n)

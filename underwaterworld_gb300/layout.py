@@ -87,6 +87,7 @@ class Tuning(C.Structure):
 
 
 UWW_TEST_WITHHOLD_FIRST = 1
+UWW_TEST_WITHHOLD_RECORDS = 2
 UWW_TUNE_NO_DEPTH_SHORTCUT = 1
 UWW_TUNE_PIPELINED = 2
 
