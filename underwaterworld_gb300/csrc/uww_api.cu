@@ -591,9 +591,7 @@ int uww_ctx_set_params(uww_ctx* ctx, const uww_params* p)
     if (st) return st;
     ctx->params = *p;
     make_dev_params(p, &ctx->dev);
-    // the kernels' table image follows the parameters (in stream order:
-    // builds already queued use the previous image)
-    return cuda_status(launch_table_image(ctx->dev, ctx->d_tables, ctx->stream), "table image");
+    return UWW_OK;
 }
 
 int uww_ctx_get_params(const uww_ctx* ctx, uww_params* p)

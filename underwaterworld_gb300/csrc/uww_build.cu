@@ -99,15 +99,18 @@ struct Offsets {
 };
 
 struct SmemTables {
-    float4 gp[256];               // gradient vector of P[i] (fast build: the last hash lookup)
+    // the marching-cubes tables, the same for every parameter set (the
+    // context's table image holds them)
     int8_t tri[256][16];
     uint16_t edges[256];
-    uint8_t ntri[256];
-    uint8_t perm[256];
-    uint8_t owner[2][8][12];      // UWW_EDGE_OWNER
-    uint8_t corners[12][2];
     uint16_t owned[2][64];        // [oriented?][boundary flags] -> owned edge mask
     uint16_t first_ref[256];      // per case: row positions that are their edge's first reference
+    uint8_t ntri[256];
+    uint8_t owner[2][8][12];      // UWW_EDGE_OWNER
+    uint8_t corners[12][2];
+    // the seeded permutation and its gradients
+    float4 gp[256];               // gradient vector of P[i] (fast build: the last hash lookup)
+    uint8_t perm[256];
     unsigned long long warp_sums[32];
     unsigned long long chunk_total;
     ChunkInfo ci[2];              // the chunks in flight (front / back)
@@ -942,11 +945,12 @@ __device__ __forceinline__ void load_tables(const DevParams& p, SmemTables& T, i
     }
 }
 
-// The tables part of SmemTables (everything before the scan words) as one
-// image: built once per parameter set by table_image_kernel into a context
-// buffer, then copied by each CTA in 8-byte words -- one round of coalesced
-// loads instead of the table loads and their derivation.
-constexpr size_t kTableImageBytes = offsetof(SmemTables, warp_sums);
+// The marching-cubes part of SmemTables (everything before the permutation)
+// as one image, built once per context by table_image_kernel and copied by
+// each CTA in 8-byte words -- one round of coalesced loads instead of the
+// table loads and their derivation; the permutation and its gradients come
+// from the kernel parameters (64 threads, four entries each).
+constexpr size_t kTableImageBytes = offsetof(SmemTables, gp);
 static_assert(kTableImageBytes % 8 == 0, "the table image is copied in 8-byte words");
 
 __device__ __forceinline__ void load_tables_image(const DevParams& p, const BuildArgs& a, SmemTables& T, int tid,
@@ -958,6 +962,16 @@ __device__ __forceinline__ void load_tables_image(const DevParams& p, const Buil
     }
     uint2* dst = reinterpret_cast<uint2*>(&T);
     for (int i = tid; i < (int)(kTableImageBytes / 8); i += nthr) dst[i] = __ldg(a.tables + i);
+    for (int i = tid; i < 64; i += nthr) {
+        const uint32_t w = reinterpret_cast<const uint32_t*>(p.perm)[i];
+        reinterpret_cast<uint32_t*>(T.perm)[i] = w;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            float gx, gy, gz;
+            grad_vec((int)((w >> (8 * k)) & 255u), gx, gy, gz);
+            T.gp[4 * i + k] = make_float4(gx, gy, gz, 0.f);
+        }
+    }
 }
 
 __global__ void __launch_bounds__(256) table_image_kernel(const DevParams p, uint2* out)

@@ -139,7 +139,7 @@ struct BuildArgs {
     uint32_t* split_ctr;             // kCtrWords counters, zero at launch (kCtr*)
     uint32_t split_planned;          // the planning kernel runs first and fills the queues
     uint32_t mask_offset;            // nonzero: per-column below-iso masks at dyn smem + mask_offset
-    const uint2* tables;             // optional: the shared-memory table image (table_image_kernel)
+    const uint2* tables;             // optional: the marching-cubes table image (table_image_kernel)
     // Optional streamed host output (batched form): device addresses of
     // page-locked host memory.  Pass 2 then runs inside the build kernel, and
     // each chunk's record, indices, vertices and normals go there as soon as
@@ -166,8 +166,9 @@ struct CopyOut {
     int nseg;
 };
 cudaError_t launch_copy_out(const CopyOut& c, const unsigned long long* totals, int blocks_x, cudaStream_t s);
-// The build kernels' shared-memory tables for parameter set p, as one image
-// in device memory (table_image_bytes() bytes at out).
+// The build kernels' marching-cubes tables in shared-memory layout, as one
+// image in device memory (table_image_bytes() bytes at out), the same for
+// every parameter set.
 size_t table_image_bytes();
 cudaError_t launch_table_image(const DevParams& p, void* out, cudaStream_t s);
 
@@ -244,7 +245,7 @@ struct uww_ctx {
     size_t lookback_cap = 0;
     uint32_t* d_plan = nullptr;   // planned batch: chunk count + list
     size_t plan_cap = 0;
-    void* d_tables = nullptr;     // the table image of the current parameters
+    void* d_tables = nullptr;     // the marching-cubes table image (launch_table_image)
     uint8_t* d_split = nullptr;   // split build: counters, tile sums, counts, queues, slots
     uint8_t* d_stage = nullptr;   // split build: staging buffers and emission units
     size_t stage_cap = 0;
