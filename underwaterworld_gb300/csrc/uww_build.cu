@@ -1421,51 +1421,62 @@ __global__ void __launch_bounds__(256, 4) emit_kernel(const DevParams p, const B
     const uint32_t nunits = na + nb;
     const bool want_color = (p.outputs & UWW_OUT_COLOR) != 0;
     const bool want_normals = (p.outputs & UWW_OUT_NORMALS) != 0 && a.normals != nullptr;
-    // ---- the records: one warp per tile of kTileChunks (32) chunks, one
-    // lane per chunk -- the tiles before it summed from the tile sums, then
-    // a warp scan; no CTA barrier ----
+    // ---- the records: warp 0 of the first CTAs, one tile of kTileChunks
+    // (32) chunks each (a lane per chunk), so that the record warps spread
+    // over the SMs -- the tiles before it summed from the tile sums (all
+    // loads in flight together), then a warp scan; no CTA barrier ----
     {
-        const int lane = tid & 31, warp = tid >> 5, nw = nthr >> 5;
+        const int lane = tid & 31, warp = tid >> 5;
         uint32_t tiles = 0;
         unsigned long long over = 0;
-        for (uint32_t tile = blockIdx.x * nw + warp; tile < ntiles; tile += gridDim.x * nw, ++tiles) {
-            unsigned long long pv = 0ull, pi = 0ull;
-            for (uint32_t k = lane; k < tile; k += 32) {
-                const unsigned long long sm = __ldcg(&a.tile_sum[k]);
-                pv += sm & 0xffffffffull;
-                pi += sm >> 32;
-            }
-            const uint32_t j = tile * kTileChunks + lane;
-            const unsigned long long w = j < nchunks ? __ldcg(&a.tinfo[j]) : 0ull;
-            const uint32_t nV = (uint32_t)(w & kField22), nI = (uint32_t)((w >> kIndShift) & kField22);
-            unsigned long long ev = nV, ei = nI;
+        if (warp == 0)
+            for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++tiles) {
+                const uint32_t j = tile * kTileChunks + lane;
+                const unsigned long long w = j < nchunks ? __ldcg(&a.tinfo[j]) : 0ull;
+                unsigned long long pv = 0ull, pi = 0ull;
+                for (uint32_t k0 = 0; k0 < tile; k0 += 8 * 32) {
+                    unsigned long long sm[8];
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                pv += __shfl_xor_sync(0xffffffffu, pv, o);
-                pi += __shfl_xor_sync(0xffffffffu, pi, o);
-            }
+                    for (int r = 0; r < 8; ++r) {
+                        const uint32_t k = k0 + (uint32_t)r * 32u + lane;
+                        sm[r] = k < tile ? __ldcg(&a.tile_sum[k]) : 0ull;
+                    }
 #pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const unsigned long long xv = __shfl_up_sync(0xffffffffu, ev, o), xi = __shfl_up_sync(0xffffffffu, ei, o);
-                if (lane >= o) { ev += xv; ei += xi; }
+                    for (int r = 0; r < 8; ++r) {
+                        pv += sm[r] & 0xffffffffull;
+                        pi += sm[r] >> 32;
+                    }
+                }
+                const uint32_t nV = (uint32_t)(w & kField22), nI = (uint32_t)((w >> kIndShift) & kField22);
+                unsigned long long ev = nV, ei = nI;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    pv += __shfl_xor_sync(0xffffffffu, pv, o);
+                    pi += __shfl_xor_sync(0xffffffffu, pi, o);
+                }
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const unsigned long long xv = __shfl_up_sync(0xffffffffu, ev, o),
+                                             xi = __shfl_up_sync(0xffffffffu, ei, o);
+                    if (lane >= o) { ev += xv; ei += xi; }
+                }
+                ev += pv - nV;  // exclusive prefix of chunk j
+                ei += pi - nI;
+                if (j < nchunks) {
+                    const bool fits = ev + nV <= a.vert_capacity && ei + nI <= a.ind_capacity;
+                    uww_chunk_record rec;
+                    rec.num_verts = nV;
+                    rec.num_inds = nI;
+                    rec.vert_offset = rec_off32(ev);
+                    rec.ind_offset = rec_off32(ei);
+                    rec.flags = ((w & kInfoEarlyBlank) ? UWW_CHUNK_EARLY_BLANK : 0u) |
+                                (nI ? UWW_CHUNK_HAS_MESH : 0u) | (fits ? 0u : UWW_CHUNK_OVERFLOW);
+                    rec.num_active_cells = (uint32_t)((w >> kActShift) & 0x3ffffull);
+                    rec.reserved[0] = rec.reserved[1] = 0;
+                    a.records[j] = rec;
+                    over += fits ? 0u : 1u;
+                }
             }
-            ev += pv - nV;  // exclusive prefix of chunk j
-            ei += pi - nI;
-            if (j < nchunks) {
-                const bool fits = ev + nV <= a.vert_capacity && ei + nI <= a.ind_capacity;
-                uww_chunk_record rec;
-                rec.num_verts = nV;
-                rec.num_inds = nI;
-                rec.vert_offset = rec_off32(ev);
-                rec.ind_offset = rec_off32(ei);
-                rec.flags = ((w & kInfoEarlyBlank) ? UWW_CHUNK_EARLY_BLANK : 0u) | (nI ? UWW_CHUNK_HAS_MESH : 0u) |
-                            (fits ? 0u : UWW_CHUNK_OVERFLOW);
-                rec.num_active_cells = (uint32_t)((w >> kActShift) & 0x3ffffull);
-                rec.reserved[0] = rec.reserved[1] = 0;
-                a.records[j] = rec;
-                over += fits ? 0u : 1u;
-            }
-        }
         if (tiles) {
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) over += __shfl_xor_sync(0xffffffffu, over, o);
@@ -1475,11 +1486,11 @@ __global__ void __launch_bounds__(256, 4) emit_kernel(const DevParams p, const B
             if (lane == 0) {
                 if (over) atomicAdd(&a.totals[2], over);
                 // (failure injection: tile 0, this warp's first, never announced)
-                const uint32_t told = tiles - ((a.withhold_records && blockIdx.x == 0 && warp == 0) ? 1u : 0u);
+                const uint32_t told = tiles - ((a.withhold_records && blockIdx.x == 0) ? 1u : 0u);
                 if (told) atomicAdd(&a.split_ctr[kCtrRecDone], told);
             }
         }
-        if (blockIdx.x == 0 && warp == 0) {
+        if (blockIdx.x == 0 && warp == 1) {
             // the totals, from every tile's sum
             unsigned long long v = 0ull, i = 0ull;
             for (uint32_t k = lane; k < ntiles; k += 32) {
