@@ -462,8 +462,12 @@ __device__ void chunk_front(const DevParams& p, const BuildArgs& a, SmemTables& 
         if (!bad && cases_ok)
             for (int c = tid; c < NC; c += ncomp) a.cases[(size_t)d.cell_offset + c] = solid ? 255 : 0;
     } else {
-        // ---- classify + count, contiguous runs of cells per thread ----
-        const int R = (NC + ncomp - 1) / ncomp;
+        // ---- classify + count, contiguous runs of cells per thread: with
+        // column masks and a thread for every column, a run is one column
+        // (its quiet cells settled together by bit operations, its active
+        // cells visited alone); else the cells split evenly ----
+        const bool colrun = masks && N <= 16 && N * N <= ncomp && (uint32_t)N <= a.smem_cells;
+        const int R = colrun ? N : (NC + ncomp - 1) / ncomp;
         const int c0 = min(tid * R, NC), c1 = min(c0 + R, NC);
         // up to 16 cells of a run keep their counts in registers for the
         // second pass, 8 bits a cell: triangles | new vertices << 3
@@ -472,7 +476,34 @@ __device__ void chunk_front(const DevParams& p, const BuildArgs& a, SmemTables& 
         unsigned long long mine = 0ull;
         unsigned actbits = 0;  // (keep) bit i: cell c0 + i is active
         const int x0 = c0 / (N * N), y0 = (c0 / N) % N, z0 = c0 % N;
-        {
+        if (colrun) {
+            if (c0 < c1) {
+                const int col = x0 * S + y0;
+                const unsigned long long m00 = masks[col], m10 = masks[col + S], m01 = masks[col + 1],
+                                         m11 = masks[col + S + 1];
+                const unsigned long long an = m00 & m10 & m01 & m11, no = ~(m00 | m10 | m01 | m11);
+                const unsigned long long allin = an & (an >> 1), quiet = allin | (no & (no >> 1));
+                const unsigned long long cellbits = (1ull << N) - 1ull;
+                if (cases_ok || !keep) {
+                    // the quiet cells' cases are read (by the cases output)
+                    for (int z = 0; z < N; ++z)
+                        if ((quiet >> z) & 1ull) cases[c0 + z] = ((allin >> z) & 1ull) ? 255 : 0;
+                }
+                const unsigned own_lo = (x0 == 0) | ((y0 == 0) << 1) | ((x0 == N - 1) << 3) | ((y0 == N - 1) << 4);
+                for (unsigned long long act = ~quiet & cellbits; act; act &= act - 1ull) {
+                    const int z = __ffsll((long long)act) - 1;
+                    const int cs = mask_case(m00, m10, m01, m11, z);
+                    cases[c0 + z] = (uint8_t)cs;
+                    const int nt = T.ntri[cs];
+                    const unsigned own = T.owned[oriented][own_lo | ((z == 0) << 2) | ((z == N - 1) << 5)];
+                    const unsigned nv = __popc(T.edges[cs] & own);
+                    mine += (unsigned long long)nv | ((unsigned long long)(3 * nt) << kIndShift) | (1ull << kActShift);
+                    const unsigned long long v = (unsigned long long)(nt | (nv << 3)) << (8 * (z & 7));
+                    if (z < 8) kept0 |= v; else kept1 |= v;
+                    actbits |= 1u << z;
+                }
+            }
+        } else {
             int x = x0, y = y0, z = z0;
             const float iso = p.iso_level;
             const int SS = S * S;
