@@ -292,6 +292,28 @@ int uww_ctx_get_tuning(const uww_ctx* ctx, uww_tuning* t);
 int uww_autotune(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint32_t max_cells,
                  const uww_mesh_out* out, const char* cache_path, uww_tuning* best, float* best_us);
 
+/* The launch shape a batched build (uww_build_chunks) of n chunks of up to
+ * max_cells cells per edge takes with the context's parameters and tuning,
+ * for diagnostics and tests (no counterpart in the reference): the build
+ * (UWW_BUILD_SPLIT: planning, front and emission kernels; UWW_BUILD_PIPELINED:
+ * the single persistent kernel), the most x slabs a chunk is built as (1:
+ * every chunk whole; chunks above 16 cells per edge are built as slabs of a
+ * few cell layers by the split build of a planned batch), the compute threads
+ * per CTA, the (front) kernel's grid, its resident CTAs per SM and its dynamic
+ * shared memory.  It assumes per-cell cases and samples are written exactly
+ * when the parameters' outputs ask for them. */
+#define UWW_BUILD_PIPELINED 0u
+#define UWW_BUILD_SPLIT     1u
+typedef struct uww_launch_shape {
+    uint32_t build;
+    uint32_t slabs_per_chunk;
+    uint32_t threads;
+    uint32_t grid;
+    uint32_t blocks_per_sm;
+    uint32_t dyn_smem;
+} uww_launch_shape;
+int uww_launch_shape_of(uww_ctx* ctx, uint32_t n, uint32_t max_cells, uww_launch_shape* out);
+
 /* ---- per-frame build as a CUDA graph -------------------------------------------- */
 /* Replaces World::build_step's per-frame slice of chunk builds (world.rs:113-145)
  * with one graph launch: copy h_chunks[0..max_chunks) and *h_count (page-locked

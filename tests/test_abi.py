@@ -117,7 +117,7 @@ def test_ctypes_mirrors_match_the_header_layouts(tmp_path):
     mirrors = {"uww_params": abi.Params, "uww_chunk_desc": abi.ChunkDesc, "uww_chunk_record": abi.ChunkRecord,
                "uww_mesh_out": abi.MeshOut, "uww_ray_scene": abi.RayScene,
                "uww_schedule_params": abi.ScheduleParams, "uww_camera_uniform": abi.CameraUniform,
-               "uww_tuning": abi.Tuning}
+               "uww_tuning": abi.Tuning, "uww_launch_shape": abi.LaunchShape}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "uww.h"', "int main(void) {"]
     for cname, cls in mirrors.items():
         lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')

@@ -1,0 +1,149 @@
+"""Chunks above 16 cells per edge built as x slabs by the split build.
+
+The split build of a planned batch (no per-cell cases or samples, depth
+shortcut on) builds every chunk of 17..63 cells per edge as slabs of a few
+cell layers, one CTA each; a slab's references to vertices of the previous
+slab's last layer go through that slab's seam.  The output must be the
+chunk's, bit for bit: against the F32 oracle (parity build, chunk.rs:135-264
+with perlin_util.rs:6-29), and against the single pipelined kernel, which
+builds each chunk whole (fast build).  Covered: the uneven-LOD batch
+(12^3 / 24^3 / 48^3), both dedup modes, odd sizes (17, 31 and 63 cells: the
+last slab shorter than the others), and a batch whose output exceeds the
+capacities, so that slabs find no room in the staging buffers and the
+emission kernel builds them again in place.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from underwaterworld_gb300 import abi, workloads
+from underwaterworld_gb300.chunk import make_descs
+
+from helpers import assert_batches_equal, relayout
+
+pytestmark = pytest.mark.gpu
+
+THREADS = os.cpu_count() or 1
+COLOR_NORMALS = abi.UWW_OUT_COLOR | abi.UWW_OUT_NORMALS
+
+
+def caps(ref):
+    return max(int(ref.totals[0]), 1), max(int(ref.totals[1]), 1)
+
+
+def assert_same_bytes(a, b):
+    np.testing.assert_array_equal(a.records, b.records)
+    np.testing.assert_array_equal(a.totals, b.totals)
+    np.testing.assert_array_equal(a.inds, b.inds)
+    np.testing.assert_array_equal(a.verts.view(np.uint32), b.verts.view(np.uint32))
+    if a.normals is not None:
+        np.testing.assert_array_equal(a.normals.view(np.uint32), b.normals.view(np.uint32))
+
+
+def odd_sizes(seed=0, n=96):
+    """Chunks of 17, 31 and 63 cells around the surface of the mixed-LOD world."""
+    p, _ = workloads.mixed_lod(seed=seed, outputs=COLOR_NORMALS)
+    rng = np.random.default_rng(seed)
+    pos = np.stack([rng.integers(-8, 8, n), rng.integers(-8, 8, n), rng.integers(-2, 2, n)], -1)
+    cells = rng.choice(np.array([12, 17, 31, 63]), size=n)
+    return p, make_descs(pos, cells)
+
+
+def test_mixed_batch_takes_the_slab_build(ctx_factory):
+    p, d = workloads.mixed_lod(seed=0, outputs=COLOR_NORMALS)
+    ctx = ctx_factory(p)
+    s = ctx.launch_shape(len(d), 48)
+    assert s.build == abi.UWW_BUILD_SPLIT and s.slabs_per_chunk > 1 and s.threads == 256
+    # per-cell cases are written chunk by chunk: the pipelined build
+    q = p.copy()
+    q.outputs = COLOR_NORMALS | abi.UWW_OUT_CASES
+    assert ctx_factory(q).launch_shape(len(d), 48).build == abi.UWW_BUILD_PIPELINED
+    ctx.set_tuning(options=abi.UWW_TUNE_PIPELINED)
+    assert ctx.launch_shape(len(d), 48).build == abi.UWW_BUILD_PIPELINED
+    ctx.set_tuning(options=0)
+
+
+@pytest.mark.parametrize("dedup", [abi.UWW_DEDUP_ORIENTED, abi.UWW_DEDUP_EDGE])
+def test_slab_build_bit_exact_against_the_oracle(ctx_factory, oracle, dedup):
+    p, d = workloads.mixed_lod(seed=0, outputs=COLOR_NORMALS)
+    p.dedup_mode = dedup
+    if dedup == abi.UWW_DEDUP_EDGE:
+        d = relayout(d[:768])
+    ref = oracle.build_chunks(p, d, precision=oracle.F32, threads=THREADS)
+    ctx = ctx_factory(p)
+    assert ctx.launch_shape(len(d), 48).slabs_per_chunk > 1
+    got = ctx.build_chunks_device(d, *caps(ref))
+    assert got.status == abi.UWW_OK
+    assert_batches_equal(got, ref)
+    big = d["cells"] > 16
+    assert (ref.records["flags"][big] & abi.UWW_CHUNK_HAS_MESH).sum() > 20
+
+
+def test_odd_sizes_bit_exact_against_the_oracle(ctx_factory, oracle):
+    p, d = odd_sizes()
+    ref = oracle.build_chunks(p, d, precision=oracle.F32, threads=THREADS)
+    got = ctx_factory(p).build_chunks_device(d, *caps(ref))
+    assert got.status == abi.UWW_OK
+    assert_batches_equal(got, ref)
+    assert (ref.records["flags"][d["cells"] == 63] & abi.UWW_CHUNK_HAS_MESH).sum() > 3
+
+
+@pytest.mark.parametrize("seed", [0, 5])
+def test_slab_and_pipelined_builds_give_the_same_bytes(ctx_factory, seed):
+    p, d = workloads.mixed_lod(seed=seed, outputs=COLOR_NORMALS)
+    p.math_mode = abi.UWW_MATH_FAST
+    ctx = ctx_factory(p)
+    slabs = ctx.build_chunks_device(d, 1 << 20, 1 << 22)
+    ctx.set_tuning(options=abi.UWW_TUNE_PIPELINED)
+    piped = ctx.build_chunks_device(d, 1 << 20, 1 << 22)
+    ctx.set_tuning(options=0)
+    again = ctx.build_chunks_device(d, 1 << 20, 1 << 22)
+    for b in (slabs, piped, again):
+        assert b.status == abi.UWW_OK
+    assert_same_bytes(slabs, piped)
+    assert_same_bytes(slabs, again)
+
+
+def test_odd_sizes_fast_build_matches_the_pipelined_build(ctx_factory):
+    p, d = odd_sizes(seed=1)
+    p.math_mode = abi.UWW_MATH_FAST
+    p.dedup_mode = abi.UWW_DEDUP_EDGE
+    ctx = ctx_factory(p)
+    slabs = ctx.build_chunks_device(d, 1 << 20, 1 << 22)
+    ctx.set_tuning(options=abi.UWW_TUNE_PIPELINED)
+    piped = ctx.build_chunks_device(d, 1 << 20, 1 << 22)
+    ctx.set_tuning(options=0)
+    assert slabs.status == abi.UWW_OK and piped.status == abi.UWW_OK
+    assert_same_bytes(slabs, piped)
+
+
+@pytest.mark.parametrize("frac", [0.5, 0.97])
+def test_slabs_without_staging_room(ctx_factory, frac):
+    """Capacities below the batch's output: the staging buffers (as large as the
+    outputs) run out, so some slabs are built again by the emission kernel;
+    chunks that fit are written as the pipelined build writes them, the rest
+    are flagged, and nothing lands past the capacities."""
+    p, d = workloads.mixed_lod(seed=3, outputs=COLOR_NORMALS)
+    p.math_mode = abi.UWW_MATH_FAST
+    ctx = ctx_factory(p)
+    full = ctx.build_chunks_device(d, 1 << 20, 1 << 22)
+    assert full.status == abi.UWW_OK
+    vcap, icap = int(full.totals[0] * frac), int(full.totals[1] * frac)
+    small = ctx.build_chunks_device(d, vcap, icap)
+    ctx.set_tuning(options=abi.UWW_TUNE_PIPELINED)
+    piped = ctx.build_chunks_device(d, vcap, icap)
+    ctx.set_tuning(options=0)
+    assert small.status == abi.UWW_ERR_CAPACITY and piped.status == abi.UWW_ERR_CAPACITY
+    np.testing.assert_array_equal(small.records, piped.records)
+    np.testing.assert_array_equal(small.totals[:3], piped.totals[:3])
+    ok = (small.records["flags"] & abi.UWW_CHUNK_OVERFLOW) == 0
+    assert ok.sum() > 100 and (~ok).sum() > 0
+    rec = full.records
+    for i in np.nonzero(ok & (rec["num_inds"] > 0))[0]:
+        v0, nv = rec["vert_offset"][i], rec["num_verts"][i]
+        i0, ni = rec["ind_offset"][i], rec["num_inds"][i]
+        np.testing.assert_array_equal(small.inds[i0:i0 + ni], full.inds[i0:i0 + ni])
+        np.testing.assert_array_equal(small.verts[v0:v0 + nv].view(np.uint32), full.verts[v0:v0 + nv].view(np.uint32))
+        np.testing.assert_array_equal(small.normals[v0:v0 + nv].view(np.uint32),
+                                      full.normals[v0:v0 + nv].view(np.uint32))

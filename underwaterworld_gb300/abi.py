@@ -19,7 +19,7 @@ HEADER = ROOT / "include" / "uww.h"
 from .layout import *  # noqa: F401,F403
 from .layout import (CHUNK_DESC_DTYPE, CHUNK_RECORD_DTYPE, VERT_COLOR_DTYPE, UWW_ERR_CUDA,  # noqa: F401
                      UWW_ERR_OOM, UWW_MAX_OCTAVES, UWW_OK, CameraUniform, ChunkDesc, ChunkRecord, MeshOut,
-                     Params, RayScene, ScheduleParams, Tuning, theta_count)
+                     Params, RayScene, ScheduleParams, Tuning, LaunchShape, theta_count)
 
 P = C.c_void_p
 _SIGS = {
@@ -42,6 +42,7 @@ _SIGS = {
     "uww_build_chunks_host": (C.c_int, [P, P, C.c_uint32, C.POINTER(MeshOut)]),
     "uww_ctx_set_tuning": (C.c_int, [P, C.POINTER(Tuning)]),
     "uww_ctx_get_tuning": (C.c_int, [P, C.POINTER(Tuning)]),
+    "uww_launch_shape_of": (C.c_int, [P, C.c_uint32, C.c_uint32, C.POINTER(LaunchShape)]),
     "uww_device_alloc": (C.c_int, [C.c_size_t, C.POINTER(P)]),
     "uww_device_free": (C.c_int, [P]),
     "uww_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(P)]),

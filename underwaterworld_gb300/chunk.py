@@ -112,6 +112,14 @@ class Context:
             t.options = options
         check(lib().uww_ctx_set_tuning(self.h, C.byref(t)), "uww_ctx_set_tuning")
 
+    def launch_shape(self, n: int, max_cells: int) -> abi.LaunchShape:
+        """The launch shape of a batched build of n chunks of up to max_cells
+        cells per edge (uww_launch_shape_of): which build, slabs per chunk,
+        threads, grid, CTAs per SM, dynamic shared memory."""
+        s = abi.LaunchShape()
+        check(lib().uww_launch_shape_of(self.h, n, max_cells, C.byref(s)), "uww_launch_shape_of")
+        return s
+
     def stream(self) -> int:
         return lib().uww_ctx_stream(self.h) or 0
 

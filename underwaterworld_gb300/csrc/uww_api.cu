@@ -147,15 +147,71 @@ struct LaunchCfg {
     uint32_t mask_offset;  // split front kernel: column masks in dynamic shared memory (0: none)
     size_t scratch_slot;
     bool split;            // the split build: front kernel, then emission over every triangle
+    uint32_t pmax;         // split build: places per chunk (> 1: chunks above 16 cells are built as slabs)
+    size_t slab_slot;      // bytes of the largest slab workspace (the emission's per-CTA scratch)
 };
+
+// Whether a batched build is planned (a first kernel decides chunks by their
+// depth bias and queues the rest): nothing reads or writes its samples or
+// cases, and the depth shortcut is on.
+bool plans(const uww_ctx* ctx, const uww_mesh_out* out, const float* samples_in)
+{
+    const bool samples_out = (ctx->params.outputs & UWW_OUT_SAMPLES) && (!out || out->samples);
+    const bool cases = (ctx->params.outputs & UWW_OUT_CASES) && (!out || out->cases);
+    return !samples_in && !samples_out && !cases && !(ctx->options & UWW_TUNE_NO_DEPTH_SHORTCUT);
+}
 
 // split_ok: nothing of the launch needs the pipelined kernel (streamed host
 // output and per-vertex edge ids do)
-int plan_launch(uww_ctx* ctx, uint32_t n, uint32_t max_cells, bool queue, LaunchCfg* cfg, bool split_ok = true)
+int plan_launch(uww_ctx* ctx, uint32_t n, uint32_t max_cells, bool queue, LaunchCfg* cfg, bool split_ok, bool planned)
 {
     const size_t cap = ctx->smem_dyn_max;
     const int compute = ctx->threads > 0 ? ctx->threads : default_compute_threads(max_cells);
     const size_t zt_max = ctx->dev.math_mode == UWW_MATH_FAST ? ztable_bytes((int)max_cells + 1, ctx->dev.octaves) : 0;
+    cfg->pmax = 1;
+    cfg->slab_slot = 0;
+    // A planned batch with chunks above 16 cells per edge (the 24^3 and 48^3
+    // LODs): the split build, with those chunks as slabs of a few x layers
+    // (one CTA of kSlabThreads threads each) and the rest whole, in one
+    // shared workspace sized for the larger of a 16^3 chunk and a slab.
+    if (queue && split_ok && planned && max_cells > 16 && max_cells <= (uint32_t)kSlabMaxCells &&
+        n < (1u << kPieceShift) && !(ctx->options & UWW_TUNE_PIPELINED) &&
+        !(ctx->test_flags & UWW_TEST_WITHHOLD_FIRST) && ctx->smem_cells <= 0 &&
+        (ctx->threads <= 0 || ctx->threads == kSlabThreads)) {
+        uint32_t slab_bytes = 0;
+        int pmax = 1;
+        for (int N = 17; N <= (int)max_cells; ++N) {
+            slab_bytes = std::max(slab_bytes, slab_layout(N).total);
+            pmax = std::max(pmax, slab_count(N));
+        }
+        const size_t ws = std::max<size_t>(chunk_layout(16).total, slab_bytes);
+        size_t dyn = ws + zt_max;
+        uint32_t mo = 0;
+        if (ctx->dev.math_mode == UWW_MATH_FAST) {
+            mo = (uint32_t)((dyn + 15) & ~size_t(15));
+            dyn = mo + 13 * 13 * sizeof(unsigned long long);
+        }
+        if (dyn <= cap) {
+            cfg->split = true;
+            cfg->pmax = (uint32_t)pmax;
+            cfg->slab_slot = align16(slab_bytes);
+            cfg->smem_cells = 16;
+            cfg->slots = 1;
+            cfg->smem_buf = ws;
+            cfg->ztable_offset = ws;
+            cfg->dyn_smem = dyn;
+            cfg->mask_offset = mo;
+            cfg->threads = kSlabThreads;
+            cfg->scratch_slot = 0;
+            const bool exact = ctx->dev.math_mode == UWW_MATH_EXACT;
+            cudaError_t e = front_occupancy(exact, cfg->threads, cfg->dyn_smem, &cfg->occupancy);
+            if (e != cudaSuccess) return cuda_status(e);
+            const int bps = ctx->blocks_per_sm > 0 ? ctx->blocks_per_sm : cfg->occupancy;
+            if (bps < 1) return UWW_ERR_INVALID_ARG;
+            cfg->grid = (int)std::min<long long>((long long)bps * ctx->num_sms, (long long)n * pmax);
+            return UWW_OK;
+        }
+    }
     // A batch whose every chunk fits one shared-memory workspace is built in
     // two kernels (the front half of every chunk, then the emission of every
     // triangle); the look-back test flag and the PIPELINED option keep the
@@ -233,7 +289,8 @@ int launch(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint32_t ma
            const HostOut* host = nullptr)
 {
     LaunchCfg cfg;
-    int st = plan_launch(ctx, n, max_cells, queue, &cfg, host == nullptr && edge_ids == nullptr);
+    int st = plan_launch(ctx, n, max_cells, queue, &cfg, host == nullptr && edge_ids == nullptr,
+                         plans(ctx, out, samples_in));
     if (st) return st;
     // the work buffers a captured frame graph refers to: a reallocation
     // moves the context's generation on, and such a frame recaptures itself
@@ -323,14 +380,17 @@ int launch(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint32_t ma
             // one launch to the next -- then per chunk a workspace slot.  The
             // counters and tile sums are zero at launch: cleared here on
             // (re)allocation and left zero by every launch's emission kernel.
-            const size_t slot = align16(chunk_layout((int)max_cells).total);
-            auto fixed_bytes = [](uint32_t m) {
+            // (with slabs: a place per slab for the staging places and the
+            // queues; the slots hold whole chunks of up to 16 cells)
+            const size_t pm = cfg.pmax;
+            const size_t slot = align16(chunk_layout(pm > 1 ? 16 : (int)max_cells).total);
+            auto fixed_bytes = [pm](uint32_t m) {
                 const size_t ntiles = ((size_t)m + kTileChunks - 1) / kTileChunks;
-                return kCtrWords * 4 + ((ntiles * 8 + 15) & ~size_t(15)) + 2 * (((size_t)m * 8 + 15) & ~size_t(15)) +
-                       (((size_t)m * 4 * kPlanRanks + 15) & ~size_t(15));
+                return kCtrWords * 4 + ((ntiles * 8 + 15) & ~size_t(15)) + (((size_t)m * 8 + 15) & ~size_t(15)) +
+                       (((size_t)m * pm * 8 + 15) & ~size_t(15)) + (((size_t)m * pm * 4 * kPlanRanks + 15) & ~size_t(15));
             };
             const uint32_t m = std::max(n, ctx->split_n);
-            if (!ctx->d_split || ctx->split_n < n || ctx->split_cap < fixed_bytes(m) + (size_t)n * slot) {
+            if (!ctx->d_split || ctx->split_n < n || ctx->split_cap < fixed_bytes(m) + (size_t)m * slot) {
                 const uint32_t mm = std::max(m, 4096u);
                 st = grow(&ctx->d_split, &ctx->split_cap, fixed_bytes(mm) + (size_t)mm * slot);
                 if (st) return st;
@@ -350,18 +410,37 @@ int launch(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint32_t ma
             a.tinfo = reinterpret_cast<unsigned long long*>(b);
             b += ((size_t)nc * 8 + 15) & ~size_t(15);
             a.stage_at = reinterpret_cast<unsigned long long*>(b);
-            b += ((size_t)nc * 8 + 15) & ~size_t(15);
+            b += ((size_t)nc * pm * 8 + 15) & ~size_t(15);
             a.split_queue = reinterpret_cast<uint32_t*>(b);
-            b += ((size_t)nc * 4 * kPlanRanks + 15) & ~size_t(15);
+            b += ((size_t)nc * pm * 4 * kPlanRanks + 15) & ~size_t(15);
             a.slots = b;
             a.slot_bytes = slot;
+            a.pmax = (uint32_t)pm;
+            a.piece_cells = 16;
+            if (pm > 1) {
+                // per place its counts and its seam (rewritten by every
+                // launch), and the emission CTAs' scratch for slabs built again
+                const size_t pinfo_bytes = ((size_t)n * pm * 8 + 15) & ~size_t(15);
+                a.seam_stride = max_cells * max_cells;
+                if ((st = grow(&ctx->d_slab, &ctx->slab_cap, pinfo_bytes + (size_t)n * pm * a.seam_stride * 4)))
+                    return st;
+                a.pinfo = reinterpret_cast<unsigned long long*>(ctx->d_slab);
+                a.seam = reinterpret_cast<uint32_t*>(ctx->d_slab + pinfo_bytes);
+                int egrid = 0;
+                size_t edyn = 0;
+                cudaError_t e = split_emit_shape(ctx->dev, a, &egrid, &edyn);
+                if (e != cudaSuccess) return cuda_status(e);
+                if ((st = grow(&ctx->d_scratch, &ctx->scratch_cap, cfg.slab_slot * (size_t)egrid))) return st;
+                a.scratch = ctx->d_scratch;
+                a.scratch_slot_bytes = cfg.slab_slot;
+            }
             // staging as large as the outputs (a batch whose output fits its
             // capacities is always staged whole), and the emission units:
             // at most one vertex block per kVertexBlock vertices plus one per
             // chunk, one index block per kIndexBlock indices plus one per
             // chunk, one whole chunk per chunk
             const size_t vc = out->vert_capacity, ic = out->ind_capacity;
-            const size_t units = vc / kVertexBlock + ic / kIndexBlock + 3 * (size_t)nc;
+            const size_t units = vc / kVertexBlock + ic / kIndexBlock + 3 * (size_t)nc * pm;
             const size_t sbytes = vc * 16 + ((ic * 4 + 15) & ~size_t(15)) + units * 8;
             if (!ctx->d_stage || ctx->stage_cap < sbytes) {
                 st = grow(&ctx->d_stage, &ctx->stage_cap, sbytes);
@@ -428,15 +507,17 @@ int prepare_batched(uww_ctx* ctx, uint32_t n, uint32_t max_cells, const uww_mesh
     return launch(ctx, nullptr, n, max_cells, out, true, nullptr, 0, nullptr, nullptr, true);
 }
 int plan_batched(uww_ctx* ctx, uint32_t n, uint32_t max_cells, int* threads, int* grid, size_t* dyn_smem,
-                 int* occupancy)
+                 int* occupancy, uint32_t* split, uint32_t* pmax)
 {
     LaunchCfg cfg;
-    const int st = plan_launch(ctx, n, max_cells, true, &cfg);
+    const int st = plan_launch(ctx, n, max_cells, true, &cfg, true, plans(ctx, nullptr, nullptr));
     if (st) return st;
     *threads = cfg.threads;
     *grid = cfg.grid;
     *dyn_smem = cfg.dyn_smem;
     *occupancy = cfg.occupancy;
+    if (split) *split = cfg.split ? 1u : 0u;
+    if (pmax) *pmax = cfg.split ? cfg.pmax : 1u;
     return UWW_OK;
 }
 }  // namespace uww
@@ -565,6 +646,7 @@ int uww_ctx_destroy(uww_ctx* ctx)
     cudaFree(ctx->d_tables);
     cudaFree(ctx->d_split);
     cudaFree(ctx->d_stage);
+    cudaFree(ctx->d_slab);
     cudaFree(ctx->d_state);
     cudaFree(ctx->d_totals);
     cudaFree(ctx->d_scratch);
@@ -711,7 +793,8 @@ int uww_build_chunks_host(uww_ctx* ctx, const uww_chunk_desc* h_chunks, uint32_t
     const bool words_ok = aligned_to(dv, 4) && aligned_to(dn, 4) && aligned_to(di, 4) && aligned_to(dr, 4);
     const bool mapped = dv && di && dr && (!want_normals || dn) && (!want_cases || dc) && (!want_samples || ds);
     LaunchCfg probe;
-    if (mapped && plan_launch(ctx, n, max_cells, true, &probe) == UWW_OK && probe.split) {
+    if (mapped && plan_launch(ctx, n, max_cells, true, &probe, true, plans(ctx, &d_out, nullptr)) == UWW_OK &&
+        probe.split) {
         // The split build.  Its emission kernel is the only one that writes
         // vertices, normals and indices, each once and in place: with host
         // buffers aligned for its stores (8 bytes for vertices) it stores
@@ -851,6 +934,23 @@ int uww_ctx_get_tuning(const uww_ctx* ctx, uww_tuning* t)
     t->test_flags = ctx->test_flags;
     t->options = ctx->options;
     t->reserved[0] = t->reserved[1] = 0;
+    return UWW_OK;
+}
+
+int uww_launch_shape_of(uww_ctx* ctx, uint32_t n, uint32_t max_cells, uww_launch_shape* out)
+{
+    if (!ctx || !out || n == 0 || max_cells < 1 || max_cells > UWW_MAX_CELLS) return UWW_ERR_INVALID_ARG;
+    int threads = 0, grid = 0, occ = 0;
+    size_t dyn = 0;
+    uint32_t split = 0, pmax = 1;
+    const int st = plan_batched(ctx, n, max_cells, &threads, &grid, &dyn, &occ, &split, &pmax);
+    if (st) return st;
+    out->build = split ? UWW_BUILD_SPLIT : UWW_BUILD_PIPELINED;
+    out->slabs_per_chunk = pmax;
+    out->threads = (uint32_t)threads;
+    out->grid = (uint32_t)grid;
+    out->blocks_per_sm = (uint32_t)(ctx->blocks_per_sm > 0 ? ctx->blocks_per_sm : occ);
+    out->dyn_smem = (uint32_t)dyn;
     return UWW_OK;
 }
 

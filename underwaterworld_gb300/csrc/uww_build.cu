@@ -64,8 +64,10 @@ constexpr unsigned long long kField22 = (1ull << 22) - 1;
 constexpr unsigned long long kInfoEarlyBlank = 1ull << 62;
 // a meshed chunk the staging buffers had no room for
 constexpr unsigned long long kUnstaged = ~0ull;
-// emission units: kind in bits 60-63, part in 32-59, chunk in 0-31
-constexpr uint32_t kUnitVerts = 0, kUnitInds = 1, kUnitChunk = 2;
+// emission units: kind in bits 60-62 (kUnitSlab: a slab of a large chunk,
+// the slab in bits 48-59 and the part in 32-47), else the part in 32-59;
+// the chunk in 0-31
+constexpr uint32_t kUnitVerts = 0, kUnitInds = 1, kUnitChunk = 2, kUnitSlab = 8;
 __device__ __forceinline__ unsigned long long unit_entry(uint32_t c, uint32_t part, uint32_t kind)
 {
     return (unsigned long long)c | ((unsigned long long)part << 32) | ((unsigned long long)kind << 60);
@@ -692,16 +694,18 @@ struct EdgeVertex {
     uint32_t edge_id;
 };
 
+// (rho holds the x planes from xo on: a slab's samples)
 template <class O>
 __device__ __forceinline__ EdgeVertex edge_vertex(const DevParams& p, const SmemTables& T, const float* rho, int S,
-                                                  int x, int y, int z, int e, float s, int ox, int oy, int oz)
+                                                  int x, int y, int z, int e, float s, int ox, int oy, int oz,
+                                                  int xo = 0)
 {
     const float iso = p.iso_level;
     const int ca = T.corners[e][0], cb = T.corners[e][1];
     const int ax = x + ((0x66 >> ca) & 1), ay = y + (ca >> 2), az = z + ((0xcc >> ca) & 1);
     const int bx = x + ((0x66 >> cb) & 1), by = y + (cb >> 2), bz = z + ((0xcc >> cb) & 1);
-    const float ia = rho[(ax * S + ay) * S + az];
-    const float ibv = rho[(bx * S + by) * S + bz];
+    const float ia = rho[((ax - xo) * S + ay) * S + az];
+    const float ibv = rho[((bx - xo) * S + by) * S + bz];
     const float sax = O::mul((float)ax, s), say = O::mul((float)ay, s), saz = O::mul((float)az, s);
     const float sbx = O::mul((float)bx, s), sby = O::mul((float)by, s), sbz = O::mul((float)bz, s);
     const float tt = O::div(O::sub(iso, ia), O::sub(ibv, ia));
@@ -1258,6 +1262,254 @@ __device__ __forceinline__ Workspace workspace_at(uint8_t* base, int N)
     return w;
 }
 
+// ---------------------------------------------------------------------------
+// Slabs of a large chunk (split build; layout and layer count: slab_layout).
+// Slab s of a chunk of N cells per edge holds the cell layers x0 = s * K ..
+// x1 - 1 and the sample planes x0 .. x1.  Its CTA's thread t owns a run of the
+// slab's cell columns (x, y) -- N cells each, in the chunk's cell order -- so
+// the slab's counts are one block scan.  A vertex is numbered by the cell that
+// owns its edge; an edge on the slab's low x face is owned by a cell of the
+// previous slab's last layer, which leaves per cell (y, z) its first vertex id
+// and case in its seam, and the emission resolves those references from it.
+
+struct SlabWs {
+    float* rho;                   // (x - x0, y, z) samples of the slab's planes
+    uint8_t* cases;               // per cell of the slab (active cells only)
+    uint16_t* vbase;              // per active cell: first vertex id within the slab
+    unsigned long long* masks;    // per sample column (x - x0, y): bits z with sample < iso
+    unsigned long long* prefix;   // per thread: its cells' exclusive count prefix
+};
+
+__device__ __forceinline__ SlabWs slab_ws(uint8_t* base, int N)
+{
+    const SlabLayout L = slab_layout(N);
+    SlabWs w;
+    w.rho = reinterpret_cast<float*>(base + L.rho);
+    w.cases = base + L.cases;
+    w.vbase = reinterpret_cast<uint16_t*>(base + L.vbase);
+    w.masks = reinterpret_cast<unsigned long long*>(base + L.masks);
+    w.prefix = reinterpret_cast<unsigned long long*>(base + L.prefix);
+    return w;
+}
+
+// whether chunk `cells` is built as slabs (the planning kernel and the
+// front kernel decide alike)
+__device__ __forceinline__ bool slab_chunk(const BuildArgs& a, uint32_t cells)
+{
+    return a.pmax > 1 && cells > a.piece_cells && cells <= a.max_cells && cells <= (uint32_t)kSlabMaxCells;
+}
+
+// A cell column (x, y) of a slab: its four corner columns' masks and its
+// active cells (bit z: the cell's corners are not all on one side)
+struct SlabColumn {
+    unsigned long long m00, m10, m01, m11, act;
+};
+
+__device__ __forceinline__ SlabColumn slab_column(const unsigned long long* masks, int S, int xl, int y, int N)
+{
+    const int col = xl * S + y;
+    SlabColumn c;
+    c.m00 = masks[col];
+    c.m10 = masks[col + S];
+    c.m01 = masks[col + 1];
+    c.m11 = masks[col + S + 1];
+    const unsigned long long an = c.m00 & c.m10 & c.m01 & c.m11, no = ~(c.m00 | c.m10 | c.m01 | c.m11);
+    const unsigned long long quiet = (an & (an >> 1)) | (no & (no >> 1));
+    c.act = ~quiet & ((1ull << N) - 1ull);
+    return c;
+}
+
+// packed counts of an active cell: new vertices | indices << kIndShift | 1 active
+__device__ __forceinline__ unsigned long long cell_counts(const SmemTables& T, int cs, unsigned own)
+{
+    return (unsigned long long)__popc(T.edges[cs] & own) | ((unsigned long long)(3 * T.ntri[cs]) << kIndShift) |
+           (1ull << kActShift);
+}
+
+// Front half of slab s of chunk c into workspace W: the noise of its planes
+// (fast build: the column form, which also leaves the columns' masks), the
+// early-blank and solid votes, the classification from the masks, the block
+// scan and each active cell's first vertex id; the last layer's ids and cases
+// to the seam when a slab follows (write_seam).  Returns the slab's packed
+// counts (every thread; 0 when no cell is crossed); *any_inside: a sample is
+// not above the iso level; *run: the thread's exclusive prefix.  Every thread
+// (kSlabThreads) must call it.  GWS: W is in global memory (this CTA's scratch).
+template <class O, bool GWS>
+__device__ unsigned long long slab_front(const DevParams& p, const BuildArgs& a, SmemTables& T, const SlabWs W,
+                                         uint8_t* ztab, const uww_chunk_desc d, uint32_t c, uint32_t s, int ncomp,
+                                         bool write_seam, int* any_inside_out, unsigned long long* run_out)
+{
+    const int tid = threadIdx.x;
+    const int oriented = p.dedup_mode == UWW_DEDUP_ORIENTED;
+    const int N = (int)d.cells, S = N + 1, K = slab_layers(N);
+    const int x0 = (int)s * K, x1 = min(x0 + K, N), nl = x1 - x0, planes = nl + 1;
+    const int ox = d.pos[0] * p.chunk_size, oy = d.pos[1] * p.chunk_size, oz = d.pos[2] * p.chunk_size;
+    const float iso = p.iso_level;
+    int inside = 0, outside = 0;
+    if constexpr (std::is_same<O, FastOps>::value) {
+        const ZTable zt = ztable_at(ztab, S, p.octaves);
+        const int io = sample_columns_fast<GWS>(p, T.perm, T.gp, zt, W.rho, N, ox, oy, oz, ncomp, W.masks, x0, planes);
+        inside = io & 1;
+        outside = io >> 1;
+    } else {
+        const float sc = __fdiv_rn((float)p.chunk_size, (float)N);
+        const int S2 = S * S;
+        for (int idx = tid; idx < planes * S2; idx += ncomp) {
+            const int xl = idx / S2, r = idx - xl * S2, y = r / S, z = r - y * S;
+            const float wx = O::add(O::mul((float)(x0 + xl), sc), (float)ox);
+            const float wy = O::add(O::mul((float)y, sc), (float)oy);
+            const float wz = O::add(O::mul((float)z, sc), (float)oz);
+            const float v = density<O, false>(p, T.perm, wx, wy, wz, nullptr);
+            W.rho[idx] = v;
+            inside |= !(v > iso);
+            outside |= !(v < iso);
+        }
+    }
+    const int any_inside = bar_or(kBarCompute, ncomp, inside);
+    const int solid = bar_and(kBarCompute, ncomp, !outside);
+    *any_inside_out = any_inside;
+    *run_out = 0ull;
+    if (!any_inside || solid) return 0ull;
+    if constexpr (!std::is_same<O, FastOps>::value) {
+        for (int col = tid; col < planes * S; col += ncomp) {
+            unsigned long long m = 0ull;
+            for (int z = 0; z < S; ++z) m |= (unsigned long long)(W.rho[col * S + z] < iso) << z;
+            W.masks[col] = m;
+        }
+        bar_sync(kBarCompute, ncomp);
+    }
+    // ---- classify + count: the thread's run of cell columns ----
+    const int ncol = nl * N, R = (ncol + ncomp - 1) / ncomp;
+    const int q0 = min(tid * R, ncol), q1 = min(q0 + R, ncol);
+    unsigned long long mine = 0ull;
+    for (int q = q0; q < q1; ++q) {
+        const int xl = q / N, y = q - xl * N, x = x0 + xl;
+        const SlabColumn col = slab_column(W.masks, S, xl, y, N);
+        const unsigned own_lo = (x == 0) | ((y == 0) << 1) | ((x == N - 1) << 3) | ((y == N - 1) << 4);
+        for (unsigned long long act = col.act; act; act &= act - 1ull) {
+            const int z = __ffsll((long long)act) - 1;
+            const int cs = mask_case(col.m00, col.m10, col.m01, col.m11, z);
+            W.cases[q * N + z] = (uint8_t)cs;
+            mine += cell_counts(T, cs, T.owned[oriented][own_lo | ((z == 0) << 2) | ((z == N - 1) << 5)]);
+        }
+    }
+    unsigned long long total = 0ull;
+    const unsigned long long run = block_exclusive_scan(mine, T, total, ncomp);
+    W.prefix[tid] = run;
+    *run_out = run;
+    // ---- each active cell's first vertex id; the seam ----
+    uint32_t* seam = write_seam && (int)s + 1 < slab_count(N) ? a.seam + ((size_t)c * a.pmax + s) * a.seam_stride
+                                                                 : nullptr;
+    unsigned long long r = run;
+    for (int q = q0; q < q1; ++q) {
+        const int xl = q / N, y = q - xl * N, x = x0 + xl;
+        const SlabColumn col = slab_column(W.masks, S, xl, y, N);
+        const unsigned own_lo = (x == 0) | ((y == 0) << 1) | ((x == N - 1) << 3) | ((y == N - 1) << 4);
+        for (unsigned long long act = col.act; act; act &= act - 1ull) {
+            const int z = __ffsll((long long)act) - 1;
+            const int cs = W.cases[q * N + z];
+            W.vbase[q * N + z] = (uint16_t)(r & kField22);
+            if (seam && x == x1 - 1) seam[y * N + z] = (uint32_t)(r & 0xffffu) | ((uint32_t)cs << 16);
+            r += cell_counts(T, cs, T.owned[oriented][own_lo | ((z == 0) << 2) | ((z == N - 1) << 5)]);
+        }
+    }
+    return total;
+}
+
+// A vertex of the previous slab, referenced from this one (staged index):
+// kCrossRef | owner edge << 24 | the owner cell's y * N + z.
+constexpr uint32_t kCrossRef = 0x80000000u;
+
+// The chunk-local id of the vertex on edge oe of cell (x0 - 1, qy, qz) of the
+// previous slab, from its seam (written by another kernel: read through L2);
+// prev_base: that slab's first vertex in the chunk.
+__device__ __forceinline__ uint32_t seam_vertex(const BuildArgs& a, const SmemTables& T, int oriented, int N,
+                                                const uint32_t* seam_prev, int x0, int qy, int qz, int oe,
+                                                uint32_t prev_base)
+{
+    const uint32_t w = __ldcg(seam_prev + qy * N + qz);
+    const unsigned oown = T.owned[oriented][boundary_flags(x0 - 1, qy, qz, N)];
+    return prev_base + (w & 0xffffu) + __popc(oown & __ldg(&UWW_EDGE_BEFORE[(w >> 16) & 255u][oe]));
+}
+
+// Pass 1 of a slab, from workspace W (this thread's run of cell columns,
+// prefix `run`): per active cell its triangles' indices and the positions of
+// the vertices it creates.  Staged (!FINAL): slab-local vertex ids (a vertex of
+// the previous slab as a kCrossRef word) at eo.inds + ioff, positions (with the
+// owner's corner b) at eo.pos + voff.  FINAL: chunk-local ids (vbase0: the
+// slab's first vertex in the chunk, prev_base: the previous slab's) into the
+// outputs at ioff and voff, colour slot 0 carrying corner b when pass 2
+// follows (carry).
+template <class O, bool FINAL>
+__device__ void slab_emit(const DevParams& p, const BuildArgs& a, const SmemTables& T, const SlabWs W,
+                          const uww_chunk_desc d, uint32_t c, uint32_t s, unsigned long long run, int ncomp,
+                          const EmitOut& eo, uint32_t voff, uint32_t ioff, uint32_t vbase0, uint32_t prev_base,
+                          bool carry)
+{
+    const int tid = threadIdx.x;
+    const int oriented = p.dedup_mode == UWW_DEDUP_ORIENTED;
+    const int N = (int)d.cells, S = N + 1, K = slab_layers(N);
+    const int x0 = (int)s * K, x1 = min(x0 + K, N), nl = x1 - x0;
+    const int ox = d.pos[0] * p.chunk_size, oy = d.pos[1] * p.chunk_size, oz = d.pos[2] * p.chunk_size;
+    const float sc = __fdiv_rn((float)p.chunk_size, (float)N);
+    const uint32_t* seam_prev = s > 0 ? a.seam + ((size_t)c * a.pmax + s - 1) * a.seam_stride : nullptr;
+    const int ncol = nl * N, R = (ncol + ncomp - 1) / ncomp;
+    const int q0 = min(tid * R, ncol), q1 = min(q0 + R, ncol);
+    unsigned long long r = run;
+    for (int q = q0; q < q1; ++q) {
+        const int xl = q / N, y = q - xl * N, x = x0 + xl;
+        const SlabColumn col = slab_column(W.masks, S, xl, y, N);
+        const unsigned own_lo = (x == 0) | ((y == 0) << 1) | ((x == N - 1) << 3) | ((y == N - 1) << 4);
+        for (unsigned long long act = col.act; act; act &= act - 1ull) {
+            const int z = __ffsll((long long)act) - 1;
+            const int cs = W.cases[q * N + z];
+            const unsigned own = T.owned[oriented][own_lo | ((z == 0) << 2) | ((z == N - 1) << 5)];
+            const int nt = T.ntri[cs];
+            const uint32_t vb = (uint32_t)(r & kField22), ir = (uint32_t)((r >> kIndShift) & kField22);
+            const int8_t* row = T.tri[cs];
+            const unsigned fr = T.first_ref[cs];
+            const uint16_t* before = UWW_EDGE_BEFORE[cs];
+            const int lo = (x == 0) | ((y == 0) << 1) | ((z == 0) << 2);
+            for (int i = 0; i < 3 * nt; ++i) {
+                const int e = row[i];
+                uint32_t id;
+                if ((own >> e) & 1u) {
+                    // the cell numbers its owned edges' vertices in first-reference order
+                    id = vb + __popc(own & __ldg(before + e));
+                    if ((fr >> i) & 1u) {
+                        const EdgeVertex ev = edge_vertex<O>(p, T, W.rho, S, x, y, z, e, sc, ox, oy, oz, x0);
+                        if (FINAL) {
+                            float2* v2 = reinterpret_cast<float2*>(eo.verts + voff + id);
+                            v2[0] = make_float2(ev.x, ev.y);
+                            v2[1] = make_float2(ev.z, carry ? (float)ev.cb : 0.f);
+                            v2[2] = make_float2(0.f, 0.f);
+                        } else {
+                            eo.pos[voff + id] = make_float4(ev.x, ev.y, ev.z, (float)ev.cb);
+                        }
+                    }
+                    if (FINAL) id += vbase0;
+                } else {
+                    // the owner: the first cell in stream order holding this edge
+                    const int ow = T.owner[oriented][lo][e];
+                    const int qx = x - ((ow >> 4) & 1), qy = y - ((ow >> 5) & 1), qz = z - ((ow >> 6) & 1);
+                    const int oe = ow & 15;
+                    if (qx < x0) {
+                        id = FINAL ? seam_vertex(a, T, oriented, N, seam_prev, x0, qy, qz, oe, prev_base)
+                                   : kCrossRef | ((uint32_t)oe << 24) | (uint32_t)(qy * N + qz);
+                    } else {
+                        const int oc = ((qx - x0) * N + qy) * N + qz;
+                        const unsigned oown = T.owned[oriented][boundary_flags(qx, qy, qz, N)];
+                        id = (uint32_t)W.vbase[oc] + __popc(oown & __ldg(&UWW_EDGE_BEFORE[W.cases[oc]][oe]));
+                        if (FINAL) id += vbase0;
+                    }
+                }
+                eo.inds[ioff + ir + i] = id;
+            }
+            r += cell_counts(T, cs, own);
+        }
+    }
+}
+
 // counts word of a chunk the depth bias decides (kind 1: every sample above
 // the iso level -- early blank; 2: every sample below it)
 __device__ __forceinline__ unsigned long long decided_info(int kind) { return kind == 1 ? kInfoEarlyBlank : 0ull; }
@@ -1278,10 +1530,21 @@ __global__ void __launch_bounds__(kPlanThreads) split_plan_kernel(const DevParam
             ok ? bias_decides_with(p, B, __fdiv_rn((float)p.chunk_size, (float)cells), (int)cells, oz, &rank) : 0;
         if (kind) {
             a.tinfo[i] = decided_info(kind);
+        } else if (ok && slab_chunk(a, cells)) {
+            // a chunk built as slabs: every slab queued (first, as the
+            // largest pieces of work); its counts word starts at zero counts
+            // and early blank, and each slab adds its counts and clears the
+            // flag when one of its samples is not above the iso level
+            const uint32_t np = (uint32_t)slab_count((int)cells), qcap = a.n * a.pmax;
+            a.tinfo[i] = kInfoEarlyBlank;
+            const uint32_t pos = atomicAdd(&a.split_ctr[kCtrQueued], np);
+            for (uint32_t sl = 0; sl < np; ++sl)
+                if (pos + sl < qcap) a.split_queue[pos + sl] = i | (sl << kPieceShift);
         } else {
-            // (the counters are zero at launch, so pos < n; checked all the same)
+            // (the counters are zero at launch, so pos < n * pmax; checked all the same)
+            const uint32_t qcap = a.n * a.pmax;
             const uint32_t pos = atomicAdd(&a.split_ctr[kCtrQueued + rank], 1u);
-            if (pos < a.n) a.split_queue[(size_t)rank * a.n + pos] = i;
+            if (pos < qcap) a.split_queue[(size_t)rank * qcap + pos] = i;
         }
     }
 }
@@ -1296,12 +1559,64 @@ __device__ __forceinline__ uint32_t split_take(const BuildArgs& a, uint32_t nchu
         const uint32_t k = atomicAdd(&a.split_ctr[kCtrTaken], 1u);
         return k < nchunks ? k : kNoChunk;
     }
+    const uint32_t qcap = a.n * a.pmax;
     while (rank < (uint32_t)kPlanRanks) {
         const uint32_t k = atomicAdd(&a.split_ctr[kCtrTaken + rank], 1u);
-        if (k < min(__ldcg(&a.split_ctr[kCtrQueued + rank]), a.n)) return __ldcg(&a.split_queue[(size_t)rank * a.n + k]);
+        if (k < min(__ldcg(&a.split_ctr[kCtrQueued + rank]), qcap)) return __ldcg(&a.split_queue[(size_t)rank * qcap + k]);
         ++rank;
     }
     return kNoChunk;
+}
+
+// The front kernel's work on slab s of chunk c: its front half in the shared
+// workspace, its counts to the chunk's counts word, its place's counts and the
+// chunk's tile sum, then (meshed) its staged pass 1 and its emission units --
+// or, when the staging buffers have no room, one unit for the emission kernel
+// to build the slab again and emit it in place.
+template <class O>
+__device__ void front_slab(const DevParams& p, const BuildArgs& a, SmemTables& T, uint8_t* dyn_smem,
+                           const uww_chunk_desc d, uint32_t c, uint32_t sl, unsigned long long& stage,
+                           uint32_t& unit_a, uint32_t& unit_b)
+{
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    const uint32_t place = c * a.pmax + sl;
+    const SlabWs W = slab_ws(dyn_smem, (int)d.cells);
+    int any_inside = 0;
+    unsigned long long run = 0ull;
+    const unsigned long long tot = slab_front<O, false>(p, a, T, W, dyn_smem + a.ztable_offset, d, c, sl, nthr, true,
+                                                        &any_inside, &run);
+    const uint32_t nV = (uint32_t)(tot & kField22), nI = (uint32_t)((tot >> kIndShift) & kField22);
+    const uint32_t vb = (nV + kVertexBlock - 1) / kVertexBlock, ib = (nI + kIndexBlock - 1) / kIndexBlock;
+    if (tid == 0) {
+        if (tot) atomicAdd(&a.tinfo[c], tot);
+        if (any_inside) atomicAnd(&a.tinfo[c], ~kInfoEarlyBlank);
+        a.pinfo[place] = (unsigned long long)nV | ((unsigned long long)nI << 32);
+        if (nV | nI) atomicAdd(&a.tile_sum[c / kTileChunks], (unsigned long long)nV | ((unsigned long long)nI << 32));
+        if (nI) {
+            const unsigned long long at =
+                atomicAdd(a.stage_ctr, (unsigned long long)nV | ((unsigned long long)nI << 32));
+            const unsigned long long sv = at & 0xffffffffull, si = at >> 32;
+            const bool room = sv + nV <= a.stage_vcap && si + nI <= a.stage_icap;
+            stage = room ? at : kUnstaged;
+            a.stage_at[place] = stage;
+            unit_a = atomicAdd(&a.split_ctr[kCtrUnitsA], room ? vb : 1u);
+            unit_b = room ? atomicAdd(&a.split_ctr[kCtrUnitsB], ib) : 0u;
+        }
+    }
+    __syncthreads();
+    if (!nI) return;
+    const unsigned long long st = stage;
+    if (st != kUnstaged) {
+        const EmitOut eo{nullptr, a.stage_inds, nullptr, a.stage_pos};
+        slab_emit<O, false>(p, a, T, W, d, c, sl, run, nthr, eo, (uint32_t)st, (uint32_t)(st >> 32), 0u, 0u, true);
+        for (uint32_t k = tid; k < vb; k += nthr)
+            if (unit_a + k < a.unit_cap) a.units[unit_a + k] = unit_entry(c, k | (sl << 16), kUnitVerts | kUnitSlab);
+        for (uint32_t k = tid; k < ib; k += nthr)
+            if (unit_b + k < a.unit_cap)
+                a.units[a.unit_cap - 1 - (unit_b + k)] = unit_entry(c, k | (sl << 16), kUnitInds | kUnitSlab);
+    } else if (tid == 0 && unit_a < a.unit_cap) {
+        a.units[unit_a] = unit_entry(c, sl << 16, kUnitChunk | kUnitSlab);
+    }
 }
 
 template <class O, int MAXT, int MINB>
@@ -1329,13 +1644,24 @@ __global__ void __launch_bounds__(MAXT, MINB) front_kernel(const DevParams p, co
     __syncthreads();
     for (;;) {
         if (tid == 0) {
-            const uint32_t c = split_take(a, T.nchunks, rank);
+            const uint32_t e = split_take(a, T.nchunks, rank);
+            // a queue entry of a batch with slabs: chunk | slab << kPieceShift
+            const uint32_t c = (e == kNoChunk || a.pmax == 1) ? e : (e & ((1u << kPieceShift) - 1u));
             T.tk[0].chunk = c;
+            T.tk[0].ticket = (e == kNoChunk || a.pmax == 1) ? 0u : e >> kPieceShift;
             if (c != kNoChunk) T.tk[0].desc = a.chunks[c];
         }
         __syncthreads();
         const uint32_t c = T.tk[0].chunk;
         if (c == kNoChunk) break;
+        if constexpr (MAXT == kSlabThreads) {
+            if (slab_chunk(a, T.tk[0].desc.cells)) {
+                front_slab<O>(p, a, T, dyn_smem, T.tk[0].desc, c, T.tk[0].ticket, stage, unit_a, unit_b);
+                __syncthreads();  // the workspace and the staged ticket are reused
+                continue;
+            }
+        }
+        const uint32_t place = c * a.pmax;
         chunk_front<O, false>(p, a, T, dyn_smem, T.tk[0].desc, c, c, 0, nthr);
         __syncthreads();
         const ChunkInfo ci = T.ci[0];
@@ -1355,7 +1681,7 @@ __global__ void __launch_bounds__(MAXT, MINB) front_kernel(const DevParams p, co
                 const unsigned long long sv = at & 0xffffffffull, si = at >> 32;
                 const bool room = sv + nV <= a.stage_vcap && si + nI <= a.stage_icap;
                 stage = room ? at : kUnstaged;
-                a.stage_at[c] = stage;
+                a.stage_at[place] = stage;
                 unit_a = atomicAdd(&a.split_ctr[kCtrUnitsA], room ? vb : 1u);
                 unit_b = room ? atomicAdd(&a.split_ctr[kCtrUnitsB], ib) : 0u;
             }
@@ -1429,6 +1755,35 @@ __device__ __forceinline__ uww_chunk_record load_record(const uww_chunk_record* 
     *reinterpret_cast<uint4*>(&rec) = __ldcg(r4);
     *(reinterpret_cast<uint4*>(&rec) + 1) = __ldcg(r4 + 1);
     return rec;
+}
+
+// The emission kernel's work on a slab the staging buffers had no room for:
+// its front half again in this CTA's global scratch (the seam is the front
+// kernel's), then pass 1 into the outputs at voff (its first vertex, chunk
+// id vbase0; the previous slab's first vertex prev_base) and ioff, and pass 2
+// over its nv vertices.  Kept out of line: the emission's other units do not
+// pay for its registers.
+template <class O>
+__device__ __noinline__ void emit_slab_again(const DevParams& p, const BuildArgs& a, SmemTables& T, uint8_t* dyn_smem,
+                                             uint32_t c, uint32_t sl, uint32_t voff, uint32_t ioff, uint32_t vbase0,
+                                             uint32_t prev_base, uint32_t nv)
+{
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    const bool want_color = (p.outputs & UWW_OUT_COLOR) != 0;
+    const bool want_normals = (p.outputs & UWW_OUT_NORMALS) != 0 && a.normals != nullptr;
+    const uww_chunk_desc d = a.chunks[c];
+    const SlabWs W = slab_ws(a.scratch + (size_t)blockIdx.x * a.scratch_slot_bytes, (int)d.cells);
+    int any_inside = 0;
+    unsigned long long run = 0ull;
+    slab_front<O, true>(p, a, T, W, dyn_smem, d, c, sl, nthr, false, &any_inside, &run);
+    __syncthreads();
+    const EmitOut eo{a.verts, a.inds, nullptr, nullptr};
+    slab_emit<O, true>(p, a, T, W, d, c, sl, run, nthr, eo, voff, ioff, vbase0, prev_base, want_color || want_normals);
+    if (want_color || want_normals) {
+        __syncthreads();  // the slab's vertex positions, written by this CTA
+        for (uint32_t v = tid; v < nv; v += nthr)
+            finish_vertex<O>(p, T.perm, T.gp, a.verts, a.normals, voff + v, want_color, want_normals);
+    }
 }
 
 template <class O>
@@ -1559,9 +1914,31 @@ __global__ void __launch_bounds__(256, 4) emit_kernel(const DevParams p, const B
     uint32_t t = blockIdx.x;
     while (t < nunits) {
         const unsigned long long ent = t < na ? __ldcg(&a.units[t]) : __ldcg(&a.units[a.unit_cap - 1 - (t - na)]);
-        const uint32_t c = (uint32_t)ent, part = (uint32_t)(ent >> 32) & 0x0fffffffu, kind = (uint32_t)(ent >> 60);
+        const uint32_t c = (uint32_t)ent, kind = (uint32_t)(ent >> 60) & 7u;
+        const bool slab = (ent >> 63) != 0ull;
+        uint32_t part = (uint32_t)(ent >> 32) & 0x0fffffffu, sl = 0;
+        if (slab) {
+            sl = part >> 16;
+            part &= 0xffffu;
+        }
+        const uint32_t place = c * a.pmax + sl;
         const unsigned long long w = __ldcg(&a.tinfo[c]);
-        const uint32_t cnV = (uint32_t)(w & kField22), cnI = (uint32_t)((w >> kIndShift) & kField22);
+        // a slab's own counts, where it starts in its chunk (bv, bi) and
+        // where the slab before it starts (pv): sums over the slabs before
+        uint32_t cnV = (uint32_t)(w & kField22), cnI = (uint32_t)((w >> kIndShift) & kField22);
+        uint32_t bv = 0, bi = 0, pv = 0;
+        if (slab) {
+            const unsigned long long* pi = a.pinfo + (size_t)c * a.pmax;
+            for (uint32_t j = 0; j < sl; ++j) {
+                const unsigned long long x = __ldcg(pi + j);
+                pv = bv;
+                bv += (uint32_t)x;
+                bi += (uint32_t)(x >> 32);
+            }
+            const unsigned long long own = __ldcg(pi + sl);
+            cnV = (uint32_t)own;
+            cnI = (uint32_t)(own >> 32);
+        }
         __syncthreads();  // every thread has read the previous next_ticket
         if (tid == 0) next_ticket = gridDim.x + atomicAdd(&a.split_ctr[kCtrUnitsTaken], 1u);
         {
@@ -1575,7 +1952,7 @@ __global__ void __launch_bounds__(256, 4) emit_kernel(const DevParams p, const B
                 const uint32_t nv = cnV > v0 ? min(kVertexBlock, cnV - v0) : 0u;
                 float* sw = reinterpret_cast<float*>(dyn_smem);  // 6 words a vertex, then 3 a normal
                 if (tid < (int)nv) {
-                    const uint32_t sv = (uint32_t)__ldcg(&a.stage_at[c]);
+                    const uint32_t sv = (uint32_t)__ldcg(&a.stage_at[place]);
                     const float4 q = __ldcg(a.stage_pos + sv + v);
                     float2 out[3];
                     float g[3];
@@ -1590,16 +1967,16 @@ __global__ void __launch_bounds__(256, 4) emit_kernel(const DevParams p, const B
                 __syncthreads();  // the block is gathered
                 const uww_chunk_record rec = load_record(&a.records[c]);
                 if (ok && !(rec.flags & UWW_CHUNK_OVERFLOW)) {
-                    float* dv = reinterpret_cast<float*>(a.verts + rec.vert_offset + v0);
+                    float* dv = reinterpret_cast<float*>(a.verts + rec.vert_offset + bv + v0);
                     for (uint32_t k = tid; k < 6 * nv; k += nthr) dv[k] = sw[k];
                     if (want_normals) {
-                        float* dn = a.normals + 3 * (size_t)(rec.vert_offset + v0);
+                        float* dn = a.normals + 3 * (size_t)(rec.vert_offset + bv + v0);
                         for (uint32_t k = tid; k < 3 * nv; k += nthr) dn[k] = sw[6 * kVertexBlock + k];
                     }
                 }
             } else if (kind == kUnitInds) {
                 // a block of the chunk's indices (loaded), then to their place
-                const uint32_t si = (uint32_t)(__ldcg(&a.stage_at[c]) >> 32);
+                const uint32_t si = (uint32_t)(__ldcg(&a.stage_at[place]) >> 32);
                 const uint32_t k0 = part * kIndexBlock, k1 = min(k0 + kIndexBlock, cnI);
                 const uint32_t* src = a.stage_inds + si;
                 uint32_t iw[kIndexBlock / 256];
@@ -1608,16 +1985,43 @@ __global__ void __launch_bounds__(256, 4) emit_kernel(const DevParams p, const B
                     const uint32_t k = k0 + (uint32_t)r * 256u + tid;
                     iw[r] = k < k1 ? __ldcg(src + k) : 0u;
                 }
+                if (slab) {
+                    // slab-local ids to chunk-local; a vertex of the previous
+                    // slab from that slab's seam
+                    const int N = (int)__ldg(&a.chunks[c].cells);
+                    const int oriented = p.dedup_mode == UWW_DEDUP_ORIENTED;
+                    const int x0 = (int)sl * slab_layers(N);
+                    const uint32_t* seam_prev =
+                        sl > 0 ? a.seam + ((size_t)c * a.pmax + sl - 1) * a.seam_stride : nullptr;
+#pragma unroll
+                    for (int r = 0; r < (int)(kIndexBlock / 256); ++r) {
+                        const uint32_t v = iw[r];
+                        if ((v & kCrossRef) && seam_prev) {
+                            const int qyz = (int)(v & 0xffffffu) % (N * N);
+                            iw[r] = seam_vertex(a, T, oriented, N, seam_prev, x0, qyz / N, qyz % N,
+                                                (int)((v >> 24) & 15u), pv);
+                        } else {
+                            iw[r] = v + bv;
+                        }
+                    }
+                }
                 const bool ok = await_records();
                 const uww_chunk_record rec = load_record(&a.records[c]);
                 if (ok && !(rec.flags & UWW_CHUNK_OVERFLOW)) {
-                    uint32_t* dst = a.inds + rec.ind_offset;
+                    uint32_t* dst = a.inds + rec.ind_offset + bi;
 #pragma unroll
                     for (int r = 0; r < (int)(kIndexBlock / 256); ++r) {
                         const uint32_t k = k0 + (uint32_t)r * 256u + tid;
                         if (k < k1) dst[k] = iw[r];
                     }
                 }
+            } else if (slab) {
+                // a slab without staging room: built again in this CTA's
+                // scratch, then passes 1 and 2 in place
+                if (!await_records()) goto unit_done;
+                const uww_chunk_record rec = load_record(&a.records[c]);
+                if (rec.flags & UWW_CHUNK_OVERFLOW) goto unit_done;
+                emit_slab_again<O>(p, a, T, dyn_smem, c, sl, rec.vert_offset + bv, rec.ind_offset + bi, bv, pv, cnV);
             } else {
                 // a chunk without staging room: pass 1 and pass 2 from its slot
                 if (!await_records()) goto unit_done;
@@ -1801,6 +2205,23 @@ cudaError_t front_occupancy(bool exact, int threads, size_t dyn_smem, int* block
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, front_for(exact, threads), threads, dyn_smem);
 }
 
+cudaError_t split_emit_shape(const DevParams& p, const BuildArgs& a, int* grid, size_t* dyn_smem)
+{
+    int dev = 0, sms = 0, ebps = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    // dynamic shared memory: a chunk's workspace (chunks without staging
+    // room), a gathered vertex block (9 words a vertex) or the z tables of a
+    // slab built again, the largest
+    size_t edyn = std::max(a.slot_bytes, (size_t)kVertexBlock * 9 * sizeof(float));
+    if (a.pmax > 1) edyn = std::max(edyn, ztable_bytes((int)a.max_cells + 1, (int)p.octaves));
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ebps, emit_for(p.math_mode == UWW_MATH_EXACT), 256, edyn);
+    if (e != cudaSuccess) return e;
+    *grid = std::max(1, sms * std::max(1, ebps));
+    *dyn_smem = edyn;
+    return cudaSuccess;
+}
+
 cudaError_t launch_build(const DevParams& p, const BuildArgs& a, bool queue, int grid, int threads, size_t dyn_smem,
                          cudaStream_t s)
 {
@@ -1829,23 +2250,17 @@ cudaError_t launch_build(const DevParams& p, const BuildArgs& a, bool queue, int
         cudaLaunchAttribute pdl[1];
         pdl[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
         pdl[0].val.programmaticStreamSerializationAllowed = 1;
-        int dev = 0, sms = 0, ebps = 0;
-        const FrontFn efn = emit_for(exact);
-        e = cudaGetDevice(&dev);
-        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        // dynamic shared memory: a chunk's workspace (chunks without staging
-        // room) or a gathered vertex block (9 words a vertex), the larger
-        const size_t edyn = std::max(a.slot_bytes, (size_t)kVertexBlock * 9 * sizeof(float));
-        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ebps, efn, 256, edyn);
-        if (e != cudaSuccess) return e;
+        int egrid = 0;
+        size_t edyn = 0;
+        if ((e = split_emit_shape(p, a, &egrid, &edyn)) != cudaSuccess) return e;
         cudaLaunchConfig_t ecfg = {};
-        ecfg.gridDim = dim3((unsigned)std::max(1, sms * std::max(1, ebps)));
+        ecfg.gridDim = dim3((unsigned)egrid);
         ecfg.blockDim = dim3(256);
         ecfg.dynamicSmemBytes = edyn;
         ecfg.stream = s;
         ecfg.attrs = pdl;
         ecfg.numAttrs = 1;
-        return cudaLaunchKernelEx(&ecfg, efn, p, a);
+        return cudaLaunchKernelEx(&ecfg, emit_for(exact), p, a);
     } else if (queue && a.plan) {
         // the planning kernel, then the build as its programmatic dependent
         const uint32_t nblk = std::max(1u, std::min((a.n + kPlanThreads - 1) / kPlanThreads, 1024u));

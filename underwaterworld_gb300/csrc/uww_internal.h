@@ -42,6 +42,60 @@ __host__ __device__ inline ChunkLayout chunk_layout(int N)
     return L;
 }
 
+// Split build, chunks above 16 cells per edge (the 24^3 and 48^3 LODs): each is
+// built as slabs of K consecutive x layers of cells -- contiguous in the
+// chunk's cell order (x, y, z), so a chunk's output is its slabs' outputs in
+// slab order -- one CTA of kSlabThreads threads per slab.  A slab's shared
+// workspace: the samples of its K+1 x planes, per sample column its
+// below-iso bits, per cell its case and (active cells) its first vertex id
+// within the slab, and per thread its cells' exclusive count prefix.  K is
+// the largest layer count whose sample columns ((K+1) * S) fit one pass of the
+// CTA's threads, whose workspace fits kSlabBudget bytes, and whose vertices fit
+// 16-bit ids (every edge of the slab's cells, counted once).
+constexpr int kSlabThreads = 256;
+constexpr uint32_t kSlabBudget = 80 * 1024;
+constexpr int kSlabMaxCells = 63;     // a sample column's bits fit one 64-bit mask
+constexpr uint32_t kPieceShift = 24;  // queue entry: chunk | slab << kPieceShift
+
+struct SlabLayout {
+    uint32_t rho, cases, vbase, masks, prefix, total;
+    int K;
+};
+
+__host__ __device__ inline SlabLayout slab_layout_k(int N, int K)
+{
+    const uint32_t S = (uint32_t)N + 1, NC = (uint32_t)K * N * N;
+    SlabLayout L;
+    L.K = K;
+    uint32_t o = 0;
+    L.rho = o;    o = align16(o + (uint32_t)(K + 1) * S * S * 4u);
+    L.cases = o;  o = align16(o + NC);
+    L.vbase = o;  o = align16(o + NC * 2u);
+    L.masks = o;  o = align16(o + (uint32_t)(K + 1) * S * 8u);
+    L.prefix = o; o = align16(o + (uint32_t)kSlabThreads * 8u);
+    L.total = o;
+    return L;
+}
+
+__host__ __device__ inline int slab_layers(int N)
+{
+    const int S = N + 1;
+    int K = kSlabThreads / S - 1;
+    if (K > N) K = N;
+    for (; K > 1; --K) {
+        const long long edges = (long long)K * S * S + 2ll * (K + 1) * N * S;
+        if (slab_layout_k(N, K).total <= kSlabBudget && edges < 65536) break;
+    }
+    return K < 1 ? 1 : K;
+}
+
+__host__ __device__ inline SlabLayout slab_layout(int N) { return slab_layout_k(N, slab_layers(N)); }
+__host__ __device__ inline int slab_count(int N)
+{
+    const int K = slab_layers(N);
+    return (N + K - 1) / K;
+}
+
 // Bytes of the fast build's per-chunk z tables for S samples per edge:
 // (dz, fade) and (first z, cell) per octave and z, run counts, z bias, run
 // start masks.
@@ -135,11 +189,23 @@ struct BuildArgs {
     unsigned long long* stage_ctr;   // the staging fill (counter block word kCtrStage)
     unsigned long long* units;       // emission units (unit_entry): list A from the front, list B from the back
     uint32_t unit_cap;
-    uint32_t* split_queue;           // planned: kPlanRanks work queues of n entries
+    uint32_t* split_queue;           // planned: kPlanRanks work queues of n * pmax entries
     uint32_t* split_ctr;             // kCtrWords counters, zero at launch (kCtr*)
     uint32_t split_planned;          // the planning kernel runs first and fills the queues
     uint32_t mask_offset;            // nonzero: per-column below-iso masks at dyn smem + mask_offset
     const uint2* tables;             // optional: the marching-cubes table image (table_image_kernel)
+    // Slabs (chunks above piece_cells cells per edge, planned split build
+    // only): a chunk has pmax piece places p = c * pmax + s.  Per place its
+    // counts (pinfo: verts | inds << 32), its staging place (stage_at[p]),
+    // its slot (slots + p * slot_bytes) and the seam it leaves its successor
+    // (seam + p * seam_stride words: per cell (y, z) of its last layer, the
+    // cell's first vertex id within the slab | case << 16).  pmax == 1: no
+    // slabs; every place is a chunk.
+    uint32_t pmax;
+    uint32_t piece_cells;
+    unsigned long long* pinfo;
+    uint32_t* seam;
+    uint32_t seam_stride;
     // Optional streamed host output (batched form): device addresses of
     // page-locked host memory.  Pass 2 then runs inside the build kernel, and
     // each chunk's record, indices, vertices and normals go there as soon as
@@ -187,6 +253,8 @@ cudaError_t build_occupancy(bool queue, bool exact, int threads, size_t dyn_smem
 // the split build's front kernel: resident CTAs per SM for this shape
 cudaError_t front_occupancy(bool exact, int threads, size_t dyn_smem, int* blocks_per_sm);
 cudaError_t prepare_build_kernels(size_t optin, size_t* max_dyn_smem);
+// the split build's emission kernel: its grid and dynamic shared memory
+cudaError_t split_emit_shape(const DevParams& p, const BuildArgs& a, int* grid, size_t* dyn_smem);
 cudaError_t launch_density(const DevParams& p, const float* xyz, uint32_t n, float* out, cudaStream_t s);
 
 // Batched build on the context (uww_api.cu); edge_ids and n_dev as in BuildArgs.
@@ -199,7 +267,7 @@ int prepare_batched(uww_ctx* ctx, uint32_t n, uint32_t max_cells, const uww_mesh
 // the launch shape a batched build of n chunks would use
 // and the resident CTAs per SM of its (front) kernel
 int plan_batched(uww_ctx* ctx, uint32_t n, uint32_t max_cells, int* threads, int* grid, size_t* dyn_smem,
-                 int* occupancy);
+                 int* occupancy, uint32_t* split = nullptr, uint32_t* pmax = nullptr);
 // (re)allocate *ptr to at least `bytes` of device memory (contents not kept)
 int ensure_device_bytes(void** ptr, size_t* cap, size_t bytes);
 // The build writes vertex positions and the totals with 8-byte stores and
@@ -248,6 +316,8 @@ struct uww_ctx {
     void* d_tables = nullptr;     // the marching-cubes table image (launch_table_image)
     uint8_t* d_split = nullptr;   // split build: counters, tile sums, counts, queues, slots
     uint8_t* d_stage = nullptr;   // split build: staging buffers and emission units
+    uint8_t* d_slab = nullptr;    // split build with slabs: per place its counts, then its seam
+    size_t slab_cap = 0;
     size_t stage_cap = 0;
     size_t split_cap = 0;
     uint32_t split_n = 0;         // the chunk count its layout is made for

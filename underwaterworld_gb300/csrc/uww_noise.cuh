@@ -369,16 +369,19 @@ __device__ __forceinline__ int sample_columns_reg(const DevParams& p, const uint
 // COLBUF: accumulate each column in a per-thread buffer (local memory, L1)
 // and write it to rho once, for rho in global memory where an accumulate per
 // sample and octave would be an L2 round trip each.
-// masks (optional, COLBUF, at most 64 samples per column): per column the
-// bits z with sample < iso level -- the columns' corner bits of every cell
-// case, so the classification of a chunk in global scratch reads no samples.
+// masks (optional, at most 64 samples per column): per column the bits z
+// with sample < iso level -- the columns' corner bits of every cell case, so
+// the classification reads no samples.
+// xlo, planes: the x planes xlo .. xlo + planes - 1 only (a slab of the
+// chunk; rho and masks then hold those planes' columns); planes < 0: all.
 template <bool COLBUF = false>
 __device__ __forceinline__ int sample_columns_fast(const DevParams& p, const uint8_t* __restrict__ P,
                                                    const float4* __restrict__ gp, const ZTable Z,
                                                    float* __restrict__ rho, int N, int ox, int oy, int oz,
-                                                   int ncomp, unsigned long long* masks = nullptr)
+                                                   int ncomp, unsigned long long* masks = nullptr, int xlo = 0,
+                                                   int planes = -1)
 {
-    const int S = N + 1, SS = S * S, K = p.octaves;
+    const int S = N + 1, SS = (planes < 0 ? S : planes) * S, K = p.octaves;
     const float s = __fdiv_rn((float)p.chunk_size, (float)N);
     const float bf = p.base_freq;
     const float norm = fbm_norm(p);
@@ -411,8 +414,9 @@ __device__ __forceinline__ int sample_columns_fast(const DevParams& p, const uin
 
     int inside = 0, outside = 0;
     for (int col = threadIdx.x; col < SS; col += ncomp) {
-        const int x = col / S, y = col - x * S;
+        const int x = xlo + col / S, y = col - (col / S) * S;
         float colbuf[COLBUF ? UWW_MAX_CELLS + 1 : 1];
+        unsigned long long below = 0ull;
         float* out = COLBUF ? colbuf : rho + col * S;
         const float nx = column_coord((float)x, s, ox, p.offset[0], bf);
         const float ny = column_coord((float)y, s, oy, p.offset[1], bf);
@@ -445,6 +449,7 @@ __device__ __forceinline__ int sample_columns_fast(const DevParams& p, const uin
                     if (last) {
                         inside |= !(r0 > iso);
                         outside |= !(r0 < iso);  // a case bit stays clear
+                        if (!COLBUF) below |= (unsigned long long)(r0 < iso) << (z & 63);
                     }
                 }
             }
@@ -457,6 +462,8 @@ __device__ __forceinline__ int sample_columns_fast(const DevParams& p, const uin
                 m |= (unsigned long long)(colbuf[z] < iso) << (z & 63);
             }
             if (masks) masks[col] = m;
+        } else if (masks) {
+            masks[col] = below;
         }
     }
     return inside | (outside << 1);

@@ -92,6 +92,15 @@ UWW_TUNE_NO_DEPTH_SHORTCUT = 1
 UWW_TUNE_PIPELINED = 2
 
 
+class LaunchShape(C.Structure):
+    _fields_ = [("build", C.c_uint32), ("slabs_per_chunk", C.c_uint32), ("threads", C.c_uint32),
+                ("grid", C.c_uint32), ("blocks_per_sm", C.c_uint32), ("dyn_smem", C.c_uint32)]
+
+
+UWW_BUILD_PIPELINED = 0
+UWW_BUILD_SPLIT = 1
+
+
 assert C.sizeof(ChunkDesc) == 32 and C.sizeof(ChunkRecord) == 32 and C.sizeof(Tuning) == 32
 
 CHUNK_DESC_DTYPE = np.dtype([("pos", "<i4", 3), ("cells", "<u4"), ("cell_offset", "<u4"),
