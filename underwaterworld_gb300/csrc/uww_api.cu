@@ -204,7 +204,7 @@ int plan_launch(uww_ctx* ctx, uint32_t n, uint32_t max_cells, bool queue, Launch
             cfg->threads = kSlabThreads;
             cfg->scratch_slot = 0;
             const bool exact = ctx->dev.math_mode == UWW_MATH_EXACT;
-            cudaError_t e = front_occupancy(exact, cfg->threads, cfg->dyn_smem, &cfg->occupancy);
+            cudaError_t e = front_occupancy(exact, cfg->threads, cfg->dyn_smem, &cfg->occupancy, true);
             if (e != cudaSuccess) return cuda_status(e);
             const int bps = ctx->blocks_per_sm > 0 ? ctx->blocks_per_sm : cfg->occupancy;
             if (bps < 1) return UWW_ERR_INVALID_ARG;

@@ -1277,7 +1277,6 @@ struct SlabWs {
     uint8_t* cases;               // per cell of the slab (active cells only)
     uint16_t* vbase;              // per active cell: first vertex id within the slab
     unsigned long long* masks;    // per sample column (x - x0, y): bits z with sample < iso
-    unsigned long long* prefix;   // per thread: its cells' exclusive count prefix
 };
 
 __device__ __forceinline__ SlabWs slab_ws(uint8_t* base, int N)
@@ -1288,7 +1287,6 @@ __device__ __forceinline__ SlabWs slab_ws(uint8_t* base, int N)
     w.cases = base + L.cases;
     w.vbase = reinterpret_cast<uint16_t*>(base + L.vbase);
     w.masks = reinterpret_cast<unsigned long long*>(base + L.masks);
-    w.prefix = reinterpret_cast<unsigned long long*>(base + L.prefix);
     return w;
 }
 
@@ -1347,6 +1345,8 @@ __device__ unsigned long long slab_front(const DevParams& p, const BuildArgs& a,
     const float iso = p.iso_level;
     int inside = 0, outside = 0;
     if constexpr (std::is_same<O, FastOps>::value) {
+        // (columns of 25 and 49 samples accumulated in registers were no
+        // faster, 49 much slower: the unrolled column outgrows the caches)
         const ZTable zt = ztable_at(ztab, S, p.octaves);
         const int io = sample_columns_fast<GWS>(p, T.perm, T.gp, zt, W.rho, N, ox, oy, oz, ncomp, W.masks, x0, planes);
         inside = io & 1;
@@ -1395,7 +1395,6 @@ __device__ unsigned long long slab_front(const DevParams& p, const BuildArgs& a,
     }
     unsigned long long total = 0ull;
     const unsigned long long run = block_exclusive_scan(mine, T, total, ncomp);
-    W.prefix[tid] = run;
     *run_out = run;
     // ---- each active cell's first vertex id; the seam ----
     uint32_t* seam = write_seam && (int)s + 1 < slab_count(N) ? a.seam + ((size_t)c * a.pmax + s) * a.seam_stride
@@ -1654,7 +1653,7 @@ __global__ void __launch_bounds__(MAXT, MINB) front_kernel(const DevParams p, co
         __syncthreads();
         const uint32_t c = T.tk[0].chunk;
         if (c == kNoChunk) break;
-        if constexpr (MAXT == kSlabThreads) {
+        if constexpr (MAXT == kSlabThreads && MINB == 2) {
             if (slab_chunk(a, T.tk[0].desc.cells)) {
                 front_slab<O>(p, a, T, dyn_smem, T.tk[0].desc, c, T.tk[0].ticket, stage, unit_a, unit_b);
                 __syncthreads();  // the workspace and the staged ticket are reused
@@ -2172,9 +2171,12 @@ using FrontFn = void (*)(const DevParams, const BuildArgs);
 // The split build's emission kernel.
 FrontFn emit_for(bool exact) { return exact ? emit_kernel<ExactOps> : emit_kernel<FastOps>; }
 
-// The split build's front kernel for a CTA of `threads` (<= 256) threads.
-FrontFn front_for(bool exact, int threads)
+// The split build's front kernel for a CTA of `threads` (<= 256) threads;
+// batches with slabs (whose workspaces leave room for two CTAs per SM) take
+// the instance with 128 registers a thread.
+FrontFn front_for(bool exact, int threads, bool slabs)
 {
+    if (slabs) return exact ? front_kernel<ExactOps, 256, 2> : front_kernel<FastOps, 256, 2>;
     if (threads <= 192) return exact ? front_kernel<ExactOps, 192, 4> : front_kernel<FastOps, 192, 4>;
     return exact ? front_kernel<ExactOps, 256, 3> : front_kernel<FastOps, 256, 3>;
 }
@@ -2187,7 +2189,8 @@ cudaError_t prepare_build_kernels(size_t optin, size_t* max_dyn_smem)
     for (int e = 0; e < 2; ++e) {
         for (int q = 0; q < 2; ++q)
             for (int l = 0; l < 2; ++l) m = std::min(m, set_smem_attr(kernel_for(e, q, l), optin));
-        for (int th : {192, 256}) m = std::min(m, set_smem_attr(front_for(e, th), optin));
+        for (int th : {192, 256}) m = std::min(m, set_smem_attr(front_for(e, th, false), optin));
+        m = std::min(m, set_smem_attr(front_for(e, 256, true), optin));
         m = std::min(m, set_smem_attr(emit_for(e), optin));
     }
     *max_dyn_smem = m;
@@ -2200,9 +2203,10 @@ cudaError_t build_occupancy(bool queue, bool exact, int threads, size_t dyn_smem
                                                          threads, dyn_smem);
 }
 
-cudaError_t front_occupancy(bool exact, int threads, size_t dyn_smem, int* blocks_per_sm)
+cudaError_t front_occupancy(bool exact, int threads, size_t dyn_smem, int* blocks_per_sm, bool slabs)
 {
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, front_for(exact, threads), threads, dyn_smem);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, front_for(exact, threads, slabs), threads,
+                                                         dyn_smem);
 }
 
 cudaError_t split_emit_shape(const DevParams& p, const BuildArgs& a, int* grid, size_t* dyn_smem)
@@ -2244,7 +2248,7 @@ cudaError_t launch_build(const DevParams& p, const BuildArgs& a, bool queue, int
         attr[0].val.programmaticStreamSerializationAllowed = 1;
         cfg.attrs = attr;
         cfg.numAttrs = a.split_planned ? 1 : 0;
-        if ((e = cudaLaunchKernelEx(&cfg, front_for(exact, threads), p, a)) != cudaSuccess) return e;
+        if ((e = cudaLaunchKernelEx(&cfg, front_for(exact, threads, a.pmax > 1), p, a)) != cudaSuccess) return e;
         // the emission (with the records) as the front kernel's programmatic
         // dependent: its CTAs load their tables as front CTAs finish
         cudaLaunchAttribute pdl[1];

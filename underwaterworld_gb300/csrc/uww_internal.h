@@ -48,7 +48,7 @@ __host__ __device__ inline ChunkLayout chunk_layout(int N)
 // slab order -- one CTA of kSlabThreads threads per slab.  A slab's shared
 // workspace: the samples of its K+1 x planes, per sample column its
 // below-iso bits, per cell its case and (active cells) its first vertex id
-// within the slab, and per thread its cells' exclusive count prefix.  K is
+// within the slab.  K is
 // the largest layer count whose sample columns ((K+1) * S) fit one pass of the
 // CTA's threads, whose workspace fits kSlabBudget bytes, and whose vertices fit
 // 16-bit ids (every edge of the slab's cells, counted once).
@@ -58,7 +58,7 @@ constexpr int kSlabMaxCells = 63;     // a sample column's bits fit one 64-bit m
 constexpr uint32_t kPieceShift = 24;  // queue entry: chunk | slab << kPieceShift
 
 struct SlabLayout {
-    uint32_t rho, cases, vbase, masks, prefix, total;
+    uint32_t rho, cases, vbase, masks, total;
     int K;
 };
 
@@ -72,7 +72,6 @@ __host__ __device__ inline SlabLayout slab_layout_k(int N, int K)
     L.cases = o;  o = align16(o + NC);
     L.vbase = o;  o = align16(o + NC * 2u);
     L.masks = o;  o = align16(o + (uint32_t)(K + 1) * S * 8u);
-    L.prefix = o; o = align16(o + (uint32_t)kSlabThreads * 8u);
     L.total = o;
     return L;
 }
@@ -251,7 +250,7 @@ cudaError_t launch_build(const DevParams& p, const BuildArgs& a, bool queue, int
                          size_t dyn_smem, cudaStream_t s);
 cudaError_t build_occupancy(bool queue, bool exact, int threads, size_t dyn_smem, int* blocks_per_sm);
 // the split build's front kernel: resident CTAs per SM for this shape
-cudaError_t front_occupancy(bool exact, int threads, size_t dyn_smem, int* blocks_per_sm);
+cudaError_t front_occupancy(bool exact, int threads, size_t dyn_smem, int* blocks_per_sm, bool slabs = false);
 cudaError_t prepare_build_kernels(size_t optin, size_t* max_dyn_smem);
 // the split build's emission kernel: its grid and dynamic shared memory
 cudaError_t split_emit_shape(const DevParams& p, const BuildArgs& a, int* grid, size_t* dyn_smem);
