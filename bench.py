@@ -507,6 +507,7 @@ def leg_mixed_lod(stream, flush, steps, warmup):
                       bufs["r"].data_ptr(), bufs["t"].data_ptr(), vcap, icap, 0, 0)
     cache = ROOT / "underwaterworld_gb300" / "_build" / "tune_cache.txt"
     tun, tuned_us = autotune(ctx, d_desc.data_ptr(), n, 48, out, str(cache))
+    shape = ctx.launch_shape(n, 48)
     L = abi.lib()
 
     def step():
@@ -527,6 +528,9 @@ def leg_mixed_lod(stream, flush, steps, warmup):
             "p99_ms": float(np.percentile(lat_ms, 99)), "steps": steps,
             "tuning": {"threads": tun.threads, "blocks_per_sm": tun.blocks_per_sm, "smem_cells": tun.smem_cells,
                        "tuned_us": tuned_us},
+            "build": {"kind": "split" if shape.build == abi.UWW_BUILD_SPLIT else "pipelined",
+                      "slabs_per_chunk": shape.slabs_per_chunk, "threads": shape.threads, "grid": shape.grid,
+                      "blocks_per_sm": shape.blocks_per_sm},
             "verts": int(tot[0]), "inds": int(tot[1])}
 
 

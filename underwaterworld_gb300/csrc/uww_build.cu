@@ -41,6 +41,9 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <type_traits>
 
 // The tables live in global memory: every CTA copies them into shared memory
@@ -2197,29 +2200,58 @@ cudaError_t prepare_build_kernels(size_t optin, size_t* max_dyn_smem)
     return m >= 16384 ? cudaSuccess : cudaErrorInvalidValue;
 }
 
+// Resident CTAs per SM of a kernel at a launch shape, and the device's SM
+// count: properties of the device that every batched launch needs, looked up
+// once per (device, kernel, threads, dynamic shared memory) and kept, so that
+// a build's host side issues its kernels without those queries in between.
+cudaError_t occupancy_of(const void* fn, int threads, size_t dyn_smem, int* blocks_per_sm, int* sms = nullptr)
+{
+    static std::mutex mu;
+    static std::map<std::tuple<int, const void*, int, size_t>, int> occ;
+    static std::map<int, int> sm_count;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lock(mu);
+    if (sms) {
+        auto it = sm_count.find(dev);
+        if (it == sm_count.end()) {
+            int n = 0;
+            if ((e = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+            it = sm_count.emplace(dev, n).first;
+        }
+        *sms = it->second;
+    }
+    const auto key = std::make_tuple(dev, fn, threads, dyn_smem);
+    auto it = occ.find(key);
+    if (it == occ.end()) {
+        int b = 0;
+        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, fn, threads, dyn_smem)) != cudaSuccess) return e;
+        it = occ.emplace(key, b).first;
+    }
+    *blocks_per_sm = it->second;
+    return cudaSuccess;
+}
+
 cudaError_t build_occupancy(bool queue, bool exact, int threads, size_t dyn_smem, int* blocks_per_sm)
 {
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, kernel_for(exact, queue, threads > 224),
-                                                         threads, dyn_smem);
+    return occupancy_of((const void*)kernel_for(exact, queue, threads > 224), threads, dyn_smem, blocks_per_sm);
 }
 
 cudaError_t front_occupancy(bool exact, int threads, size_t dyn_smem, int* blocks_per_sm, bool slabs)
 {
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, front_for(exact, threads, slabs), threads,
-                                                         dyn_smem);
+    return occupancy_of((const void*)front_for(exact, threads, slabs), threads, dyn_smem, blocks_per_sm);
 }
 
 cudaError_t split_emit_shape(const DevParams& p, const BuildArgs& a, int* grid, size_t* dyn_smem)
 {
-    int dev = 0, sms = 0, ebps = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    int sms = 0, ebps = 0;
     // dynamic shared memory: a chunk's workspace (chunks without staging
     // room), a gathered vertex block (9 words a vertex) or the z tables of a
     // slab built again, the largest
     size_t edyn = std::max(a.slot_bytes, (size_t)kVertexBlock * 9 * sizeof(float));
     if (a.pmax > 1) edyn = std::max(edyn, ztable_bytes((int)a.max_cells + 1, (int)p.octaves));
-    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ebps, emit_for(p.math_mode == UWW_MATH_EXACT), 256, edyn);
+    const cudaError_t e = occupancy_of((const void*)emit_for(p.math_mode == UWW_MATH_EXACT), 256, edyn, &ebps, &sms);
     if (e != cudaSuccess) return e;
     *grid = std::max(1, sms * std::max(1, ebps));
     *dyn_smem = edyn;
@@ -2291,13 +2323,10 @@ cudaError_t launch_build(const DevParams& p, const BuildArgs& a, bool queue, int
     // CTAs striding over the vertices, launched as a programmatic dependent
     // of the build so that its launch and table setup overlap the build's
     // last CTAs
-    int dev = 0, sms = 0;
-    e = cudaGetDevice(&dev);
-    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (e != cudaSuccess) return e;
+    int sms = 0;
     const VertexFn vfn = exact ? vertex_kernel<ExactOps> : vertex_kernel<FastOps>;
     int vbps = 0;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&vbps, vfn, 256, 0)) != cudaSuccess) return e;
+    if ((e = occupancy_of((const void*)vfn, 256, 0, &vbps, &sms)) != cudaSuccess) return e;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)std::max(1, sms * std::max(1, vbps)));
     cfg.blockDim = dim3(256);
