@@ -1,9 +1,10 @@
 """Chunks above 16 cells per edge built as x slabs by the split build.
 
-The split build of a planned batch (no per-cell cases or samples, depth
-shortcut on) builds every chunk of 17..63 cells per edge as slabs of a few
-cell layers, one CTA each; a slab's references to vertices of the previous
-slab's last layer go through that slab's seam.  The output must be the
+The split build builds every chunk of 17..63 cells per edge as slabs of a
+few cell layers, one CTA each (any batch whose samples are computed, not
+read); a slab's references to vertices of the previous slab's last layer go
+through that slab's seam.  Per-cell cases, samples and per-vertex edge ids
+(the adjoint's forward) come from the slabs too.  The output must be the
 chunk's, bit for bit: against the F32 oracle (parity build, chunk.rs:135-264
 with perlin_util.rs:6-29), and against the single pipelined kernel, which
 builds each chunk whole (fast build).  Covered: the uneven-LOD batch
@@ -18,6 +19,7 @@ import numpy as np
 import pytest
 
 from underwaterworld_gb300 import abi, workloads
+from underwaterworld_gb300.adjoint import Adjoint
 from underwaterworld_gb300.chunk import make_descs
 
 from helpers import assert_batches_equal, relayout
@@ -55,10 +57,11 @@ def test_mixed_batch_takes_the_slab_build(ctx_factory):
     ctx = ctx_factory(p)
     s = ctx.launch_shape(len(d), 48)
     assert s.build == abi.UWW_BUILD_SPLIT and s.slabs_per_chunk > 1 and s.threads == 256
-    # per-cell cases are written chunk by chunk: the pipelined build
+    # per-cell cases as well (the planning kernel then decides nothing)
     q = p.copy()
     q.outputs = COLOR_NORMALS | abi.UWW_OUT_CASES
-    assert ctx_factory(q).launch_shape(len(d), 48).build == abi.UWW_BUILD_PIPELINED
+    s = ctx_factory(q).launch_shape(len(d), 48)
+    assert s.build == abi.UWW_BUILD_SPLIT and s.slabs_per_chunk > 1
     ctx.set_tuning(options=abi.UWW_TUNE_PIPELINED)
     assert ctx.launch_shape(len(d), 48).build == abi.UWW_BUILD_PIPELINED
     ctx.set_tuning(options=0)
@@ -147,3 +150,25 @@ def test_slabs_without_staging_room(ctx_factory, frac):
         np.testing.assert_array_equal(small.verts[v0:v0 + nv].view(np.uint32), full.verts[v0:v0 + nv].view(np.uint32))
         np.testing.assert_array_equal(small.normals[v0:v0 + nv].view(np.uint32),
                                       full.normals[v0:v0 + nv].view(np.uint32))
+
+
+@pytest.mark.parametrize("cells", [24, 16])
+def test_forward_with_edge_ids_matches_the_pipelined_build(ctx_factory, cells):
+    """uww_forward (records, vertices, cases and per-vertex edge ids) through the
+    split build -- slabs for 24^3, whole chunks for 16^3 -- against the
+    pipelined build, byte for byte (fast build)."""
+    p, d = workloads.adjoint_batch(seed=0, side=6, cells=cells)
+    p.math_mode = abi.UWW_MATH_FAST
+    ctx = ctx_factory(p)
+    assert ctx.launch_shape(len(d), cells).build == abi.UWW_BUILD_SPLIT
+    a = Adjoint(ctx, d, 1 << 20, 1 << 22)
+    a.forward()
+    split = a.fetch_forward()
+    ctx.set_tuning(options=abi.UWW_TUNE_PIPELINED)
+    a.forward()
+    piped = a.fetch_forward()
+    ctx.set_tuning(options=0)
+    assert int(split["totals"][0]) > 1000
+    for k in ("totals", "records", "edge_ids", "cases"):
+        np.testing.assert_array_equal(split[k], piped[k], err_msg=k)
+    np.testing.assert_array_equal(split["verts"].view(np.uint32), piped["verts"].view(np.uint32))

@@ -163,18 +163,21 @@ bool plans(const uww_ctx* ctx, const uww_mesh_out* out, const float* samples_in)
 
 // split_ok: nothing of the launch needs the pipelined kernel (streamed host
 // output and per-vertex edge ids do)
-int plan_launch(uww_ctx* ctx, uint32_t n, uint32_t max_cells, bool queue, LaunchCfg* cfg, bool split_ok, bool planned)
+int plan_launch(uww_ctx* ctx, uint32_t n, uint32_t max_cells, bool queue, LaunchCfg* cfg, bool split_ok, bool planned,
+                bool samples_in = false)
 {
     const size_t cap = ctx->smem_dyn_max;
     const int compute = ctx->threads > 0 ? ctx->threads : default_compute_threads(max_cells);
     const size_t zt_max = ctx->dev.math_mode == UWW_MATH_FAST ? ztable_bytes((int)max_cells + 1, ctx->dev.octaves) : 0;
     cfg->pmax = 1;
     cfg->slab_slot = 0;
-    // A planned batch with chunks above 16 cells per edge (the 24^3 and 48^3
-    // LODs): the split build, with those chunks as slabs of a few x layers
-    // (one CTA of kSlabThreads threads each) and the rest whole, in one
-    // shared workspace sized for the larger of a 16^3 chunk and a slab.
-    if (queue && split_ok && planned && max_cells > 16 && max_cells <= (uint32_t)kSlabMaxCells &&
+    // A batch with chunks above 16 cells per edge (the 24^3 and 48^3 LODs)
+    // whose samples are computed, not read: the split build, with those
+    // chunks as slabs of a few x layers (one CTA of kSlabThreads threads
+    // each) and the rest whole, in one shared workspace sized for the larger
+    // of a 16^3 chunk and a slab.
+    (void)planned;
+    if (queue && split_ok && !samples_in && max_cells > 16 && max_cells <= (uint32_t)kSlabMaxCells &&
         n < (1u << kPieceShift) && !(ctx->options & UWW_TUNE_PIPELINED) &&
         !(ctx->test_flags & UWW_TEST_WITHHOLD_FIRST) && ctx->smem_cells <= 0 &&
         (ctx->threads <= 0 || ctx->threads == kSlabThreads)) {
@@ -289,8 +292,8 @@ int launch(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint32_t ma
            const HostOut* host = nullptr)
 {
     LaunchCfg cfg;
-    int st = plan_launch(ctx, n, max_cells, queue, &cfg, host == nullptr && edge_ids == nullptr,
-                         plans(ctx, out, samples_in));
+    int st = plan_launch(ctx, n, max_cells, queue, &cfg, host == nullptr, plans(ctx, out, samples_in),
+                         samples_in != nullptr);
     if (st) return st;
     // the work buffers a captured frame graph refers to: a reallocation
     // moves the context's generation on, and such a frame recaptures itself
@@ -377,22 +380,20 @@ int launch(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint32_t ma
             // The counters, the tile sums, per chunk its counts word and its
             // staging place, and the work queues -- laid out for the chunk
             // count the buffer was sized for, so that they stay in place from
-            // one launch to the next -- then per chunk a workspace slot.  The
-            // counters and tile sums are zero at launch: cleared here on
-            // (re)allocation and left zero by every launch's emission kernel.
-            // (with slabs: a place per slab for the staging places and the
-            // queues; the slots hold whole chunks of up to 16 cells)
+            // one launch to the next.  The counters and tile sums are zero at
+            // launch: cleared here on (re)allocation and left zero by every
+            // launch's emission kernel.  (With slabs: a place per slab for
+            // the staging places and the queues.)
             const size_t pm = cfg.pmax;
-            const size_t slot = align16(chunk_layout(pm > 1 ? 16 : (int)max_cells).total);
             auto fixed_bytes = [pm](uint32_t m) {
                 const size_t ntiles = ((size_t)m + kTileChunks - 1) / kTileChunks;
                 return kCtrWords * 4 + ((ntiles * 8 + 15) & ~size_t(15)) + (((size_t)m * 8 + 15) & ~size_t(15)) +
                        (((size_t)m * pm * 8 + 15) & ~size_t(15)) + (((size_t)m * pm * 4 * kPlanRanks + 15) & ~size_t(15));
             };
             const uint32_t m = std::max(n, ctx->split_n);
-            if (!ctx->d_split || ctx->split_n < n || ctx->split_cap < fixed_bytes(m) + (size_t)m * slot) {
+            if (!ctx->d_split || ctx->split_n < n || ctx->split_cap < fixed_bytes(m)) {
                 const uint32_t mm = std::max(m, 4096u);
-                st = grow(&ctx->d_split, &ctx->split_cap, fixed_bytes(mm) + (size_t)mm * slot);
+                st = grow(&ctx->d_split, &ctx->split_cap, fixed_bytes(mm));
                 if (st) return st;
                 ctx->split_n = mm;
                 const size_t ntiles = ((size_t)mm + kTileChunks - 1) / kTileChunks;
@@ -413,8 +414,7 @@ int launch(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint32_t ma
             b += ((size_t)nc * pm * 8 + 15) & ~size_t(15);
             a.split_queue = reinterpret_cast<uint32_t*>(b);
             b += ((size_t)nc * pm * 4 * kPlanRanks + 15) & ~size_t(15);
-            a.slots = b;
-            a.slot_bytes = slot;
+            a.split = 1;
             a.pmax = (uint32_t)pm;
             a.piece_cells = 16;
             if (pm > 1) {
@@ -441,7 +441,7 @@ int launch(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint32_t ma
             // chunk, one whole chunk per chunk
             const size_t vc = out->vert_capacity, ic = out->ind_capacity;
             const size_t units = vc / kVertexBlock + ic / kIndexBlock + 3 * (size_t)nc * pm;
-            const size_t sbytes = vc * 16 + ((ic * 4 + 15) & ~size_t(15)) + units * 8;
+            const size_t sbytes = vc * 16 + ((ic * 4 + 15) & ~size_t(15)) + units * 8 + (edge_ids ? vc * 4 : 0);
             if (!ctx->d_stage || ctx->stage_cap < sbytes) {
                 st = grow(&ctx->d_stage, &ctx->stage_cap, sbytes);
                 if (st) return st;
@@ -452,10 +452,15 @@ int launch(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint32_t ma
             a.stage_inds = reinterpret_cast<uint32_t*>(sb);
             sb += (ic * 4 + 15) & ~size_t(15);
             a.units = reinterpret_cast<unsigned long long*>(sb);
+            sb += units * 8;
+            a.stage_eids = edge_ids ? reinterpret_cast<uint32_t*>(sb) : nullptr;
             a.unit_cap = (uint32_t)std::min<size_t>(units, 0xffffffffu);
             a.stage_vcap = out->vert_capacity;
             a.stage_icap = out->ind_capacity;
-            a.split_planned = a.plan != nullptr;
+            // (a batch with slabs always runs the planning kernel, which
+            // queues the slabs; it decides chunks only when planned)
+            a.split_planned = a.plan != nullptr || pm > 1;
+            a.split_decide = a.plan != nullptr;
             a.plan = nullptr;  // the split build plans into its own queues
         }
     }

@@ -738,8 +738,8 @@ struct EmitOut {
 // triangle map (else a binary search over the active cells), its three
 // chunk-local vertex ids into inds, and the positions of the vertices its
 // cell creates (the first reference of an owned edge).  The workspace W is
-// in shared memory or a scratch slot (the build kernel) or in a global slot
-// (the split build's emission kernel); the arithmetic is the same either way.
+// in shared memory or a scratch slot (the build kernel); the arithmetic is the
+// same either way.
 // carry_corner: pass 2 follows, and colour slot 0 carries the owner's corner b.
 // positions: write the vertices the cell creates (the split build's vertex
 // work writes them instead).
@@ -1226,13 +1226,16 @@ __global__ void __launch_bounds__(kPlanThreads) plan_kernel(const DevParams p, c
 }
 
 // ---------------------------------------------------------------------------
-// Split build, for batches whose chunks all work in shared memory: the front
-// half with the chunk-local pass 1, the records, and the rest of the
-// emission, as separate kernels instead of one pipelined one.
-//   split_plan_kernel (planned batches): one pass, one thread per chunk -- a
-//     chunk the depth bias decides gets its counts word (zero, early-blank
-//     flag) at once; the others go to one of kPlanRanks work queues by cost
-//     rank (bias_decides_with), the likely costliest first.
+// Split build, for batches whose chunks (or slabs of them) all work in
+// shared memory: the front half with the chunk-local pass 1, the records,
+// and the rest of the emission, as separate kernels instead of one pipelined
+// one.
+//   split_plan_kernel (planned batches, and every batch with slabs): one
+//     pass, one thread per chunk -- a chunk the depth bias decides gets its
+//     counts word (zero, early-blank flag) at once (planned batches); the
+//     others go to one of kPlanRanks work queues by cost rank
+//     (bias_decides_with), the likely costliest first, a large chunk as its
+//     slabs.
 //   front_kernel: persistent, every thread a compute thread, one chunk per CTA
 //     at a time from the queues -- noise, votes, classification and block scan
 //     (chunk_front), then for a meshed chunk pass 1 from shared memory:
@@ -1245,25 +1248,11 @@ __global__ void __launch_bounds__(kPlanThreads) plan_kernel(const DevParams p, c
 //     write the records and totals, a tile of chunks each; then every CTA
 //     takes units from a counter -- a vertex block's colours and normals
 //     from its staged positions, an index block -- and, once the records
-//     are written, stores them in place.  A chunk the staging buffers had no room
-//     for (the batch's output then exceeds the capacities) left its
-//     workspace in its slot and is emitted from there by one CTA.
+//     are written, stores them in place.  A chunk or slab the staging buffers
+//     had no room for (the batch's output then exceeds the capacities) is
+//     built again by one CTA and emitted in place.
 // The same device functions as the pipelined build: the same bits.  The work
 // order (queues, mesh list) varies from run to run; the outputs do not.
-
-__device__ __forceinline__ Workspace workspace_at(uint8_t* base, int N)
-{
-    const ChunkLayout L = chunk_layout(N);
-    Workspace w;
-    w.rho = reinterpret_cast<float*>(base + L.rho);
-    w.cases = base + L.cases;
-    w.vbase = base + L.vbase;
-    w.active = base + L.active;
-    w.ibase = base + L.ibase;
-    w.idx16 = L.idx16;
-    w.active16 = L.active16;
-    return w;
-}
 
 // ---------------------------------------------------------------------------
 // Slabs of a large chunk (split build; layout and layer count: slab_layout).
@@ -1303,7 +1292,7 @@ __device__ __forceinline__ bool slab_chunk(const BuildArgs& a, uint32_t cells)
 // A cell column (x, y) of a slab: its four corner columns' masks and its
 // active cells (bit z: the cell's corners are not all on one side)
 struct SlabColumn {
-    unsigned long long m00, m10, m01, m11, act;
+    unsigned long long m00, m10, m01, m11, act, allin;
 };
 
 __device__ __forceinline__ SlabColumn slab_column(const unsigned long long* masks, int S, int xl, int y, int N)
@@ -1315,7 +1304,8 @@ __device__ __forceinline__ SlabColumn slab_column(const unsigned long long* mask
     c.m01 = masks[col + 1];
     c.m11 = masks[col + S + 1];
     const unsigned long long an = c.m00 & c.m10 & c.m01 & c.m11, no = ~(c.m00 | c.m10 | c.m01 | c.m11);
-    const unsigned long long quiet = (an & (an >> 1)) | (no & (no >> 1));
+    c.allin = an & (an >> 1);
+    const unsigned long long quiet = c.allin | (no & (no >> 1));
     c.act = ~quiet & ((1ull << N) - 1ull);
     return c;
 }
@@ -1330,15 +1320,17 @@ __device__ __forceinline__ unsigned long long cell_counts(const SmemTables& T, i
 // Front half of slab s of chunk c into workspace W: the noise of its planes
 // (fast build: the column form, which also leaves the columns' masks), the
 // early-blank and solid votes, the classification from the masks, the block
-// scan and each active cell's first vertex id; the last layer's ids and cases
-// to the seam when a slab follows (write_seam).  Returns the slab's packed
-// counts (every thread; 0 when no cell is crossed); *any_inside: a sample is
-// not above the iso level; *run: the thread's exclusive prefix.  Every thread
-// (kSlabThreads) must call it.  GWS: W is in global memory (this CTA's scratch).
+// scan and each active cell's first vertex id.  The first time (first: the
+// front kernel, not a rebuild) it also writes the last layer's ids and cases
+// to the seam when a slab follows, and the slab's samples and cell cases when
+// the batch asks for them.  Returns the slab's packed counts (every thread; 0
+// when no cell is crossed); *any_inside: a sample is not above the iso level;
+// *run: the thread's exclusive prefix.  Every thread (kSlabThreads) must call
+// it.  GWS: W is in global memory (this CTA's scratch).
 template <class O, bool GWS>
 __device__ unsigned long long slab_front(const DevParams& p, const BuildArgs& a, SmemTables& T, const SlabWs W,
                                          uint8_t* ztab, const uww_chunk_desc d, uint32_t c, uint32_t s, int ncomp,
-                                         bool write_seam, int* any_inside_out, unsigned long long* run_out)
+                                         bool first, int* any_inside_out, unsigned long long* run_out)
 {
     const int tid = threadIdx.x;
     const int oriented = p.dedup_mode == UWW_DEDUP_ORIENTED;
@@ -1346,8 +1338,12 @@ __device__ unsigned long long slab_front(const DevParams& p, const BuildArgs& a,
     const int x0 = (int)s * K, x1 = min(x0 + K, N), nl = x1 - x0, planes = nl + 1;
     const int ox = d.pos[0] * p.chunk_size, oy = d.pos[1] * p.chunk_size, oz = d.pos[2] * p.chunk_size;
     const float iso = p.iso_level;
-    int inside = 0, outside = 0;
-    if constexpr (std::is_same<O, FastOps>::value) {
+    // a chunk the depth bias decides (met here when the batch is not planned:
+    // its cases are written) needs no noise unless its samples are written
+    const int decided = (first && !a.samples_out && !a.no_depth_shortcut) ? bias_decides(p, N, oz) : 0;
+    int inside = decided == 2, outside = decided == 1;
+    if (decided) {
+    } else if constexpr (std::is_same<O, FastOps>::value) {
         // (columns of 25 and 49 samples accumulated in registers were no
         // faster, 49 much slower: the unrolled column outgrows the caches)
         const ZTable zt = ztable_at(ztab, S, p.octaves);
@@ -1372,7 +1368,24 @@ __device__ unsigned long long slab_front(const DevParams& p, const BuildArgs& a,
     const int solid = bar_and(kBarCompute, ncomp, !outside);
     *any_inside_out = any_inside;
     *run_out = 0ull;
-    if (!any_inside || solid) return 0ull;
+    // the samples and cell cases the batch asks for, within the capacities
+    // the caller gave (the chunk's planes x0..x1 and cells of layers x0..x1-1)
+    const bool want_cases = first && (p.outputs & UWW_OUT_CASES) != 0 && a.cases != nullptr;
+    const bool cases_ok = want_cases && (unsigned long long)d.cell_offset + (unsigned long long)N * N * N <= a.case_capacity;
+    const bool samples_ok = first && a.samples_out &&
+                            (unsigned long long)d.sample_offset + (unsigned long long)S * S * S <= a.sample_capacity;
+    if (tid == 0 && ((want_cases && !cases_ok) || (first && a.samples_out && !samples_ok)))
+        atomicOr(&T.errflags, (uint32_t)kErrRange);
+    if (samples_ok) {
+        float* dst = a.samples_out + d.sample_offset + (size_t)x0 * S * S;
+        for (int idx = tid; idx < planes * S * S; idx += ncomp) dst[idx] = W.rho[idx];
+    }
+    uint8_t* cases_out = cases_ok ? a.cases + d.cell_offset + (size_t)x0 * N * N : nullptr;
+    if (!any_inside || solid) {
+        if (cases_out)
+            for (int k = tid; k < nl * N * N; k += ncomp) cases_out[k] = solid ? 255 : 0;
+        return 0ull;
+    }
     if constexpr (!std::is_same<O, FastOps>::value) {
         for (int col = tid; col < planes * S; col += ncomp) {
             unsigned long long m = 0ull;
@@ -1389,6 +1402,10 @@ __device__ unsigned long long slab_front(const DevParams& p, const BuildArgs& a,
         const int xl = q / N, y = q - xl * N, x = x0 + xl;
         const SlabColumn col = slab_column(W.masks, S, xl, y, N);
         const unsigned own_lo = (x == 0) | ((y == 0) << 1) | ((x == N - 1) << 3) | ((y == N - 1) << 4);
+        if (cases_out)
+            for (int z = 0; z < N; ++z)
+                cases_out[q * N + z] = ((col.act >> z) & 1ull) ? (uint8_t)mask_case(col.m00, col.m10, col.m01, col.m11, z)
+                                                               : ((col.allin >> z) & 1ull) ? 255 : 0;
         for (unsigned long long act = col.act; act; act &= act - 1ull) {
             const int z = __ffsll((long long)act) - 1;
             const int cs = mask_case(col.m00, col.m10, col.m01, col.m11, z);
@@ -1400,8 +1417,7 @@ __device__ unsigned long long slab_front(const DevParams& p, const BuildArgs& a,
     const unsigned long long run = block_exclusive_scan(mine, T, total, ncomp);
     *run_out = run;
     // ---- each active cell's first vertex id; the seam ----
-    uint32_t* seam = write_seam && (int)s + 1 < slab_count(N) ? a.seam + ((size_t)c * a.pmax + s) * a.seam_stride
-                                                                 : nullptr;
+    uint32_t* seam = first && (int)s + 1 < slab_count(N) ? a.seam + ((size_t)c * a.pmax + s) * a.seam_stride : nullptr;
     unsigned long long r = run;
     for (int q = q0; q < q1; ++q) {
         const int xl = q / N, y = q - xl * N, x = x0 + xl;
@@ -1480,6 +1496,7 @@ __device__ void slab_emit(const DevParams& p, const BuildArgs& a, const SmemTabl
                     id = vb + __popc(own & __ldg(before + e));
                     if ((fr >> i) & 1u) {
                         const EdgeVertex ev = edge_vertex<O>(p, T, W.rho, S, x, y, z, e, sc, ox, oy, oz, x0);
+                        if (eo.edge_ids) eo.edge_ids[voff + id] = ev.edge_id;
                         if (FINAL) {
                             float2* v2 = reinterpret_cast<float2*>(eo.verts + voff + id);
                             v2[0] = make_float2(ev.x, ev.y);
@@ -1528,8 +1545,9 @@ __global__ void __launch_bounds__(kPlanThreads) split_plan_kernel(const DevParam
         const int oz = __ldg(&a.chunks[i].pos[2]) * p.chunk_size;
         const bool ok = cells >= 1 && cells <= a.max_cells && cells <= UWW_MAX_CELLS;
         int rank = 0;
-        const int kind =
-            ok ? bias_decides_with(p, B, __fdiv_rn((float)p.chunk_size, (float)cells), (int)cells, oz, &rank) : 0;
+        const int kind = (ok && a.split_decide)
+                             ? bias_decides_with(p, B, __fdiv_rn((float)p.chunk_size, (float)cells), (int)cells, oz, &rank)
+                             : 0;
         if (kind) {
             a.tinfo[i] = decided_info(kind);
         } else if (ok && slab_chunk(a, cells)) {
@@ -1609,7 +1627,7 @@ __device__ void front_slab(const DevParams& p, const BuildArgs& a, SmemTables& T
     if (!nI) return;
     const unsigned long long st = stage;
     if (st != kUnstaged) {
-        const EmitOut eo{nullptr, a.stage_inds, nullptr, a.stage_pos};
+        const EmitOut eo{nullptr, a.stage_inds, a.edge_ids ? a.stage_eids : nullptr, a.stage_pos};
         slab_emit<O, false>(p, a, T, W, d, c, sl, run, nthr, eo, (uint32_t)st, (uint32_t)(st >> 32), 0u, 0u, true);
         for (uint32_t k = tid; k < vb; k += nthr)
             if (unit_a + k < a.unit_cap) a.units[unit_a + k] = unit_entry(c, k | (sl << 16), kUnitVerts | kUnitSlab);
@@ -1670,7 +1688,7 @@ __global__ void __launch_bounds__(MAXT, MINB) front_kernel(const DevParams p, co
         const uint32_t nV = (uint32_t)(ci.total & kField22), nI = (uint32_t)((ci.total >> kIndShift) & kField22);
         // the chunk's emission work: blocks of kVertexBlock vertices (colour,
         // normal; list A) and of kIndexBlock indices (list B) when its pass 1
-        // is staged, else the whole chunk from its slot (list A)
+        // is staged, else the whole chunk, built again (list A)
         const uint32_t vb = (nV + kVertexBlock - 1) / kVertexBlock, ib = (nI + kIndexBlock - 1) / kIndexBlock;
         if (tid == 0) {
             a.tinfo[c] = ci.total | ((ci.flags & UWW_CHUNK_EARLY_BLANK) ? kInfoEarlyBlank : 0ull);
@@ -1700,21 +1718,17 @@ __global__ void __launch_bounds__(MAXT, MINB) front_kernel(const DevParams p, co
                 const uint32_t nT = nI / 3u, nA = (uint32_t)(ci.total >> kActShift);
                 const bool direct = direct_triangles(W, N, ci.total);
                 const float s = __fdiv_rn((float)p.chunk_size, (float)N);
-                const EmitOut eo{nullptr, a.stage_inds, nullptr, a.stage_pos};
+                const EmitOut eo{nullptr, a.stage_inds, a.edge_ids ? a.stage_eids : nullptr, a.stage_pos};
                 for (uint32_t t = tid; t < nT; t += nthr)
                     emit_triangle<O>(p, eo, T, W, N, nA, direct, t, sv, si, ci.ox, ci.oy, ci.oz, s, true);
                 for (uint32_t k = tid; k < vb; k += nthr)
                     if (unit_a + k < a.unit_cap) a.units[unit_a + k] = unit_entry(c, k, kUnitVerts);
                 for (uint32_t k = tid; k < ib; k += nthr)
                     if (unit_b + k < a.unit_cap) a.units[a.unit_cap - 1 - (unit_b + k)] = unit_entry(c, k, kUnitInds);
-            } else {
-                // no room: the workspace to the chunk's slot, in 16-byte
-                // words, for the emission kernel to emit the chunk from
-                const uint32_t words = chunk_layout(ci.N).total / 16u;
-                const uint4* src = reinterpret_cast<const uint4*>(dyn_smem);
-                uint4* dst = reinterpret_cast<uint4*>(a.slots + (size_t)c * a.slot_bytes);
-                for (uint32_t i = tid; i < words; i += nthr) dst[i] = src[i];
-                if (tid == 0 && unit_a < a.unit_cap) a.units[unit_a] = unit_entry(c, 0, kUnitChunk);
+            } else if (tid == 0 && unit_a < a.unit_cap) {
+                // no room: one unit, for the emission kernel to build the
+                // chunk again and emit it in place
+                a.units[unit_a] = unit_entry(c, 0, kUnitChunk);
             }
         }
         __syncthreads();  // the workspace and the staged ticket are reused
@@ -1779,7 +1793,7 @@ __device__ __noinline__ void emit_slab_again(const DevParams& p, const BuildArgs
     unsigned long long run = 0ull;
     slab_front<O, true>(p, a, T, W, dyn_smem, d, c, sl, nthr, false, &any_inside, &run);
     __syncthreads();
-    const EmitOut eo{a.verts, a.inds, nullptr, nullptr};
+    const EmitOut eo{a.verts, a.inds, a.edge_ids, nullptr};
     slab_emit<O, true>(p, a, T, W, d, c, sl, run, nthr, eo, voff, ioff, vbase0, prev_base, want_color || want_normals);
     if (want_color || want_normals) {
         __syncthreads();  // the slab's vertex positions, written by this CTA
@@ -1788,10 +1802,49 @@ __device__ __noinline__ void emit_slab_again(const DevParams& p, const BuildArgs
     }
 }
 
+// The emission kernel's work on a whole chunk the staging buffers had no
+// room for: its front half again in this CTA's dynamic shared memory (laid
+// out by rebuild_layout; its cases and samples are the front kernel's), then
+// pass 1 into the outputs at its record's offsets and pass 2.  Kept out of
+// line, like emit_slab_again.
+template <class O>
+__device__ __noinline__ void emit_chunk_again(const DevParams& p, const BuildArgs& a, SmemTables& T, uint8_t* dyn_smem,
+                                              uint32_t c, const uww_chunk_record rec)
+{
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    const bool want_color = (p.outputs & UWW_OUT_COLOR) != 0;
+    const bool want_normals = (p.outputs & UWW_OUT_NORMALS) != 0 && a.normals != nullptr;
+    BuildArgs b = a;
+    b.cases = nullptr;
+    b.samples_out = nullptr;
+    b.smem_buf_bytes = chunk_layout((int)a.smem_cells).total;
+    size_t zt = 0, mo = 0;
+    rebuild_layout((int)a.smem_cells, (int)p.octaves, std::is_same<O, FastOps>::value, a.mask_offset != 0, &zt, &mo);
+    b.ztable_offset = zt;
+    b.mask_offset = (uint32_t)mo;
+    const uww_chunk_desc d = a.chunks[c];
+    chunk_front<O, false>(p, b, T, dyn_smem, d, c, c, 0, nthr);
+    __syncthreads();
+    const int N = (int)d.cells;
+    const Workspace W = workspace(b, dyn_smem, 0, N);
+    const bool direct = direct_triangles(W, N, T.ci[0].total);
+    const float s = __fdiv_rn((float)p.chunk_size, (float)N);
+    const EmitOut eo{a.verts, a.inds, a.edge_ids, nullptr};
+    for (uint32_t tr = tid; tr < rec.num_inds / 3u; tr += nthr)
+        emit_triangle<O>(p, eo, T, W, N, rec.num_active_cells, direct, tr, rec.vert_offset, rec.ind_offset,
+                         d.pos[0] * p.chunk_size, d.pos[1] * p.chunk_size, d.pos[2] * p.chunk_size, s,
+                         want_color || want_normals);
+    if (want_color || want_normals) {
+        __syncthreads();  // the chunk's vertex positions, written by this CTA
+        for (uint32_t v = tid; v < rec.num_verts; v += nthr)
+            finish_vertex<O>(p, T.perm, T.gp, a.verts, a.normals, rec.vert_offset + v, want_color, want_normals);
+    }
+}
+
 template <class O>
 __global__ void __launch_bounds__(256, 4) emit_kernel(const DevParams p, const BuildArgs a)
 {
-    // one workspace (chunks emitted from their slot) or a gathered vertex block
+    // a chunk built again (chunks without staging room) or a gathered vertex block
     extern __shared__ __align__(16) uint8_t dyn_smem[];
     __shared__ SmemTables T;
     __shared__ int last;
@@ -1969,6 +2022,9 @@ __global__ void __launch_bounds__(256, 4) emit_kernel(const DevParams p, const B
                 __syncthreads();  // the block is gathered
                 const uww_chunk_record rec = load_record(&a.records[c]);
                 if (ok && !(rec.flags & UWW_CHUNK_OVERFLOW)) {
+                    if (a.edge_ids && tid < (int)nv)
+                        a.edge_ids[rec.vert_offset + bv + v] =
+                            __ldcg(a.stage_eids + (uint32_t)__ldcg(&a.stage_at[place]) + v);
                     float* dv = reinterpret_cast<float*>(a.verts + rec.vert_offset + bv + v0);
                     for (uint32_t k = tid; k < 6 * nv; k += nthr) dv[k] = sw[k];
                     if (want_normals) {
@@ -2025,31 +2081,12 @@ __global__ void __launch_bounds__(256, 4) emit_kernel(const DevParams p, const B
                 if (rec.flags & UWW_CHUNK_OVERFLOW) goto unit_done;
                 emit_slab_again<O>(p, a, T, dyn_smem, c, sl, rec.vert_offset + bv, rec.ind_offset + bi, bv, pv, cnV);
             } else {
-                // a chunk without staging room: pass 1 and pass 2 from its slot
+                // a chunk without staging room: built again here, then
+                // passes 1 and 2 in place
                 if (!await_records()) goto unit_done;
                 const uww_chunk_record rec = load_record(&a.records[c]);
                 if (rec.flags & UWW_CHUNK_OVERFLOW) goto unit_done;
-                const uww_chunk_desc d = a.chunks[c];
-                const int N = (int)d.cells;
-                const uint32_t words = chunk_layout(N).total / 16u;
-                const uint4* src = reinterpret_cast<const uint4*>(a.slots + (size_t)c * a.slot_bytes);
-                uint4* dst = reinterpret_cast<uint4*>(dyn_smem);
-                for (uint32_t i = tid; i < words; i += nthr) dst[i] = __ldcg(src + i);
-                __syncthreads();
-                const Workspace W = workspace_at(dyn_smem, N);
-                const bool direct = direct_triangles(W, N, w & (kInfoEarlyBlank - 1));
-                const float s = __fdiv_rn((float)p.chunk_size, (float)N);
-                const EmitOut eo{a.verts, a.inds, a.edge_ids, nullptr};
-                for (uint32_t tr = tid; tr < rec.num_inds / 3u; tr += nthr)
-                    emit_triangle<O>(p, eo, T, W, N, rec.num_active_cells, direct, tr, rec.vert_offset,
-                                     rec.ind_offset, d.pos[0] * p.chunk_size, d.pos[1] * p.chunk_size,
-                                     d.pos[2] * p.chunk_size, s, want_color || want_normals);
-                if (want_color || want_normals) {
-                    __syncthreads();  // the chunk's vertex positions, written by this CTA
-                    for (uint32_t v = tid; v < rec.num_verts; v += nthr)
-                        finish_vertex<O>(p, T.perm, T.gp, a.verts, a.normals, rec.vert_offset + v, want_color,
-                                         want_normals);
-                }
+                emit_chunk_again<O>(p, a, T, dyn_smem, c, rec);
             }
         }
     unit_done:
@@ -2246,10 +2283,13 @@ cudaError_t front_occupancy(bool exact, int threads, size_t dyn_smem, int* block
 cudaError_t split_emit_shape(const DevParams& p, const BuildArgs& a, int* grid, size_t* dyn_smem)
 {
     int sms = 0, ebps = 0;
-    // dynamic shared memory: a chunk's workspace (chunks without staging
-    // room), a gathered vertex block (9 words a vertex) or the z tables of a
-    // slab built again, the largest
-    size_t edyn = std::max(a.slot_bytes, (size_t)kVertexBlock * 9 * sizeof(float));
+    // dynamic shared memory: a whole chunk built again (chunks without
+    // staging room), a gathered vertex block (9 words a vertex) or the z
+    // tables of a slab built again, the largest
+    size_t zt = 0, mo = 0;
+    size_t edyn = std::max(rebuild_layout((int)a.smem_cells, (int)p.octaves, p.math_mode != UWW_MATH_EXACT,
+                                          a.mask_offset != 0, &zt, &mo),
+                           (size_t)kVertexBlock * 9 * sizeof(float));
     if (a.pmax > 1) edyn = std::max(edyn, ztable_bytes((int)a.max_cells + 1, (int)p.octaves));
     const cudaError_t e = occupancy_of((const void*)emit_for(p.math_mode == UWW_MATH_EXACT), 256, edyn, &ebps, &sms);
     if (e != cudaSuccess) return e;
@@ -2263,7 +2303,7 @@ cudaError_t launch_build(const DevParams& p, const BuildArgs& a, bool queue, int
 {
     const bool exact = p.math_mode == UWW_MATH_EXACT;
     cudaError_t e = cudaSuccess;
-    if (queue && a.slots) {
+    if (queue && a.split) {
         // the split build: [planning ->] front -> emission (-> vertex pass below)
         if (a.split_planned) {
             const uint32_t nblk = std::max(1u, std::min((a.n + kPlanThreads - 1) / kPlanThreads, 1024u));

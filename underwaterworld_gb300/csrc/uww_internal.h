@@ -104,6 +104,26 @@ __host__ __device__ inline size_t ztable_bytes(int S, int octaves)
            (size_t)S * sizeof(float) + (size_t)octaves * sizeof(unsigned) + 16;
 }
 
+// The split build's emission kernel builds a whole chunk again (one the
+// staging buffers had no room for) in its dynamic shared memory laid out
+// like the front kernel's, sized for chunks of up to smem_cells: the
+// workspace, the z tables (fast build) at *zt_off, the 13^3 column masks (when
+// the front kernel keeps them) at *mask_off; returns the bytes.
+__host__ __device__ inline size_t rebuild_layout(int smem_cells, int octaves, bool fast, bool masks, size_t* zt_off,
+                                                 size_t* mask_off)
+{
+    size_t o = chunk_layout(smem_cells).total;
+    *zt_off = o;
+    if (fast) o += ztable_bytes(smem_cells + 1, octaves);
+    *mask_off = 0;
+    if (masks) {
+        o = (o + 15) & ~size_t(15);
+        *mask_off = o;
+        o += 13 * 13 * sizeof(unsigned long long);
+    }
+    return o;
+}
+
 // Plan buffer of a planned batched build of n chunks: u32 [0] the planning
 // kernel's finish counter (zero between launches, at a fixed place whatever
 // n), [1] the number of listed chunks, [2 .. n+1] the listed chunks in
@@ -171,14 +191,14 @@ struct BuildArgs {
     uint32_t* edge_ids;              // optional, per output vertex: (first corner sample << 3) | direction
     const uint32_t* n_dev;           // optional device chunk count; the launch builds min(*n_dev, n)
     uint32_t* plan;                  // planned batch: finish counter, count, list (plan_kernel; kPlan*)
-    // Split build (every chunk in shared memory, no streamed host output).
-    // Per chunk c: its counts word tinfo[c] (packed counts, early-blank flag
-    // in bit 62) and, when meshed, where its staged pass 1 sits (stage_at[c]:
-    // vertices | indices << 32; all ones when the staging buffers had no
-    // room -- its workspace is then in slot c); per tile of kTileChunks
-    // chunks the sum of its counts (verts | inds << 32).
-    uint8_t* slots;                  // chunks x slot_bytes, 16-byte aligned
-    size_t slot_bytes;
+    // Split build (every chunk or slab in shared memory, no streamed host
+    // output).  Per chunk c: its counts word tinfo[c] (packed counts,
+    // early-blank flag in bit 62) and, when meshed, where its staged pass 1
+    // sits (stage_at[c * pmax]: vertices | indices << 32; all ones when the
+    // staging buffers had no room -- the emission kernel then builds it
+    // again); per tile of kTileChunks chunks the sum of its counts
+    // (verts | inds << 32).
+    uint32_t split;                  // the split build (planning, front and emission kernels)
     unsigned long long* tinfo;
     unsigned long long* tile_sum;    // zero at launch; re-zeroed by the emission kernel's last CTA
     unsigned long long* stage_at;
@@ -191,15 +211,18 @@ struct BuildArgs {
     uint32_t* split_queue;           // planned: kPlanRanks work queues of n * pmax entries
     uint32_t* split_ctr;             // kCtrWords counters, zero at launch (kCtr*)
     uint32_t split_planned;          // the planning kernel runs first and fills the queues
+    uint32_t split_decide;           // ... and settles the chunks the depth bias decides (else queues every chunk)
+    uint32_t* stage_eids;            // staging: per vertex its edge id (when edge_ids is set)
     uint32_t mask_offset;            // nonzero: per-column below-iso masks at dyn smem + mask_offset
     const uint2* tables;             // optional: the marching-cubes table image (table_image_kernel)
-    // Slabs (chunks above piece_cells cells per edge, planned split build
-    // only): a chunk has pmax piece places p = c * pmax + s.  Per place its
-    // counts (pinfo: verts | inds << 32), its staging place (stage_at[p]),
-    // its slot (slots + p * slot_bytes) and the seam it leaves its successor
-    // (seam + p * seam_stride words: per cell (y, z) of its last layer, the
-    // cell's first vertex id within the slab | case << 16).  pmax == 1: no
-    // slabs; every place is a chunk.
+    // Slabs (chunks above piece_cells cells per edge, split build): a chunk
+    // has pmax piece places p = c * pmax + s.  Per place its counts (pinfo:
+    // verts | inds << 32), its staging place (stage_at[p]) and the seam it
+    // leaves its successor (seam + p * seam_stride words: per cell (y, z) of
+    // its last layer, the cell's first vertex id within the slab | case <<
+    // 16); a slab built again by the emission kernel works in scratch +
+    // blockIdx.x * scratch_slot_bytes.  pmax == 1: no slabs; every place is a
+    // chunk.
     uint32_t pmax;
     uint32_t piece_cells;
     unsigned long long* pinfo;
