@@ -1269,6 +1269,7 @@ struct SlabWs {
     uint8_t* cases;               // per cell of the slab (active cells only)
     uint16_t* vbase;              // per active cell: first vertex id within the slab
     unsigned long long* masks;    // per sample column (x - x0, y): bits z with sample < iso
+    uint32_t* alist;              // active cells in order: cell | first triangle << 16 (up to kSlabActCap)
 };
 
 __device__ __forceinline__ SlabWs slab_ws(uint8_t* base, int N)
@@ -1279,6 +1280,7 @@ __device__ __forceinline__ SlabWs slab_ws(uint8_t* base, int N)
     w.cases = base + L.cases;
     w.vbase = reinterpret_cast<uint16_t*>(base + L.vbase);
     w.masks = reinterpret_cast<unsigned long long*>(base + L.masks);
+    w.alist = reinterpret_cast<uint32_t*>(base + L.alist);
     return w;
 }
 
@@ -1427,6 +1429,9 @@ __device__ unsigned long long slab_front(const DevParams& p, const BuildArgs& a,
             const int z = __ffsll((long long)act) - 1;
             const int cs = W.cases[q * N + z];
             W.vbase[q * N + z] = (uint16_t)(r & kField22);
+            const uint32_t ar = (uint32_t)(r >> kActShift);
+            if (ar < kSlabActCap)
+                W.alist[ar] = (uint32_t)(q * N + z) | ((uint32_t)((r >> kIndShift) & kField22) / 3u) << 16;
             if (seam && x == x1 - 1) seam[y * N + z] = (uint32_t)(r & 0xffffu) | ((uint32_t)cs << 16);
             r += cell_counts(T, cs, T.owned[oriented][own_lo | ((z == 0) << 2) | ((z == N - 1) << 5)]);
         }
@@ -1460,9 +1465,9 @@ __device__ __forceinline__ uint32_t seam_vertex(const BuildArgs& a, const SmemTa
 // follows (carry).
 template <class O, bool FINAL>
 __device__ void slab_emit(const DevParams& p, const BuildArgs& a, const SmemTables& T, const SlabWs W,
-                          const uww_chunk_desc d, uint32_t c, uint32_t s, unsigned long long run, int ncomp,
-                          const EmitOut& eo, uint32_t voff, uint32_t ioff, uint32_t vbase0, uint32_t prev_base,
-                          bool carry)
+                          const uww_chunk_desc d, uint32_t c, uint32_t s, unsigned long long run,
+                          unsigned long long total, int ncomp, const EmitOut& eo, uint32_t voff, uint32_t ioff,
+                          uint32_t vbase0, uint32_t prev_base, bool carry)
 {
     const int tid = threadIdx.x;
     const int oriented = p.dedup_mode == UWW_DEDUP_ORIENTED;
@@ -1471,60 +1476,75 @@ __device__ void slab_emit(const DevParams& p, const BuildArgs& a, const SmemTabl
     const int ox = d.pos[0] * p.chunk_size, oy = d.pos[1] * p.chunk_size, oz = d.pos[2] * p.chunk_size;
     const float sc = __fdiv_rn((float)p.chunk_size, (float)N);
     const uint32_t* seam_prev = s > 0 ? a.seam + ((size_t)c * a.pmax + s - 1) * a.seam_stride : nullptr;
+    // active cell (xl, y, z) of the slab (index cell, case cs, first vertex
+    // vb and first index position ir within the slab): its triangles
+    auto emit_cell = [&](int xl, int y, int z, int cell, int cs, uint32_t vb, uint32_t ir) {
+        const int x = x0 + xl;
+        const unsigned own = T.owned[oriented][boundary_flags(x, y, z, N)];
+        const int nt = T.ntri[cs];
+        const int8_t* row = T.tri[cs];
+        const unsigned fr = T.first_ref[cs];
+        const uint16_t* before = UWW_EDGE_BEFORE[cs];
+        const int lo = (x == 0) | ((y == 0) << 1) | ((z == 0) << 2);
+        for (int i = 0; i < 3 * nt; ++i) {
+            const int e = row[i];
+            uint32_t id;
+            if ((own >> e) & 1u) {
+                // the cell numbers its owned edges' vertices in first-reference order
+                id = vb + __popc(own & __ldg(before + e));
+                if ((fr >> i) & 1u) {
+                    const EdgeVertex ev = edge_vertex<O>(p, T, W.rho, S, x, y, z, e, sc, ox, oy, oz, x0);
+                    if (eo.edge_ids) eo.edge_ids[voff + id] = ev.edge_id;
+                    if (FINAL) {
+                        float2* v2 = reinterpret_cast<float2*>(eo.verts + voff + id);
+                        v2[0] = make_float2(ev.x, ev.y);
+                        v2[1] = make_float2(ev.z, carry ? (float)ev.cb : 0.f);
+                        v2[2] = make_float2(0.f, 0.f);
+                    } else {
+                        eo.pos[voff + id] = make_float4(ev.x, ev.y, ev.z, (float)ev.cb);
+                    }
+                }
+                if (FINAL) id += vbase0;
+            } else {
+                // the owner: the first cell in stream order holding this edge
+                const int ow = T.owner[oriented][lo][e];
+                const int qx = x - ((ow >> 4) & 1), qy = y - ((ow >> 5) & 1), qz = z - ((ow >> 6) & 1);
+                const int oe = ow & 15;
+                if (qx < x0) {
+                    id = FINAL ? seam_vertex(a, T, oriented, N, seam_prev, x0, qy, qz, oe, prev_base)
+                               : kCrossRef | ((uint32_t)oe << 24) | (uint32_t)(qy * N + qz);
+                } else {
+                    const int oc = ((qx - x0) * N + qy) * N + qz;
+                    const unsigned oown = T.owned[oriented][boundary_flags(qx, qy, qz, N)];
+                    id = (uint32_t)W.vbase[oc] + __popc(oown & __ldg(&UWW_EDGE_BEFORE[W.cases[oc]][oe]));
+                    if (FINAL) id += vbase0;
+                }
+            }
+            eo.inds[ioff + ir + i] = id;
+        }
+    };
+    const uint32_t nA = (uint32_t)(total >> kActShift);
+    if (nA <= kSlabActCap) {
+        // a thread per active cell, from the list the scan filled
+        for (uint32_t k = tid; k < nA; k += ncomp) {
+            const uint32_t en = W.alist[k];
+            const int cell = (int)(en & 0xffffu), q = cell / N, z = cell - q * N, xl = q / N;
+            emit_cell(xl, q - xl * N, z, cell, W.cases[cell], W.vbase[cell], 3u * (en >> 16));
+        }
+        return;
+    }
+    // (more active cells than the list holds) each thread its run of columns
     const int ncol = nl * N, R = (ncol + ncomp - 1) / ncomp;
     const int q0 = min(tid * R, ncol), q1 = min(q0 + R, ncol);
     unsigned long long r = run;
     for (int q = q0; q < q1; ++q) {
-        const int xl = q / N, y = q - xl * N, x = x0 + xl;
+        const int xl = q / N, y = q - xl * N;
         const SlabColumn col = slab_column(W.masks, S, xl, y, N);
-        const unsigned own_lo = (x == 0) | ((y == 0) << 1) | ((x == N - 1) << 3) | ((y == N - 1) << 4);
         for (unsigned long long act = col.act; act; act &= act - 1ull) {
             const int z = __ffsll((long long)act) - 1;
             const int cs = W.cases[q * N + z];
-            const unsigned own = T.owned[oriented][own_lo | ((z == 0) << 2) | ((z == N - 1) << 5)];
-            const int nt = T.ntri[cs];
-            const uint32_t vb = (uint32_t)(r & kField22), ir = (uint32_t)((r >> kIndShift) & kField22);
-            const int8_t* row = T.tri[cs];
-            const unsigned fr = T.first_ref[cs];
-            const uint16_t* before = UWW_EDGE_BEFORE[cs];
-            const int lo = (x == 0) | ((y == 0) << 1) | ((z == 0) << 2);
-            for (int i = 0; i < 3 * nt; ++i) {
-                const int e = row[i];
-                uint32_t id;
-                if ((own >> e) & 1u) {
-                    // the cell numbers its owned edges' vertices in first-reference order
-                    id = vb + __popc(own & __ldg(before + e));
-                    if ((fr >> i) & 1u) {
-                        const EdgeVertex ev = edge_vertex<O>(p, T, W.rho, S, x, y, z, e, sc, ox, oy, oz, x0);
-                        if (eo.edge_ids) eo.edge_ids[voff + id] = ev.edge_id;
-                        if (FINAL) {
-                            float2* v2 = reinterpret_cast<float2*>(eo.verts + voff + id);
-                            v2[0] = make_float2(ev.x, ev.y);
-                            v2[1] = make_float2(ev.z, carry ? (float)ev.cb : 0.f);
-                            v2[2] = make_float2(0.f, 0.f);
-                        } else {
-                            eo.pos[voff + id] = make_float4(ev.x, ev.y, ev.z, (float)ev.cb);
-                        }
-                    }
-                    if (FINAL) id += vbase0;
-                } else {
-                    // the owner: the first cell in stream order holding this edge
-                    const int ow = T.owner[oriented][lo][e];
-                    const int qx = x - ((ow >> 4) & 1), qy = y - ((ow >> 5) & 1), qz = z - ((ow >> 6) & 1);
-                    const int oe = ow & 15;
-                    if (qx < x0) {
-                        id = FINAL ? seam_vertex(a, T, oriented, N, seam_prev, x0, qy, qz, oe, prev_base)
-                                   : kCrossRef | ((uint32_t)oe << 24) | (uint32_t)(qy * N + qz);
-                    } else {
-                        const int oc = ((qx - x0) * N + qy) * N + qz;
-                        const unsigned oown = T.owned[oriented][boundary_flags(qx, qy, qz, N)];
-                        id = (uint32_t)W.vbase[oc] + __popc(oown & __ldg(&UWW_EDGE_BEFORE[W.cases[oc]][oe]));
-                        if (FINAL) id += vbase0;
-                    }
-                }
-                eo.inds[ioff + ir + i] = id;
-            }
-            r += cell_counts(T, cs, own);
+            emit_cell(xl, y, z, q * N + z, cs, (uint32_t)(r & kField22), (uint32_t)((r >> kIndShift) & kField22));
+            r += cell_counts(T, cs, T.owned[oriented][boundary_flags(x0 + xl, y, z, N)]);
         }
     }
 }
@@ -1628,7 +1648,8 @@ __device__ void front_slab(const DevParams& p, const BuildArgs& a, SmemTables& T
     const unsigned long long st = stage;
     if (st != kUnstaged) {
         const EmitOut eo{nullptr, a.stage_inds, a.edge_ids ? a.stage_eids : nullptr, a.stage_pos};
-        slab_emit<O, false>(p, a, T, W, d, c, sl, run, nthr, eo, (uint32_t)st, (uint32_t)(st >> 32), 0u, 0u, true);
+        slab_emit<O, false>(p, a, T, W, d, c, sl, run, tot, nthr, eo, (uint32_t)st, (uint32_t)(st >> 32), 0u, 0u,
+                            true);
         for (uint32_t k = tid; k < vb; k += nthr)
             if (unit_a + k < a.unit_cap) a.units[unit_a + k] = unit_entry(c, k | (sl << 16), kUnitVerts | kUnitSlab);
         for (uint32_t k = tid; k < ib; k += nthr)
@@ -1791,10 +1812,11 @@ __device__ __noinline__ void emit_slab_again(const DevParams& p, const BuildArgs
     const SlabWs W = slab_ws(a.scratch + (size_t)blockIdx.x * a.scratch_slot_bytes, (int)d.cells);
     int any_inside = 0;
     unsigned long long run = 0ull;
-    slab_front<O, true>(p, a, T, W, dyn_smem, d, c, sl, nthr, false, &any_inside, &run);
+    const unsigned long long total = slab_front<O, true>(p, a, T, W, dyn_smem, d, c, sl, nthr, false, &any_inside, &run);
     __syncthreads();
     const EmitOut eo{a.verts, a.inds, a.edge_ids, nullptr};
-    slab_emit<O, true>(p, a, T, W, d, c, sl, run, nthr, eo, voff, ioff, vbase0, prev_base, want_color || want_normals);
+    slab_emit<O, true>(p, a, T, W, d, c, sl, run, total, nthr, eo, voff, ioff, vbase0, prev_base,
+                       want_color || want_normals);
     if (want_color || want_normals) {
         __syncthreads();  // the slab's vertex positions, written by this CTA
         for (uint32_t v = tid; v < nv; v += nthr)

@@ -48,17 +48,19 @@ __host__ __device__ inline ChunkLayout chunk_layout(int N)
 // slab order -- one CTA of kSlabThreads threads per slab.  A slab's shared
 // workspace: the samples of its K+1 x planes, per sample column its
 // below-iso bits, per cell its case and (active cells) its first vertex id
-// within the slab.  K is
+// within the slab, and the list of its active cells (up to kSlabActCap:
+// cell | first triangle << 16) that spreads pass 1 over the CTA.  K is
 // the largest layer count whose sample columns ((K+1) * S) fit one pass of the
 // CTA's threads, whose workspace fits kSlabBudget bytes, and whose vertices fit
 // 16-bit ids (every edge of the slab's cells, counted once).
 constexpr int kSlabThreads = 256;
-constexpr uint32_t kSlabBudget = 80 * 1024;
+constexpr uint32_t kSlabBudget = 96 * 1024;
+constexpr uint32_t kSlabActCap = 2048;
 constexpr int kSlabMaxCells = 63;     // a sample column's bits fit one 64-bit mask
 constexpr uint32_t kPieceShift = 24;  // queue entry: chunk | slab << kPieceShift
 
 struct SlabLayout {
-    uint32_t rho, cases, vbase, masks, total;
+    uint32_t rho, cases, vbase, masks, alist, total;
     int K;
 };
 
@@ -72,6 +74,7 @@ __host__ __device__ inline SlabLayout slab_layout_k(int N, int K)
     L.cases = o;  o = align16(o + NC);
     L.vbase = o;  o = align16(o + NC * 2u);
     L.masks = o;  o = align16(o + (uint32_t)(K + 1) * S * 8u);
+    L.alist = o;  o = align16(o + kSlabActCap * 4u);
     L.total = o;
     return L;
 }
