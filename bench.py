@@ -57,10 +57,10 @@ FLOPS_PER_VERTEX_EXTRA = 60    # interpolation, colour ramp, normalisation
 # the step's dominant kernel, front_kernel, on this workload, from a
 # single-kernel ncu capture of this script's own step (-k regex:front_kernel
 # -s 12 -c 1 of `bench.py --steps 5 --warmup 3 --quick --no-cpu
-# --clock-window 0`, caches flushed before the launch): 182.8 KB read, 0
-# written.  Its staged output stays in L2 for the emission kernel, so this is
+# --clock-window 0`, caches flushed before the launch): 186.4 KB read,
+# 0.3 KB written.  Its staged output stays in L2 for the emission kernel, so this is
 # far below the algorithmic output bytes.
-NCU_DRAM_BYTES_PER_LAUNCH = 182_784
+NCU_DRAM_BYTES_PER_LAUNCH = 186_624
 NCU_TRAFFIC_SOURCE = ("ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum -k regex:front_kernel -s 12 -c 1, "
                       "python bench.py --steps 5 --warmup 3 --quick --no-cpu --clock-window 0")
 # FP32 flops the noise-stage kernel executes per launch of this workload
