@@ -129,3 +129,28 @@ def test_autotune_picks_caches_and_reuses(ctx_factory, tmp_path):
     assert (t2.threads, t2.blocks_per_sm, t2.smem_cells) == (t1.threads, t1.blocks_per_sm, t1.smem_cells)
     assert us2 == pytest.approx(us1, rel=1e-3)
     assert len(cache.read_text().splitlines()) == 1
+
+
+def test_frame_graph_with_slabs_matches_direct_builds(ctx_factory):
+    """The uneven-LOD world (24^3 and 48^3 chunks built as slabs) through a
+    captured frame graph, with frames of different sizes read from the device
+    count: the same records and mesh as direct builds."""
+    p, d = workloads.mixed_lod(seed=4, outputs=OUT)
+    p.math_mode = abi.UWW_MATH_FAST
+    ctx = ctx_factory(p)
+    assert ctx.launch_shape(len(d), 48).slabs_per_chunk > 1
+    vcap, icap = 1 << 20, 1 << 22
+    fb = FrameBuilder(ctx, len(d), 48, vcap, icap)
+    rng = np.random.default_rng(1)
+    for n in (len(d), 700, 3):
+        idx = rng.permutation(len(d))[:n]
+        sel = make_descs(d["pos"][idx], d["cells"][idx])
+        rec, tot = fb.build(sel)
+        want = direct_build(ctx, sel, vcap, icap)
+        np.testing.assert_array_equal(tot[:3], want.totals[:3])
+        np.testing.assert_array_equal(rec, want.records)
+        verts, norms, inds = fb.mesh(int(tot[0]), int(tot[1]))
+        np.testing.assert_array_equal(inds, want.inds)
+        np.testing.assert_array_equal(verts, want.verts)
+        np.testing.assert_array_equal(norms, want.normals)
+    fb.close()
