@@ -418,22 +418,24 @@ int launch(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint32_t ma
             a.pmax = (uint32_t)pm;
             a.piece_cells = 16;
             if (pm > 1) {
-                // per place its counts and its seam (rewritten by every
-                // launch), and the emission CTAs' scratch for slabs built again
+                // per place its counts and its seam (rewritten by every launch)
                 const size_t pinfo_bytes = ((size_t)n * pm * 8 + 15) & ~size_t(15);
                 a.seam_stride = max_cells * max_cells;
                 if ((st = grow(&ctx->d_slab, &ctx->slab_cap, pinfo_bytes + (size_t)n * pm * a.seam_stride * 4)))
                     return st;
                 a.pinfo = reinterpret_cast<unsigned long long*>(ctx->d_slab);
                 a.seam = reinterpret_cast<uint32_t*>(ctx->d_slab + pinfo_bytes);
-                int egrid = 0;
-                size_t edyn = 0;
-                cudaError_t e = split_emit_shape(ctx->dev, a, &egrid, &edyn);
-                if (e != cudaSuccess) return cuda_status(e);
-                if ((st = grow(&ctx->d_scratch, &ctx->scratch_cap, cfg.slab_slot * (size_t)egrid))) return st;
-                a.scratch = ctx->d_scratch;
-                a.scratch_slot_bytes = cfg.slab_slot;
             }
+            // the emission CTAs' scratch slots, for chunks and slabs built
+            // again (their output found no staging room)
+            int egrid = 0;
+            size_t edyn = 0;
+            cudaError_t e = split_emit_shape(ctx->dev, a, &egrid, &edyn);
+            if (e != cudaSuccess) return cuda_status(e);
+            const size_t eslot = std::max(cfg.slab_slot, (size_t)align16(chunk_layout((int)cfg.smem_cells).total));
+            if ((st = grow(&ctx->d_scratch, &ctx->scratch_cap, eslot * (size_t)egrid))) return st;
+            a.scratch = ctx->d_scratch;
+            a.scratch_slot_bytes = eslot;
             // staging as large as the outputs (a batch whose output fits its
             // capacities is always staged whole), and the emission units:
             // at most one vertex block per kVertexBlock vertices plus one per

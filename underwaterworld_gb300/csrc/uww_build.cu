@@ -1825,10 +1825,10 @@ __device__ __noinline__ void emit_slab_again(const DevParams& p, const BuildArgs
 }
 
 // The emission kernel's work on a whole chunk the staging buffers had no
-// room for: its front half again in this CTA's dynamic shared memory (laid
-// out by rebuild_layout; its cases and samples are the front kernel's), then
-// pass 1 into the outputs at its record's offsets and pass 2.  Kept out of
-// line, like emit_slab_again.
+// room for: its front half again in this CTA's global scratch slot (shared
+// memory as rebuild_layout says; its cases and samples are the front
+// kernel's), then pass 1 into the outputs at its record's offsets and pass 2.
+// Kept out of line, like emit_slab_again.
 template <class O>
 __device__ __noinline__ void emit_chunk_again(const DevParams& p, const BuildArgs& a, SmemTables& T, uint8_t* dyn_smem,
                                               uint32_t c, const uww_chunk_record rec)
@@ -1839,11 +1839,15 @@ __device__ __noinline__ void emit_chunk_again(const DevParams& p, const BuildArg
     BuildArgs b = a;
     b.cases = nullptr;
     b.samples_out = nullptr;
-    b.smem_buf_bytes = chunk_layout((int)a.smem_cells).total;
-    size_t zt = 0, mo = 0;
-    rebuild_layout((int)a.smem_cells, (int)p.octaves, std::is_same<O, FastOps>::value, a.mask_offset != 0, &zt, &mo);
+    // every chunk in the scratch slot: the masks at the start of the dynamic
+    // shared memory, the z tables after them
+    size_t zt = 0;
+    rebuild_layout((int)a.smem_cells, (int)p.octaves, std::is_same<O, FastOps>::value, &zt);
+    b.smem_cells = 0;
+    b.slots_per_cta = 1;
+    b.smem_buf_bytes = zt;
     b.ztable_offset = zt;
-    b.mask_offset = (uint32_t)mo;
+    b.mask_offset = 0;
     const uww_chunk_desc d = a.chunks[c];
     chunk_front<O, false>(p, b, T, dyn_smem, d, c, c, 0, nthr);
     __syncthreads();
@@ -2305,12 +2309,12 @@ cudaError_t front_occupancy(bool exact, int threads, size_t dyn_smem, int* block
 cudaError_t split_emit_shape(const DevParams& p, const BuildArgs& a, int* grid, size_t* dyn_smem)
 {
     int sms = 0, ebps = 0;
-    // dynamic shared memory: a whole chunk built again (chunks without
-    // staging room), a gathered vertex block (9 words a vertex) or the z
+    // dynamic shared memory: a gathered vertex block (9 words a vertex),
+    // the masks and z tables of a whole chunk built again (chunks without
+    // staging room; its workspace is in the CTA's scratch slot) or the z
     // tables of a slab built again, the largest
-    size_t zt = 0, mo = 0;
-    size_t edyn = std::max(rebuild_layout((int)a.smem_cells, (int)p.octaves, p.math_mode != UWW_MATH_EXACT,
-                                          a.mask_offset != 0, &zt, &mo),
+    size_t zt = 0;
+    size_t edyn = std::max(rebuild_layout((int)a.smem_cells, (int)p.octaves, p.math_mode != UWW_MATH_EXACT, &zt),
                            (size_t)kVertexBlock * 9 * sizeof(float));
     if (a.pmax > 1) edyn = std::max(edyn, ztable_bytes((int)a.max_cells + 1, (int)p.octaves));
     const cudaError_t e = occupancy_of((const void*)emit_for(p.math_mode == UWW_MATH_EXACT), 256, edyn, &ebps, &sms);

@@ -108,23 +108,15 @@ __host__ __device__ inline size_t ztable_bytes(int S, int octaves)
 }
 
 // The split build's emission kernel builds a whole chunk again (one the
-// staging buffers had no room for) in its dynamic shared memory laid out
-// like the front kernel's, sized for chunks of up to smem_cells: the
-// workspace, the z tables (fast build) at *zt_off, the 13^3 column masks (when
-// the front kernel keeps them) at *mask_off; returns the bytes.
-__host__ __device__ inline size_t rebuild_layout(int smem_cells, int octaves, bool fast, bool masks, size_t* zt_off,
-                                                 size_t* mask_off)
+// staging buffers had no room for, of up to `cells` cells per edge) with its
+// workspace in the CTA's global scratch slot; its dynamic shared memory holds
+// (fast build) the chunk's column masks and, at *zt_off, its z tables.
+// Returns those bytes.
+__host__ __device__ inline size_t rebuild_layout(int cells, int octaves, bool fast, size_t* zt_off)
 {
-    size_t o = chunk_layout(smem_cells).total;
-    *zt_off = o;
-    if (fast) o += ztable_bytes(smem_cells + 1, octaves);
-    *mask_off = 0;
-    if (masks) {
-        o = (o + 15) & ~size_t(15);
-        *mask_off = o;
-        o += 13 * 13 * sizeof(unsigned long long);
-    }
-    return o;
+    const size_t S = (size_t)cells + 1;
+    *zt_off = fast ? ((S * S * 8 + 15) & ~size_t(15)) : 0;
+    return fast ? *zt_off + ztable_bytes((int)S, octaves) : 0;
 }
 
 // Plan buffer of a planned batched build of n chunks: u32 [0] the planning
