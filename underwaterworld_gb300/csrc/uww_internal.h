@@ -173,7 +173,7 @@ struct BuildArgs {
     unsigned long long* lookback;    // n words, zero at launch; the last CTA re-zeroes them (queue mode)
     unsigned int* work_counter;      // zero at launch; reset by the last CTA (queue mode)
     unsigned long long* acc;         // [0] overflow count, [1] error flags, [2] CTAs finished (queue mode)
-    uint8_t* scratch;                // per-CTA slots for chunks above smem_cells
+    uint8_t* scratch;                // per-CTA slots: chunks above smem_cells (pipelined), rebuilds (split emission)
     size_t scratch_slot_bytes;
     uint32_t slots_per_cta;          // workspaces per CTA (2 in the pipelined batched form)
     size_t smem_buf_bytes;           // bytes of one shared-memory workspace
@@ -331,7 +331,7 @@ struct uww_ctx {
     uint32_t* d_plan = nullptr;   // planned batch: chunk count + list
     size_t plan_cap = 0;
     void* d_tables = nullptr;     // the marching-cubes table image (launch_table_image)
-    uint8_t* d_split = nullptr;   // split build: counters, tile sums, counts, queues, slots
+    uint8_t* d_split = nullptr;   // split build: counters, tile sums, counts, staging places, queues
     uint8_t* d_stage = nullptr;   // split build: staging buffers and emission units
     uint8_t* d_slab = nullptr;    // split build with slabs: per place its counts, then its seam
     size_t slab_cap = 0;
