@@ -28,7 +28,7 @@ import pytest
 from underwaterworld_gb300 import abi, workloads
 from underwaterworld_gb300.chunk import DeviceArray, totals_status
 
-from helpers import assert_batches_equal
+from helpers import assert_batches_equal, relayout
 
 pytestmark = pytest.mark.gpu
 
@@ -118,8 +118,17 @@ def test_spin_limit_and_test_flags_are_validated(ctx_factory):
     assert (t.threads, t.spin_limit, t.test_flags) == (160, 5000, 0)
 
 
-def test_withheld_records_time_out_and_the_context_recovers(ctx_factory, oracle):
-    p, d = workloads.uniform_grid(seed=4, outputs=abi.UWW_OUT_COLOR | abi.UWW_OUT_NORMALS)
+@pytest.mark.parametrize("world", ["uniform", "slabs"])
+def test_withheld_records_time_out_and_the_context_recovers(ctx_factory, oracle, world):
+    """The split build's records wait runs out (records withheld): whole chunks
+    on the uniform grid, and a batch of the uneven-LOD world whose 24^3 and
+    48^3 chunks are built as slabs."""
+    if world == "uniform":
+        p, d = workloads.uniform_grid(seed=4, outputs=abi.UWW_OUT_COLOR | abi.UWW_OUT_NORMALS)
+    else:
+        p, d = workloads.mixed_lod(seed=4, outputs=abi.UWW_OUT_COLOR | abi.UWW_OUT_NORMALS)
+        d = relayout(d[:384])
+    max_cells = int(d["cells"].max())
     p.math_mode = abi.UWW_MATH_FAST
     n = len(d)
     ref = oracle.build_chunks(p, d, precision=oracle.F32, threads=8)
@@ -136,8 +145,10 @@ def test_withheld_records_time_out_and_the_context_recovers(ctx_factory, oracle)
     out = abi.MeshOut(bufs["verts"].ptr, bufs["normals"].ptr, bufs["inds"].ptr, None, None, bufs["records"].ptr,
                       bufs["totals"].ptr, vcap, icap, 0, 0)
 
+    if world == "slabs":
+        assert ctx.launch_shape(n, max_cells).slabs_per_chunk > 1
     set_tuning(ctx, SHORT_SPIN, abi.UWW_TEST_WITHHOLD_RECORDS)
-    abi.check(abi.lib().uww_build_chunks(ctx.h, C.c_void_p(d_desc.ptr), n, 12, C.byref(out)), "launch")
+    abi.check(abi.lib().uww_build_chunks(ctx.h, C.c_void_p(d_desc.ptr), n, max_cells, C.byref(out)), "launch")
     ctx.sync()  # the launch ended by itself
     tot = ctx.download(bufs["totals"], (4,), np.uint64)
     assert totals_status(tot) == abi.UWW_ERR_TIMEOUT, tot
