@@ -172,3 +172,45 @@ def test_forward_with_edge_ids_matches_the_pipelined_build(ctx_factory, cells):
     for k in ("totals", "records", "edge_ids", "cases"):
         np.testing.assert_array_equal(split[k], piped[k], err_msg=k)
     np.testing.assert_array_equal(split["verts"].view(np.uint32), piped["verts"].view(np.uint32))
+
+
+@pytest.mark.parametrize("shift", [0, 4])
+def test_host_buffers_with_slabs(ctx_factory, shift):
+    """uww_build_chunks_host into page-locked buffers on an uneven-LOD batch
+    (slabs): the emission's direct stores (aligned buffers) or the sized copy
+    (buffers shifted by 4 bytes) give the device build's records, vertices,
+    normals and indices."""
+    import ctypes as C
+    from underwaterworld_gb300.chunk import HostArray
+    p, d = workloads.mixed_lod(seed=6, outputs=COLOR_NORMALS)
+    p.math_mode = abi.UWW_MATH_FAST
+    d = relayout(d[:512])
+    ctx = ctx_factory(p)
+    want = ctx.build_chunks_device(d, 1 << 20, 1 << 22)
+    assert want.status == abi.UWW_OK
+    n = len(d)
+    vcap, icap = int(want.totals[0]) + 3, int(want.totals[1]) + 5
+    keep = []
+
+    def host(shape, dtype):
+        dtype = np.dtype(dtype)
+        nbytes = int(np.prod(shape)) * dtype.itemsize
+        h = HostArray((nbytes + 16,), np.uint8)
+        keep.append(h)
+        return h.ptr + shift, h.array[shift:shift + nbytes].view(dtype).reshape(shape)
+
+    pv, hv = host((vcap,), abi.VERT_COLOR_DTYPE)
+    pn, hn = host((vcap, 3), np.float32)
+    pi, hi = host((icap,), np.uint32)
+    pr, hr = host((n,), abi.CHUNK_RECORD_DTYPE)
+    tot = np.zeros(4, np.uint64)
+    out = abi.MeshOut(pv, pn, pi, None, None, pr, tot.ctypes.data, vcap, icap, 0, 0)
+    h_desc = HostArray((n,), abi.CHUNK_DESC_DTYPE)
+    h_desc.array[:] = d
+    abi.check(abi.lib().uww_build_chunks_host(ctx.h, C.c_void_p(h_desc.ptr), n, C.byref(out)), "host build")
+    nv, ni = int(tot[0]), int(tot[1])
+    np.testing.assert_array_equal(tot[:3], want.totals[:3])
+    np.testing.assert_array_equal(hr, want.records)
+    np.testing.assert_array_equal(hv[:nv].view(np.uint32), want.verts.view(np.uint32))
+    np.testing.assert_array_equal(hn[:nv].view(np.uint32), want.normals.view(np.uint32))
+    np.testing.assert_array_equal(hi[:ni], want.inds)
