@@ -1571,18 +1571,23 @@ __global__ void __launch_bounds__(kPlanThreads) split_plan_kernel(const DevParam
         if (kind) {
             a.tinfo[i] = decided_info(kind);
         } else if (ok && slab_chunk(a, cells)) {
-            // a chunk built as slabs: every slab queued (first, as the
-            // largest pieces of work); its counts word starts at zero counts
-            // and early blank, and each slab adds its counts and clears the
-            // flag when one of its samples is not above the iso level
+            // a chunk built as slabs: every slab queued first, as the
+            // largest pieces of work (those of chunks above 32 cells, the
+            // longest, in queue 0; the rest in queue 1); its counts word
+            // starts at zero counts and early blank, and each slab adds its
+            // counts and clears the flag when one of its samples is not above
+            // the iso level
             const uint32_t np = (uint32_t)slab_count((int)cells), qcap = a.n * a.pmax;
+            const uint32_t q = cells > 32 ? 0u : 1u;
             a.tinfo[i] = kInfoEarlyBlank;
-            const uint32_t pos = atomicAdd(&a.split_ctr[kCtrQueued], np);
+            const uint32_t pos = atomicAdd(&a.split_ctr[kCtrQueued + q], np);
             for (uint32_t sl = 0; sl < np; ++sl)
-                if (pos + sl < qcap) a.split_queue[pos + sl] = i | (sl << kPieceShift);
+                if (pos + sl < qcap) a.split_queue[(size_t)q * qcap + pos + sl] = i | (sl << kPieceShift);
         } else {
             // (the counters are zero at launch, so pos < n * pmax; checked all the same)
             const uint32_t qcap = a.n * a.pmax;
+            // with slabs, whole chunks queue after them (queues 2..)
+            if (a.pmax > 1) rank = min(rank + 2, kPlanRanks - 1);
             const uint32_t pos = atomicAdd(&a.split_ctr[kCtrQueued + rank], 1u);
             if (pos < qcap) a.split_queue[(size_t)rank * qcap + pos] = i;
         }
