@@ -363,6 +363,228 @@ __device__ __forceinline__ int sample_columns_reg(const DevParams& p, const uint
     return inside | (outside << 1);
 }
 
+// Settling a chunk early.  After the first octaves a chunk whose every
+// partial sum stays above (below) the iso level by more than the remaining
+// octaves can reach is blank (solid) whatever they add: its other octaves are
+// not needed (its samples are not kept, so callers that write samples do not
+// settle early).  The reach is kPerlinBound |norm| sum_{k' > k} |amp_k'| (see
+// fbm_bound) and the margin covers f32 rounding as in bias_decides_with.
+// Checked after octaves 0 .. kSettleChecks-1.
+constexpr int kSettleChecks = 2;
+
+__device__ __forceinline__ float fbm_reach_after(const DevParams& p, int k)
+{
+    float sa = 0.f;
+    for (int j = k + 1; j < p.octaves; ++j) sa = __fadd_rn(sa, fabsf(p.amp[j]));
+    return __fmul_rn(__fmul_rn(kPerlinBound, fabsf(fbm_norm(p))), sa);
+}
+
+// bit 0: partial sum v stays above the iso level whatever the reach R adds;
+// bit 1: it stays below
+__device__ __forceinline__ unsigned settled_bits(float v, float R, float iso)
+{
+    const float m = __fmul_rn(1.0e-3f, __fadd_rn(__fadd_rn(1.f, R), fabsf(v)));
+    return (__fsub_rn(__fsub_rn(v, R), m) > iso ? 1u : 0u) | (__fadd_rn(__fadd_rn(v, R), m) < iso ? 2u : 0u);
+}
+
+// sample_columns_reg for at most one column per compute thread (S * S <=
+// ncomp), settling the chunk early when it can: then it writes neither rho
+// nor masks and returns the votes of a blank (2: a sample not below) or a
+// solid (1: a sample not above) chunk.  Otherwise the same samples, masks and
+// votes as sample_columns_reg.  Every compute thread must call it.
+template <int S>
+__device__ __forceinline__ int sample_columns_reg_settle(const DevParams& p, const uint8_t* __restrict__ P,
+                                                         const float4* __restrict__ gp, const ZTable Z,
+                                                         float* __restrict__ rho, int ox, int oy, int oz, int ncomp,
+                                                         unsigned long long* masks = nullptr)
+{
+    constexpr int SS = S * S;
+    const int K = p.octaves;
+    const float s = __fdiv_rn((float)p.chunk_size, (float)(S - 1));
+    const float bf = p.base_freq;
+    const float norm = fbm_norm(p);
+    const float zoff = __fadd_rn((float)oz, p.offset[2]);
+    const float iso = p.iso_level;
+    ztable_warps(p, Z, S, s, zoff, oz, ncomp);
+    bar_sync(kBarCompute, ncomp);
+
+    const int col = threadIdx.x;
+    const bool has = col < SS;
+    const int x = has ? col / S : 0, y = has ? col - x * S : 0;
+    const float nx = column_coord((float)x, s, ox, p.offset[0], bf);
+    const float ny = column_coord((float)y, s, oy, p.offset[1], bf);
+    float acc[S];
+#pragma unroll
+    for (int z = 0; z < S; ++z) acc[z] = Z.bias[z];
+    for (int k = 0; k < K; ++k) {
+        if (has) {
+            const ColumnOctave co = column_octave(p, P, nx, ny, k, norm);
+            const unsigned rm = Z.rmask[k];
+            const int2* runs = Z.runs + k * S;
+            const float2* dzc = Z.dzc + k * S;
+            float SA0 = 0.f, SG0 = 0.f, SA1 = 0.f, SG1 = 0.f;
+            RunPoly q = {0.f, 0.f, 0.f, 0.f};
+            int prev = 0, r = 0;
+#pragma unroll
+            for (int z = 0; z < S; ++z) {
+                if (rm & (1u << z)) {  // the same for every column
+                    const int c = runs[r++].y;
+                    if (z > 0 && c == prev + 1) {
+                        SA0 = SA1;
+                        SG0 = SG1;
+                    } else {
+                        column_face(co, gp, c & 255, SA0, SG0);
+                    }
+                    column_face(co, gp, (c + 1) & 255, SA1, SG1);
+                    prev = c;
+                    q = run_poly(SA0, SG0, SA1, SG1);
+                }
+                acc[z] = __fadd_rn(run_value(q, dzc[z]), acc[z]);
+            }
+        }
+        if (k < kSettleChecks && k + 1 < K) {
+            const float R = fbm_reach_after(p, k);
+            unsigned st = 3u;
+            if (has) {
+#pragma unroll
+                for (int z = 0; z < S; ++z) st &= settled_bits(acc[z], R, iso);
+            }
+            if (bar_and(kBarCompute, ncomp, (int)(st & 1u))) return 2;  // blank
+            if (bar_and(kBarCompute, ncomp, (int)(st >> 1))) return 1;   // solid
+        }
+    }
+    int inside = 0, outside = 0;
+    if (has) {
+        float* out = rho + col * S;
+        unsigned below = 0;
+#pragma unroll
+        for (int z = 0; z < S; ++z) {
+            out[z] = acc[z];
+            inside |= !(acc[z] > iso);
+            outside |= !(acc[z] < iso);
+            below |= (unsigned)(acc[z] < iso) << z;
+        }
+        if (masks) masks[col] = below;
+    }
+    return inside | (outside << 1);
+}
+
+// The per-chunk z tables of S samples per edge (any S), shared by every
+// column: entries by all compute threads, then each octave's cells compacted
+// into runs by one thread.  Every compute thread calls it; it synchronises
+// the compute warps before it returns.
+__device__ __forceinline__ void ztable_serial(const DevParams& p, const ZTable Z, int S, float s, float zoff, int oz,
+                                              int ncomp)
+{
+    const int K = p.octaves;
+    for (int i = threadIdx.x; i < K * S; i += ncomp) {
+        const int k = i / S, z = i - k * S;
+        float dz, fd;
+        int cell;
+        z_entry(p, k, z, s, zoff, dz, fd, cell);
+        Z.dzc[i] = make_float2(dz, fd);
+        reinterpret_cast<int*>(Z.runs)[2 * i + 1] = cell;  // staged: cell of sample z
+        if (k == 0) Z.bias[z] = z_bias(p, z, s, oz);
+    }
+    bar_sync(kBarCompute, ncomp);
+    for (int k = threadIdx.x; k < K; k += ncomp) {
+        int2* r = Z.runs + k * S;
+        int n = 0, prev = 0;
+        for (int z = 0; z < S; ++z) {
+            const int iz = r[z].y;  // staged value; r[n] with n <= z is already consumed
+            if (z == 0 || iz != prev) r[n++] = make_int2(z, iz);
+            prev = iz;
+        }
+        Z.nruns[k] = n;
+    }
+    bar_sync(kBarCompute, ncomp);
+}
+
+// One octave of one column accumulated into out[0..S) (shared memory or a
+// per-thread buffer), the operations of sample_columns_fast; on the last
+// octave also the votes and the below-iso bits.
+__device__ __forceinline__ void column_octave_runs(const DevParams& p, const uint8_t* __restrict__ P,
+                                                   const float4* __restrict__ gp, const ZTable Z, int S, float nx,
+                                                   float ny, float norm, int k, float* out, float iso, int& inside,
+                                                   int& outside, unsigned long long& below)
+{
+    const int K = p.octaves;
+    const ColumnOctave co = column_octave(p, P, nx, ny, k, norm);
+    const float2* dzc = Z.dzc + k * S;
+    const int2* runs = Z.runs + k * S;
+    const int nr = Z.nruns[k];
+    const bool first = k == 0, last = k == K - 1;
+    // consecutive runs usually sit in consecutive z cells, whose shared
+    // plane is then read once (the condition is the same for every column)
+    float SA0 = 0.f, SG0 = 0.f, SA1 = 0.f, SG1 = 0.f;
+    int prev = 0;
+    for (int r = 0; r < nr; ++r) {
+        const int2 run = runs[r];
+        const int zb = run.x, ze = r + 1 < nr ? runs[r + 1].x : S;
+        if (r > 0 && run.y == prev + 1) {
+            SA0 = SA1;
+            SG0 = SG1;
+        } else {
+            column_face(co, gp, run.y & 255, SA0, SG0);
+        }
+        column_face(co, gp, (run.y + 1) & 255, SA1, SG1);
+        prev = run.y;
+        const RunPoly q = run_poly(SA0, SG0, SA1, SG1);
+#pragma unroll 2
+        for (int z = zb; z < ze; ++z) {
+            const float r0 = __fadd_rn(run_value(q, dzc[z]), first ? Z.bias[z] : out[z]);
+            out[z] = r0;
+            if (last) {
+                inside |= !(r0 > iso);
+                outside |= !(r0 < iso);  // a case bit stays clear
+                below |= (unsigned long long)(r0 < iso) << (z & 63);
+            }
+        }
+    }
+}
+
+// sample_columns_fast with rho in shared memory, for at most one column per
+// compute thread (planes * S <= ncomp), settling the chunk (or slab) early as
+// sample_columns_reg_settle does: then rho and masks are not complete and it
+// returns the votes of a blank (2) or a solid (1) one.  Otherwise the same
+// samples, masks and votes as sample_columns_fast.  Every compute thread must
+// call it.
+__device__ __forceinline__ int sample_columns_fast_settle(const DevParams& p, const uint8_t* __restrict__ P,
+                                                          const float4* __restrict__ gp, const ZTable Z,
+                                                          float* __restrict__ rho, int N, int ox, int oy, int oz,
+                                                          int ncomp, unsigned long long* masks, int xlo, int planes)
+{
+    const int S = N + 1, SS = planes * S, K = p.octaves;
+    const float s = __fdiv_rn((float)p.chunk_size, (float)N);
+    const float bf = p.base_freq;
+    const float norm = fbm_norm(p);
+    const float zoff = __fadd_rn((float)oz, p.offset[2]);
+    const float iso = p.iso_level;
+    ztable_serial(p, Z, S, s, zoff, oz, ncomp);
+
+    const int col = threadIdx.x;
+    const bool has = col < SS;
+    const int x = xlo + (has ? col / S : 0), y = has ? col - (col / S) * S : 0;
+    const float nx = column_coord((float)x, s, ox, p.offset[0], bf);
+    const float ny = column_coord((float)y, s, oy, p.offset[1], bf);
+    float* out = rho + (has ? col : 0) * S;
+    int inside = 0, outside = 0;
+    unsigned long long below = 0ull;
+    for (int k = 0; k < K; ++k) {
+        if (has) column_octave_runs(p, P, gp, Z, S, nx, ny, norm, k, out, iso, inside, outside, below);
+        if (k < kSettleChecks && k + 1 < K) {
+            const float R = fbm_reach_after(p, k);
+            unsigned st = 3u;
+            if (has)
+                for (int z = 0; z < S; ++z) st &= settled_bits(out[z], R, iso);
+            if (bar_and(kBarCompute, ncomp, (int)(st & 1u))) return 2;  // blank
+            if (bar_and(kBarCompute, ncomp, (int)(st >> 1))) return 1;   // solid
+        }
+    }
+    if (has && masks) masks[col] = below;
+    return inside | (outside << 1);
+}
+
 // Returns bit 0: a sample of this thread's columns is not above the iso
 // level (the early blank vote); bit 1: one is not below it (its corner bit in
 // a cell's case stays clear).
@@ -388,29 +610,7 @@ __device__ __forceinline__ int sample_columns_fast(const DevParams& p, const uin
     const float zoff = __fadd_rn((float)oz, p.offset[2]);
     const float iso = p.iso_level;
 
-    // ---- per-chunk z tables, shared by every column ----
-    for (int i = threadIdx.x; i < K * S; i += ncomp) {
-        const int k = i / S, z = i - k * S;
-        float dz, fd;
-        int cell;
-        z_entry(p, k, z, s, zoff, dz, fd, cell);
-        Z.dzc[i] = make_float2(dz, fd);
-        reinterpret_cast<int*>(Z.runs)[2 * i + 1] = cell;  // staged: cell of sample z
-        if (k == 0) Z.bias[z] = z_bias(p, z, s, oz);
-    }
-    bar_sync(kBarCompute, ncomp);
-    // compact each octave's cells into runs (one thread per octave)
-    for (int k = threadIdx.x; k < K; k += ncomp) {
-        int2* r = Z.runs + k * S;
-        int n = 0, prev = 0;
-        for (int z = 0; z < S; ++z) {
-            const int iz = r[z].y;  // staged value; r[n] with n <= z is already consumed
-            if (z == 0 || iz != prev) r[n++] = make_int2(z, iz);
-            prev = iz;
-        }
-        Z.nruns[k] = n;
-    }
-    bar_sync(kBarCompute, ncomp);
+    ztable_serial(p, Z, S, s, zoff, oz, ncomp);
 
     int inside = 0, outside = 0;
     for (int col = threadIdx.x; col < SS; col += ncomp) {
