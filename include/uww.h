@@ -245,8 +245,9 @@ typedef struct uww_tuning {
     int32_t reserved[2];
 } uww_tuning;               /* 32 bytes */
 
-/* uww_tuning.options.  NO_DEPTH_SHORTCUT: evaluate the noise of every chunk,
- * also of the chunks whose depth bias alone decides every sample (the
+/* uww_tuning.options.  NO_DEPTH_SHORTCUT: evaluate the whole noise of every
+ * chunk, also of the chunks whose depth bias alone decides every sample and
+ * of those whose first octaves already settle them as blank or solid (the
  * output does not change; for measuring the per-chunk cost of the full
  * path). */
 #define UWW_TUNE_NO_DEPTH_SHORTCUT 1u

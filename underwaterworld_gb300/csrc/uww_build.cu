@@ -434,8 +434,9 @@ __device__ void chunk_front(const DevParams& p, const BuildArgs& a, SmemTables& 
             // chunk in a global scratch slot accumulates them in local memory
             const bool in_smem = (uint32_t)N <= a.smem_cells;
             // (a chunk whose samples are not written may settle early as
-            // blank or solid, after its first octaves)
-            const bool settle = !a.samples_out && 13 * 13 <= ncomp;
+            // blank or solid, after its first octaves, unless every chunk's
+            // noise is to be evaluated)
+            const bool settle = !a.samples_out && !a.no_depth_shortcut && 13 * 13 <= ncomp;
             const int io = (in_smem && S == 13 && settle)
                                ? sample_columns_reg_settle<13>(p, T.perm, T.gp, zt, rho, ox, oy, oz, ncomp, masks)
                            : (in_smem && S == 13)
@@ -1355,9 +1356,9 @@ __device__ unsigned long long slab_front(const DevParams& p, const BuildArgs& a,
         // faster, 49 much slower: the unrolled column outgrows the caches)
         const ZTable zt = ztable_at(ztab, S, p.octaves);
         // (a slab whose samples are not written may settle early as blank or
-        // solid, after its first octaves)
+        // solid, after its first octaves, unless every noise is to be evaluated)
         const int io =
-            (!GWS && first && !a.samples_out && planes * S <= ncomp)
+            (!GWS && first && !a.samples_out && !a.no_depth_shortcut && planes * S <= ncomp)
                 ? sample_columns_fast_settle(p, T.perm, T.gp, zt, W.rho, N, ox, oy, oz, ncomp, W.masks, x0, planes)
                 : sample_columns_fast<GWS>(p, T.perm, T.gp, zt, W.rho, N, ox, oy, oz, ncomp, W.masks, x0, planes);
         inside = io & 1;
