@@ -433,13 +433,9 @@ __device__ void chunk_front(const DevParams& p, const BuildArgs& a, SmemTables& 
             // the reference's 12^3 chunk accumulates its columns in registers; a
             // chunk in a global scratch slot accumulates them in local memory
             const bool in_smem = (uint32_t)N <= a.smem_cells;
-            // (a chunk whose samples are not written may settle early as
-            // blank or solid, after its first octaves, unless every chunk's
-            // noise is to be evaluated)
-            const bool settle = !a.samples_out && !a.no_depth_shortcut && 13 * 13 <= ncomp;
-            const int io = (in_smem && S == 13 && settle)
-                               ? sample_columns_reg_settle<13>(p, T.perm, T.gp, zt, rho, ox, oy, oz, ncomp, masks)
-                           : (in_smem && S == 13)
+            // (whole chunks do not settle early: on 12^3 chunks the checks
+            // cost more than they save)
+            const int io = (in_smem && S == 13)
                                ? sample_columns_reg<13>(p, T.perm, T.gp, zt, rho, ox, oy, oz, ncomp, masks)
                            : in_smem ? sample_columns_fast<false>(p, T.perm, T.gp, zt, rho, N, ox, oy, oz, ncomp)
                                      : sample_columns_fast<true>(p, T.perm, T.gp, zt, rho, N, ox, oy, oz, ncomp, masks);
@@ -1357,9 +1353,11 @@ __device__ unsigned long long slab_front(const DevParams& p, const BuildArgs& a,
         const ZTable zt = ztable_at(ztab, S, p.octaves);
         // (a slab whose samples are not written may settle early as blank or
         // solid, after its first octaves, unless every noise is to be evaluated)
+        const bool settle = first && !a.samples_out && !a.no_depth_shortcut && p.octaves >= kSettleMinOctaves;
         const int io =
-            (!GWS && first && !a.samples_out && !a.no_depth_shortcut && planes * S <= ncomp)
-                ? sample_columns_fast_settle(p, T.perm, T.gp, zt, W.rho, N, ox, oy, oz, ncomp, W.masks, x0, planes)
+            (!GWS && planes * S <= ncomp)
+                ? sample_columns_fast_settle(p, T.perm, T.gp, zt, W.rho, N, ox, oy, oz, ncomp, W.masks, x0, planes,
+                                             settle)
                 : sample_columns_fast<GWS>(p, T.perm, T.gp, zt, W.rho, N, ox, oy, oz, ncomp, W.masks, x0, planes);
         inside = io & 1;
         outside = io >> 1;

@@ -294,6 +294,33 @@ __device__ __forceinline__ void ztable_warps(const DevParams& p, const ZTable Z,
     for (int z = threadIdx.x; z < S; z += ncomp) Z.bias[z] = z_bias(p, z, s, oz);
 }
 
+// Settling a chunk early.  After the first octaves a chunk whose every
+// partial sum stays above (below) the iso level by more than the remaining
+// octaves can reach is blank (solid) whatever they add: its other octaves are
+// not needed (its samples are not kept, so callers that write samples do not
+// settle early).  The reach is kPerlinBound |norm| sum_{k' > k} |amp_k'| (see
+// fbm_bound) and the margin covers f32 rounding as in bias_decides_with.
+// Checked after octaves 0 .. kSettleChecks-1, in fBm of at least
+// kSettleMinOctaves octaves (with fewer the checks' barriers cost more than
+// the octaves they skip).
+constexpr int kSettleChecks = 2;
+constexpr int kSettleMinOctaves = 5;
+
+__device__ __forceinline__ float fbm_reach_after(const DevParams& p, int k)
+{
+    float sa = 0.f;
+    for (int j = k + 1; j < p.octaves; ++j) sa = __fadd_rn(sa, fabsf(p.amp[j]));
+    return __fmul_rn(__fmul_rn(kPerlinBound, fabsf(fbm_norm(p))), sa);
+}
+
+// bit 0: partial sum v stays above the iso level whatever the reach R adds;
+// bit 1: it stays below
+__device__ __forceinline__ unsigned settled_bits(float v, float R, float iso)
+{
+    const float m = __fmul_rn(1.0e-3f, __fadd_rn(__fadd_rn(1.f, R), fabsf(v)));
+    return (__fsub_rn(__fsub_rn(v, R), m) > iso ? 1u : 0u) | (__fadd_rn(__fadd_rn(v, R), m) < iso ? 2u : 0u);
+}
+
 // sample_columns_fast for chunks of S samples per edge (a compile-time S <=
 // 32) in shared memory: each thread's column is accumulated in registers,
 // over a fully unrolled z loop whose run starts are uniform branches, and
@@ -349,112 +376,6 @@ __device__ __forceinline__ int sample_columns_reg(const DevParams& p, const uint
                 acc[z] = __fadd_rn(run_value(q, dzc[z]), acc[z]);
             }
         }
-        float* out = rho + col * S;
-        unsigned below = 0;
-#pragma unroll
-        for (int z = 0; z < S; ++z) {
-            out[z] = acc[z];
-            inside |= !(acc[z] > iso);
-            outside |= !(acc[z] < iso);
-            below |= (unsigned)(acc[z] < iso) << z;
-        }
-        if (masks) masks[col] = below;
-    }
-    return inside | (outside << 1);
-}
-
-// Settling a chunk early.  After the first octaves a chunk whose every
-// partial sum stays above (below) the iso level by more than the remaining
-// octaves can reach is blank (solid) whatever they add: its other octaves are
-// not needed (its samples are not kept, so callers that write samples do not
-// settle early).  The reach is kPerlinBound |norm| sum_{k' > k} |amp_k'| (see
-// fbm_bound) and the margin covers f32 rounding as in bias_decides_with.
-// Checked after octaves 0 .. kSettleChecks-1.
-constexpr int kSettleChecks = 2;
-
-__device__ __forceinline__ float fbm_reach_after(const DevParams& p, int k)
-{
-    float sa = 0.f;
-    for (int j = k + 1; j < p.octaves; ++j) sa = __fadd_rn(sa, fabsf(p.amp[j]));
-    return __fmul_rn(__fmul_rn(kPerlinBound, fabsf(fbm_norm(p))), sa);
-}
-
-// bit 0: partial sum v stays above the iso level whatever the reach R adds;
-// bit 1: it stays below
-__device__ __forceinline__ unsigned settled_bits(float v, float R, float iso)
-{
-    const float m = __fmul_rn(1.0e-3f, __fadd_rn(__fadd_rn(1.f, R), fabsf(v)));
-    return (__fsub_rn(__fsub_rn(v, R), m) > iso ? 1u : 0u) | (__fadd_rn(__fadd_rn(v, R), m) < iso ? 2u : 0u);
-}
-
-// sample_columns_reg for at most one column per compute thread (S * S <=
-// ncomp), settling the chunk early when it can: then it writes neither rho
-// nor masks and returns the votes of a blank (2: a sample not below) or a
-// solid (1: a sample not above) chunk.  Otherwise the same samples, masks and
-// votes as sample_columns_reg.  Every compute thread must call it.
-template <int S>
-__device__ __forceinline__ int sample_columns_reg_settle(const DevParams& p, const uint8_t* __restrict__ P,
-                                                         const float4* __restrict__ gp, const ZTable Z,
-                                                         float* __restrict__ rho, int ox, int oy, int oz, int ncomp,
-                                                         unsigned long long* masks = nullptr)
-{
-    constexpr int SS = S * S;
-    const int K = p.octaves;
-    const float s = __fdiv_rn((float)p.chunk_size, (float)(S - 1));
-    const float bf = p.base_freq;
-    const float norm = fbm_norm(p);
-    const float zoff = __fadd_rn((float)oz, p.offset[2]);
-    const float iso = p.iso_level;
-    ztable_warps(p, Z, S, s, zoff, oz, ncomp);
-    bar_sync(kBarCompute, ncomp);
-
-    const int col = threadIdx.x;
-    const bool has = col < SS;
-    const int x = has ? col / S : 0, y = has ? col - x * S : 0;
-    const float nx = column_coord((float)x, s, ox, p.offset[0], bf);
-    const float ny = column_coord((float)y, s, oy, p.offset[1], bf);
-    float acc[S];
-#pragma unroll
-    for (int z = 0; z < S; ++z) acc[z] = Z.bias[z];
-    for (int k = 0; k < K; ++k) {
-        if (has) {
-            const ColumnOctave co = column_octave(p, P, nx, ny, k, norm);
-            const unsigned rm = Z.rmask[k];
-            const int2* runs = Z.runs + k * S;
-            const float2* dzc = Z.dzc + k * S;
-            float SA0 = 0.f, SG0 = 0.f, SA1 = 0.f, SG1 = 0.f;
-            RunPoly q = {0.f, 0.f, 0.f, 0.f};
-            int prev = 0, r = 0;
-#pragma unroll
-            for (int z = 0; z < S; ++z) {
-                if (rm & (1u << z)) {  // the same for every column
-                    const int c = runs[r++].y;
-                    if (z > 0 && c == prev + 1) {
-                        SA0 = SA1;
-                        SG0 = SG1;
-                    } else {
-                        column_face(co, gp, c & 255, SA0, SG0);
-                    }
-                    column_face(co, gp, (c + 1) & 255, SA1, SG1);
-                    prev = c;
-                    q = run_poly(SA0, SG0, SA1, SG1);
-                }
-                acc[z] = __fadd_rn(run_value(q, dzc[z]), acc[z]);
-            }
-        }
-        if (k < kSettleChecks && k + 1 < K) {
-            const float R = fbm_reach_after(p, k);
-            unsigned st = 3u;
-            if (has) {
-#pragma unroll
-                for (int z = 0; z < S; ++z) st &= settled_bits(acc[z], R, iso);
-            }
-            if (bar_and(kBarCompute, ncomp, (int)(st & 1u))) return 2;  // blank
-            if (bar_and(kBarCompute, ncomp, (int)(st >> 1))) return 1;   // solid
-        }
-    }
-    int inside = 0, outside = 0;
-    if (has) {
         float* out = rho + col * S;
         unsigned below = 0;
 #pragma unroll
@@ -544,15 +465,15 @@ __device__ __forceinline__ void column_octave_runs(const DevParams& p, const uin
 }
 
 // sample_columns_fast with rho in shared memory, for at most one column per
-// compute thread (planes * S <= ncomp), settling the chunk (or slab) early as
-// sample_columns_reg_settle does: then rho and masks are not complete and it
-// returns the votes of a blank (2) or a solid (1) one.  Otherwise the same
-// samples, masks and votes as sample_columns_fast.  Every compute thread must
-// call it.
+// compute thread (planes * S <= ncomp): the same samples, masks and votes.
+// With settle it checks, after octaves 0 .. kSettleChecks-1, whether the
+// slab has settled: then rho and masks are not complete and it returns the
+// votes of a blank (2) or a solid (1) one.  Every compute thread must call it.
 __device__ __forceinline__ int sample_columns_fast_settle(const DevParams& p, const uint8_t* __restrict__ P,
                                                           const float4* __restrict__ gp, const ZTable Z,
                                                           float* __restrict__ rho, int N, int ox, int oy, int oz,
-                                                          int ncomp, unsigned long long* masks, int xlo, int planes)
+                                                          int ncomp, unsigned long long* masks, int xlo, int planes,
+                                                          bool settle)
 {
     const int S = N + 1, SS = planes * S, K = p.octaves;
     const float s = __fdiv_rn((float)p.chunk_size, (float)N);
@@ -572,7 +493,7 @@ __device__ __forceinline__ int sample_columns_fast_settle(const DevParams& p, co
     unsigned long long below = 0ull;
     for (int k = 0; k < K; ++k) {
         if (has) column_octave_runs(p, P, gp, Z, S, nx, ny, norm, k, out, iso, inside, outside, below);
-        if (k < kSettleChecks && k + 1 < K) {
+        if (settle && k < kSettleChecks && k + 1 < K) {
             const float R = fbm_reach_after(p, k);
             unsigned st = 3u;
             if (has)
