@@ -9,9 +9,10 @@ chunk's, bit for bit: against the F32 oracle (parity build, chunk.rs:135-264
 with perlin_util.rs:6-29), and against the single pipelined kernel, which
 builds each chunk whole (fast build).  Covered: the uneven-LOD batch
 (12^3 / 24^3 / 48^3), both dedup modes, odd sizes (17, 31 and 63 cells: the
-last slab shorter than the others), and a batch whose output exceeds the
-capacities, so that slabs find no room in the staging buffers and the
-emission kernel builds them again in place.
+last slab shorter than the others), dense slabs (more active cells than a
+slab's active-cell list holds, so that pass 1 walks the cell columns), and
+batches whose output exceeds the capacities, so that slabs find no room in
+the staging buffers and the emission kernel builds them again in place.
 """
 import os
 
@@ -52,6 +53,20 @@ def odd_sizes(seed=0, n=96):
     return p, make_descs(pos, cells)
 
 
+# a slab's active-cell list holds this many cells; a slab with more walks its
+# cell columns in pass 1 instead
+SLAB_LIST_CELLS = 2048
+
+
+def dense_slabs(seed=0):
+    """Chunks of 48, 24, 63, 17, 12 and 31 cells in a short-wavelength 6-octave
+    fBm (0.3 per world unit) with no depth bias: about 2,100 to 3,900 active
+    cells in most slabs of every size, a few below the list's capacity."""
+    p = workloads.fbm_params(seed, 6, 0.3, 0.0, 0.0, 0.0, COLOR_NORMALS)
+    pos = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [1, 1, 0], [2, 0, 0], [0, 2, 0]])
+    return p, make_descs(pos, np.array([48, 24, 63, 17, 12, 31]))
+
+
 def test_mixed_batch_takes_the_slab_build(ctx_factory):
     p, d = workloads.mixed_lod(seed=0, outputs=COLOR_NORMALS)
     ctx = ctx_factory(p)
@@ -90,6 +105,56 @@ def test_odd_sizes_bit_exact_against_the_oracle(ctx_factory, oracle):
     assert got.status == abi.UWW_OK
     assert_batches_equal(got, ref)
     assert (ref.records["flags"][d["cells"] == 63] & abi.UWW_CHUNK_HAS_MESH).sum() > 3
+
+
+@pytest.mark.parametrize("dedup", [abi.UWW_DEDUP_ORIENTED, abi.UWW_DEDUP_EDGE])
+def test_dense_slabs_bit_exact_against_the_oracle(ctx_factory, oracle, dedup):
+    p, d = dense_slabs()
+    p.dedup_mode = dedup
+    ref = oracle.build_chunks(p, d, precision=oracle.F32, threads=THREADS)
+    ctx = ctx_factory(p)
+    # the 48^3 chunk averages more active cells per slab than the list holds
+    slabs = ctx.launch_shape(1, 48).slabs_per_chunk
+    assert slabs > 1 and int(ref.records["num_active_cells"][0]) > SLAB_LIST_CELLS * slabs
+    got = ctx.build_chunks_device(d, *caps(ref))
+    assert got.status == abi.UWW_OK
+    assert_batches_equal(got, ref)
+
+
+@pytest.mark.parametrize("frac", [1.0, 0.6])
+def test_dense_slabs_match_the_pipelined_build(ctx_factory, frac):
+    """Fast build, dense slabs: byte-equal to the pipelined build; at 60 % of
+    the output's size the staging buffers run out, so the emission kernel
+    builds dense slabs again (walking their columns), and the chunks that fit
+    are identical to the full build's."""
+    p, d = dense_slabs(seed=1)
+    p.math_mode = abi.UWW_MATH_FAST
+    ctx = ctx_factory(p)
+    full = ctx.build_chunks_device(d, 1 << 20, 1 << 22)
+    assert full.status == abi.UWW_OK
+    vcap, icap = int(full.totals[0] * frac), int(full.totals[1] * frac)
+    slabs = ctx.build_chunks_device(d, vcap, icap)
+    ctx.set_tuning(options=abi.UWW_TUNE_PIPELINED)
+    piped = ctx.build_chunks_device(d, vcap, icap)
+    ctx.set_tuning(options=0)
+    if frac == 1.0:
+        assert slabs.status == abi.UWW_OK and piped.status == abi.UWW_OK
+        assert_same_bytes(slabs, piped)
+        assert_same_bytes(slabs, full)
+        return
+    assert slabs.status == abi.UWW_ERR_CAPACITY and piped.status == abi.UWW_ERR_CAPACITY
+    np.testing.assert_array_equal(slabs.records, piped.records)
+    np.testing.assert_array_equal(slabs.totals[:3], piped.totals[:3])
+    ok = (slabs.records["flags"] & abi.UWW_CHUNK_OVERFLOW) == 0
+    assert ok[0] and (~ok).sum() > 0
+    rec = full.records
+    for i in np.nonzero(ok & (rec["num_inds"] > 0))[0]:
+        v0, nv = rec["vert_offset"][i], rec["num_verts"][i]
+        i0, ni = rec["ind_offset"][i], rec["num_inds"][i]
+        np.testing.assert_array_equal(slabs.inds[i0:i0 + ni], full.inds[i0:i0 + ni])
+        np.testing.assert_array_equal(slabs.verts[v0:v0 + nv].view(np.uint32), full.verts[v0:v0 + nv].view(np.uint32))
+        np.testing.assert_array_equal(slabs.normals[v0:v0 + nv].view(np.uint32),
+                                      full.normals[v0:v0 + nv].view(np.uint32))
 
 
 @pytest.mark.parametrize("seed", [0, 5])
