@@ -178,9 +178,14 @@ int   uww_ctx_sync(uww_ctx* ctx);
 
 /* ---- chunk builds ------------------------------------------------------------ */
 /* Batched build (replaces World's one-chunk-per-frame loop over Chunk::build_partial,
- * world.rs:113-145): every chunk in one persistent launch fed by a device work
- * queue.  d_chunks and out are device memory; max_cells bounds desc.cells.
- * Asynchronous; read out->totals or records after uww_ctx_sync(). */
+ * world.rs:113-145): every chunk in one call -- a planning kernel, a persistent
+ * kernel fed by device work queues and an emission kernel, chained on the
+ * context's stream (uww_launch_shape_of names the build a batch takes).
+ * d_chunks and out are device memory; max_cells bounds desc.cells and sizes
+ * the context's work buffers, which grow to the largest batch (chunks above 16
+ * cells: max_cells^2 words of slab seam per slab place); a failed allocation
+ * returns UWW_ERR_OOM.  Asynchronous; read out->totals or records after
+ * uww_ctx_sync(). */
 int uww_build_chunks(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n,
                      uint32_t max_cells, const uww_mesh_out* out);
 
