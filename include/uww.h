@@ -237,12 +237,14 @@ int uww_build_chunks_host(uww_ctx* ctx, const uww_chunk_desc* h_chunks, uint32_t
 /* ---- tuning (written by the autotuner; 0 = automatic) ------------------------ */
 typedef struct uww_tuning {
     int32_t threads;        /* compute threads per CTA (multiple of 32, <= 192 or 224..512); the
-                               batched build adds one control warp                          */
+                               pipelined build adds one control warp                        */
     int32_t blocks_per_sm;  /* resident CTAs per SM of the persistent grid                   */
     int32_t smem_cells;     /* chunks up to this many cells per edge work in shared memory;
-                               larger ones use a global scratch slot per CTA                */
+                               larger ones are built as x slabs (split build) or in a
+                               global scratch slot per CTA (pipelined build)                */
     int32_t spin_limit;     /* bound, in SM clock cycles, on each device-side wait of the
-                               batched build (the prefix-sum look-back); 0 = the default,
+                               batched builds (the pipelined build's prefix-sum look-back,
+                               the split build's wait for the records); 0 = the default,
                                4e9 cycles (about 2 s).  A wait that runs out raises
                                UWW_ERRFLAG_TIMEOUT and the build finishes without it      */
     uint32_t test_flags;    /* UWW_TEST_*: failure injection for tests; 0 in normal use      */
@@ -258,10 +260,12 @@ typedef struct uww_tuning {
 #define UWW_TUNE_NO_DEPTH_SHORTCUT 1u
 /* PIPELINED: build every batch with the single pipelined kernel (look-back
  * prefix sum, one CTA emits the chunks it sampled).  By default a batch whose
- * chunks all fit one shared-memory workspace (<= 256 compute threads, no
- * streamed host output, no failure injection) is built in two kernels
- * instead: the front half of every chunk, then the emission of every
- * triangle of the batch.  Both give the same output. */
+ * chunks all fit one shared-memory workspace (<= 256 compute threads), or
+ * whose chunks above 16 cells per edge (up to 63) can be built as x slabs of
+ * a few cell layers, with no streamed host output, no samples read in and no
+ * look-back failure injection, takes the split build instead: a planning
+ * kernel, the front half of every chunk or slab, then the emission of every
+ * vertex and index of the batch.  Both give the same output. */
 #define UWW_TUNE_PIPELINED 2u
 
 /* Failure injection (uww_tuning.test_flags).  WITHHOLD_FIRST: the first chunk
