@@ -307,8 +307,8 @@ int uww_autotune(uww_ctx* ctx, const uww_chunk_desc* d_chunks, uint32_t n, uint3
  * for diagnostics and tests (no counterpart in the reference): the build
  * (UWW_BUILD_SPLIT: planning, front and emission kernels; UWW_BUILD_PIPELINED:
  * the single persistent kernel), the most x slabs a chunk is built as (1:
- * every chunk whole; chunks above 16 cells per edge are built as slabs of a
- * few cell layers by the split build of a planned batch), the compute threads
+ * every chunk whole; the split build builds chunks of 17 to 63 cells per edge
+ * as slabs of a few cell layers), the compute threads
  * per CTA, the (front) kernel's grid, its resident CTAs per SM and its dynamic
  * shared memory.  It assumes per-cell cases and samples are written exactly
  * when the parameters' outputs ask for them. */
