@@ -489,7 +489,8 @@ def leg_frame_graph(ctx, params, descs, steps, warmup):
 
 def leg_mixed_lod(stream, flush, steps, warmup):
     """Uneven LOD batch (2048 chunks, 12^3/24^3/48^3 at 50/35/15 %, 6-octave fBm)
-    in one persistent launch, autotuned (cached per config); p50/p99 latency."""
+    in one build call (the split build: its 24^3 and 48^3 chunks as x slabs),
+    autotuned (cached per config); p50/p99 latency."""
     import torch
     from underwaterworld_gb300 import abi, workloads
     from underwaterworld_gb300.chunk import Context
