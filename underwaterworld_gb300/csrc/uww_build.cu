@@ -38,6 +38,18 @@
 // the control warp of each listed chunk writes the records of the decided
 // chunks that follow it (their offsets are its inclusive prefix).  A decided
 // chunk thus costs a record write, not a ticket.
+//
+// Split form (the default batched build; the pipelined form above remains for
+// samples read in, streamed host output and when asked for): three kernels,
+// each the programmatic dependent of the one before.  split_plan_kernel
+// decides what the depth bias decides and queues the rest, largest first;
+// front_kernel (persistent, every thread a compute thread) runs steps 1-2 and
+// pass 1 of each queued chunk into staging buffers and adds the chunk's counts
+// to its tile's sum -- no look-back; emit_kernel writes the records from the
+// tile sums, then takes blocks of staged vertices (pass 2) and of indices and
+// stores them at their final offsets.  Chunks of 17..63 cells per edge are
+// queued as x slabs of a few cell layers, one CTA each; a slab refers to the
+// vertices of the previous slab's last layer through that slab's seam.
 #include <cuda_runtime.h>
 
 #include <algorithm>
