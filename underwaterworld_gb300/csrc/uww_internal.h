@@ -52,7 +52,7 @@ __host__ __device__ inline ChunkLayout chunk_layout(int N)
 // cell | first triangle << 16) that spreads pass 1 over the CTA.  K is
 // the largest layer count whose sample columns ((K+1) * S) fit one pass of the
 // CTA's threads, whose workspace fits kSlabBudget bytes, and whose vertices fit
-// 16-bit ids (every edge of the slab's cells, counted once).
+// 16-bit ids (slab_vertex_bound).
 constexpr int kSlabThreads = 256;
 constexpr uint32_t kSlabBudget = 96 * 1024;
 constexpr uint32_t kSlabActCap = 2048;
@@ -79,15 +79,27 @@ __host__ __device__ inline SlabLayout slab_layout_k(int N, int K)
     return L;
 }
 
+// The most vertices a slab of K layers of an N-cell chunk can create, in
+// either dedup mode: with one vertex per cube edge, every edge of its cells
+// once, K S^2 + 2 (K+1) N S; with one per ordered corner pair (the
+// reference's), the cells on either side of an x or a z edge list it with
+// opposite corner order, so those edges can carry two vertices and y edges
+// one, (5K+1) N S -- the larger.  Both are reached when every edge is crossed.
+__host__ __device__ inline long long slab_vertex_bound(int N, int K)
+{
+    const long long S = N + 1;
+    const long long edges = (long long)K * S * S + 2ll * (K + 1) * N * S;
+    const long long oriented = (5ll * K + 1) * N * S;
+    return edges > oriented ? edges : oriented;
+}
+
 __host__ __device__ inline int slab_layers(int N)
 {
     const int S = N + 1;
     int K = kSlabThreads / S - 1;
     if (K > N) K = N;
-    for (; K > 1; --K) {
-        const long long edges = (long long)K * S * S + 2ll * (K + 1) * N * S;
-        if (slab_layout_k(N, K).total <= kSlabBudget && edges < 65536) break;
-    }
+    for (; K > 1; --K)
+        if (slab_layout_k(N, K).total <= kSlabBudget && slab_vertex_bound(N, K) < 65536) break;
     return K < 1 ? 1 : K;
 }
 
