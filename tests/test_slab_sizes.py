@@ -88,3 +88,11 @@ def test_every_slab_size_fits_its_limits(sizes):
         assert K * N * N < 1 << 16, N
         assert vbound == vertex_bound(N, K) and vbound < 1 << 16, N
         assert count == -(-N // K) and (count - 1) * K < N <= count * K, N
+        # a staged reference into the previous slab: bit 31, the owner's edge
+        # in bits 24..27, its cell's y * N + z below them
+        assert N * N < 1 << 24, N
+        # queue entry: chunk | slab << 24
+        assert count < 1 << 8, N
+    # an active-cell list entry: the cell's first triangle in 16 bits (at most
+    # 5 triangles a cell, and the list holds act_cap cells)
+    assert 5 * sizes["act_cap"] < 1 << 16
